@@ -1,0 +1,326 @@
+#!/usr/bin/env python3
+"""Benchmark of the per-stage RHS on the gas-gas triple point, 7168 x 3072 cells.
+
+Workload (the headline configuration): fluid 1 gamma 1.5 for x < 1 and for x >= 1, y >= 1.5,
+fluid 2 gamma 1.4 for x >= 1, y < 1.5, both p_inf = 0, on [0,7] x [0,3] with 7168 x 3072 cells and
+5 ghost layers; slip (reflective) walls on all four sides; SC scheme with MP5 + THINC +
+central-6 reconstruction; CFL 0.4. Data are synthetic (the analytic initial state; the reference
+publishes no dataset). A step is one SSP-RK3 step = three RHS stages over the whole grid.
+
+Reported (one JSON line from rank 0):
+  value        Mcell-stage/s over all ranks, device-timed with CUDA events around K steps whose
+               state (1.8 GB) is already in HBM; the state is larger than L2, so no flush is needed.
+  e2e          the same metric through the C ABI with the state in pinned host memory: every
+               step copies the ten cell arrays host->device, runs the step and copies them back.
+  roofline     algorithmic bytes of a stage (128 B per cell-stage: read the stage state and the
+               step-start state, write the new state, averaged over the three stages) divided by
+               the measured stage time, against the measured HBM copy bandwidth.
+  fp64         the face-sweep kernels' binary64 throughput against the device's measured FP64
+               FMA peak (GB300's FP64 rate bounds the plain form, not HBM).
+  cpu_baseline the CPU oracle (C restatement of the reference kernels, OpenMP on every host core)
+               on a bounded sample of the same workload.
+With --impl reference the script times that CPU implementation alone (the reference's own path is
+NVIDIA Warp, which is not installable here) and prints its line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "wave-multiphase_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+WORKLOAD = "triple_point_7168x3072"
+NX, NY, G = 7168, 3072, 5
+ALG_BYTES_PER_CELL_STAGE = 128.0     # read stage state + step-start state, write new state (avg)
+SAMPLE_NX, SAMPLE_NY = 3584, 1536    # CPU sample: a quarter of the cells of the same problem
+# Face-sweep binary64 work per face (x or y) and traffic per cell-stage, from the ncu captures
+# summarised in profiles/ (None until measured).
+FP64_FLOP_PER_FACE = None
+DRAM_BYTES_PER_CELL_STAGE = None
+
+
+def params(nx=NX, ny=NY):
+    import wavemp
+
+    return wavemp.SolverParams(dx=7.0 / nx, dy=3.0 / ny, gamma1=1.5, pinf1=0.0, gamma2=1.4,
+                               pinf2=0.0, variant="sc", recon="mp5c6", bc=("slip",) * 4, cfl=0.4)
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------------------ clocks ------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.gpu = gpu_index
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------------------- CPU oracle -------
+def cpu_oracle_rate(nx, ny, steps=None, seconds=12.0):
+    """Mcell-stage/s of the CPU oracle (all host cores) on the same problem at nx x ny."""
+    import numpy as np
+
+    import wavemp
+    from oracle import oracle as orc
+
+    st = wavemp.ic.triple_point(nx, ny, device="cpu")
+    P = orc.make_params(7.0 / nx, 3.0 / ny, 1.5, 0.0, 1.4, 0.0, variant=orc.SC, recon=orc.MP5C6,
+                        bc=[orc.SLIP] * 4, cfl=0.4)
+    o = orc.PackedOracle(nx, ny, P)
+    for c, k in enumerate(orc.ALL10):
+        o.fields[c][...] = st[k].numpy()
+    o.init_sequence()
+    dt = o.get_dt()
+    dt = o.steps(1, dt)  # warm-up step (page-in, thread start)
+    done, t0 = 0, time.perf_counter()
+    while True:
+        dt = o.steps(1, dt)
+        done += 1
+        el = time.perf_counter() - t0
+        if (steps is not None and done >= steps) or (steps is None and el >= seconds):
+            break
+    assert np.isfinite(dt)
+    return nx * ny * 3 * done / el / 1e6, done, el
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle import oracle as orc
+
+    orc.build()
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    rate_w, _, _ = cpu_oracle_rate(SAMPLE_NX, SAMPLE_NY, steps=max(args.warmup, 1))
+    rate, steps, el = cpu_oracle_rate(SAMPLE_NX, SAMPLE_NY, steps=args.steps)
+    sample = (f"{SAMPLE_NX}x{SAMPLE_NY} cells of the same problem (a quarter of the cells), "
+              f"{steps} SSP-RK3 steps after {max(args.warmup, 1)} warm-up")
+    line = {
+        "impl": "reference", "metric": "Mcell-stage/s", "value": round(rate, 3),
+        "unit": "Mcell-stage/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(el / steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "sampled_as": f"{SAMPLE_NX}x{SAMPLE_NY}",
+                   "scheme": "SC, MP5 + THINC + central-6", "form": "plain binary64",
+                   "step": "one SSP-RK3 step (3 RHS stages)"},
+        "cpu_baseline": {"value": round(rate, 3), "unit": "Mcell-stage/s", "cores": int(os.environ["OMP_NUM_THREADS"]),
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": round(rate, 3), "unit": "Mcell-stage/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": "the reference's own path is NVIDIA Warp (not installable offline); the CPU oracle "
+                "restates its kernels and is pinned bit-exact to the reference's kernel source",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------------------ GPU ---------
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import wavemp
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    fp64_peak = wavemp.probe_fp64_flops()
+    s = wavemp.Solver(params(), NX, NY)
+    q = wavemp.ic.triple_point(NX, NY, device=dev)
+    old = wavemp.alloc_state(NX, NY, names=wavemp.FIELDS, device=dev)
+    s.initialize(q)
+    s.init_dt(q)
+    for _ in range(args.warmup):
+        s.step(q, old, None, sync=False)
+    torch.cuda.synchronize()
+
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local)
+    time.sleep(0.4)
+    s.profile(True)
+    s.profile_read(reset=True)
+    barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        s.step(q, old, None, sync=False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    prof = s.profile_read(reset=True)
+    s.profile(False)
+    clk = clocks.stop()
+    dt_now = s.get_dt(q)
+    finite = all(bool(torch.isfinite(q[k]).all()) for k in wavemp.FIELDS) and dt_now > 0
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    cells = NX * NY
+    value = cells * 3 * args.steps * world / (ms * 1e-3) / 1e6
+    ms_step = ms / args.steps
+    launches = sum(n for _, n in prof.values())
+
+    # ---- end to end through the C ABI with host buffers ----
+    host = {k: torch.empty((NX + 2 * G, NY + 2 * G), dtype=torch.float64, pin_memory=True)
+            for k in wavemp.ALL}
+    for k in wavemp.ALL:
+        host[k].copy_(q[k])
+    torch.cuda.synchronize()
+    ke = max(2, args.steps // 2)
+    h2d = sum(t.numel() * 8 for t in host.values())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(ke):
+        for k in wavemp.ALL:
+            q[k].copy_(host[k], non_blocking=True)
+        s.step(q, old, None, sync=False)
+        for k in wavemp.ALL:
+            host[k].copy_(q[k], non_blocking=True)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    ms_e2e = max(f0.elapsed_time(f1), wall * 1e3)
+    if world > 1:
+        t = torch.tensor([ms_e2e], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+    e2e_value = cells * 3 * ke * world / (ms_e2e * 1e-3) / 1e6
+
+    # ---- roofline and FP64 rate ----
+    hbm, hbm_kind = measured_peaks()
+    stage_ms = ms_step / 3.0
+    achieved = ALG_BYTES_PER_CELL_STAGE * cells / (stage_ms * 1e-3) / 1e9
+    face_ms, face_n = prof["faces"]
+    face_ms_per_launch = face_ms / max(face_n, 1)
+    faces_per_stage = (NX + 1) * NY + NX * (NY + 1)
+    fp64 = {"peak": round(fp64_peak / 1e12, 4), "unit": "TFLOP/s", "peak_kind": "measured (DFMA loop)",
+            "face_sweep_ms_per_stage": round(face_ms / max(face_n / 2, 1), 3)}
+    if FP64_FLOP_PER_FACE:
+        fl = FP64_FLOP_PER_FACE * faces_per_stage / (face_ms / max(face_n / 2, 1) * 1e-3)
+        fp64.update({"achieved": round(fl / 1e12, 4), "frac": round(fl / fp64_peak, 4)})
+    roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
+            "frac": round(achieved / hbm, 5), "peak_kind": hbm_kind,
+            "traffic": (round(DRAM_BYTES_PER_CELL_STAGE * cells / 1e9, 3) if DRAM_BYTES_PER_CELL_STAGE else None),
+            "unit_of_work": "one RHS stage over all cells (128 B algorithmic per cell-stage)",
+            "stage_ms": round(stage_ms, 3)}
+
+    kernels = {g: {"ms_per_launch": round(t / max(n, 1), 4), "launches": n,
+                   "share": round(t / max(sum(v[0] for v in prof.values()), 1e-9), 4)}
+               for g, (t, n) in prof.items()}
+    line = {
+        "metric": "Mcell-stage/s", "value": round(value, 3), "unit": "Mcell-stage/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "ghost": G,
+                   "scheme": "SC, MP5 + THINC + central-6", "form": "plain binary64",
+                   "bc": "slip walls on four sides", "step": "one SSP-RK3 step (3 RHS stages)",
+                   "l2": "state of 1.8 GB is larger than L2; no flush", "parallelism": "replicas"},
+        "roofline": roof, "fp64": fp64,
+        "e2e": {"value": round(e2e_value, 3), "unit": "Mcell-stage/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": h2d, "steps": ke},
+        "gpu_launches": launches, "kernels": kernels, "clocks": clk, "finite": finite,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+        rate, steps, el = cpu_oracle_rate(SAMPLE_NX, SAMPLE_NY, seconds=12.0)
+        line["cpu_baseline"] = {"value": round(rate, 3), "unit": "Mcell-stage/s",
+                                "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
+                                "sample": f"{SAMPLE_NX}x{SAMPLE_NY} cells of the same problem, "
+                                          f"{steps} SSP-RK3 steps in {el:.1f} s"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        print("note: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,182 @@
+/*
+ * wavemp.h -- C ABI of the GB300 (sm_103a) implementation of the per-stage right-hand side of the
+ * 2-D five-equation stiffened-gas solver of aschamarthi/Wave-Multiphase.
+ *
+ * The reference (sainath_SC_it_works.py "SC", Sainath_M10.py "M10") has no library interface; its
+ * RHS is a set of Warp kernels driven by closures inside main() (SC:1894-1995). Each entry point
+ * below replaces one of those closures with the same argument meaning and the same array layout,
+ * so a host loop written like the reference's time loop (SC:2009-2082) can call them in the same
+ * order. The fused entry points (wm_rhs_stage, wm_step) run the same sequence with fewer passes
+ * over memory.
+ *
+ * Conventions (as in the reference):
+ *  - Every field is a double array of (nx + 2g) rows by (ny + 2g) columns: x index i is the row,
+ *    y index j is contiguous; row i starts at ptr + i * pitch (pitch >= ny + 2g, in elements).
+ *    Interior cells are i in [g, g+nx), j in [g, g+ny). g >= 4 (the reference uses g = 5).
+ *  - The caller owns every field array. The handle owns (or is given) the workspace: face fluxes,
+ *    limiter factors, per-cell sensors and the time-step accumulator.
+ *  - All device work is enqueued on the caller's stream (a cudaStream_t passed as void*; NULL is
+ *    the legacy default stream) and returns without waiting, except where a host value is
+ *    requested (wm_get_dt, and wm_step with dt_next != NULL).
+ *  - Return codes: WM_OK (0) or a negative WM_ERR_*; no exception crosses the ABI. One handle per
+ *    stream at a time: a handle is not safe for concurrent use from several streams or threads.
+ */
+#ifndef WAVEMP_H
+#define WAVEMP_H
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WM_OK 0
+#define WM_ERR_INVALID (-1) /* bad argument: null pointer, size, enum, pitch, alignment */
+#define WM_ERR_CUDA (-2)    /* a CUDA runtime call failed; see wm_last_error() */
+#define WM_ERR_NOMEM (-3)   /* device allocation failed or caller workspace too small */
+#define WM_ERR_STATE (-4)   /* call out of order (e.g. limit_fluxes before compute_fluxes) */
+
+/* Scheme variant: which reference script's face kernel (fx_kernel / gy_kernel) is followed. */
+#define WM_VARIANT_SC 0  /* SC:966-1301: Ducros-gated central shear, THINC under the indicator */
+#define WM_VARIANT_M10 1 /* M10:868-1222: THINC always on the interface field, Wong staged limiter
+                            on reconstructed states and a pressure floor */
+
+/* Reconstruction of the characteristic fields. */
+#define WM_RECON_SHIPPED 0 /* MUSCL kappa=1/3 (SC:430-446), central-4 shear (SC:1076-1082) */
+#define WM_RECON_MP5C6 1   /* MP5 (SC:353-405) where the shipped code uses MUSCL, central-6
+                              (SC:407-412) where it uses central-4 */
+
+/* Ghost-cell rule per side (bc_x_kernel / bc_y_kernel, SC:1616-1682). */
+#define WM_BC_TRANSMISSIVE 0 /* copy the nearest interior cell */
+#define WM_BC_SLIP 1         /* copy it and negate the wall-normal momentum and velocity */
+
+/* Arithmetic of the face sweeps. */
+#define WM_PREC_FP64 0 /* plain form: everything in binary64 */
+#define WM_PREC_FP32 1 /* precision form: reconstruction and fluxes in binary32; pressure and
+                          sound-speed recovery, the limiter's bound solves and the conserved-state
+                          accumulation in binary64 */
+
+typedef struct wm_params {
+    double gamma1, pinf1; /* stiffened gas of fluid 1 (alpha1 = its volume fraction) */
+    double gamma2, pinf2; /* fluid 2 */
+    double dx, dy;        /* uniform cell sizes */
+    double cfl;           /* CFL number of get_dt (SC:33) */
+    int variant;          /* WM_VARIANT_* */
+    int recon;            /* WM_RECON_* */
+    int bc[4];            /* x-low, x-high, y-low, y-high: WM_BC_* */
+    int emergency_repair; /* USE_EMERGENCY_REPAIR (SC:37): run enforce_admissible every stage */
+    int precision;        /* WM_PREC_* */
+} wm_params;
+
+/* The reference's ten per-cell arrays (SC:1839-1841): conserved state, primitives, al_prim. */
+typedef struct wm_fields {
+    double *ar1, *ar2; /* partial densities alpha1*rho1, alpha2*rho2 */
+    double *ru, *rv;   /* momenta */
+    double *E;         /* total energy */
+    double *al;        /* alpha1 (conserved copy, clamped by update_prims) */
+    double *u_p, *v_p, *p_p; /* primitives written by update_prims */
+    double *al_prim;   /* alpha1 snapshot used by the non-conservative source */
+    long long pitch;   /* elements between consecutive x rows */
+} wm_fields;
+
+/* Counters read back by wm_status (device-side, cumulative since wm_create or wm_reset_status). */
+typedef struct wm_stats {
+    long long repaired_cells;   /* cells whose energy enforce_admissible reset */
+    long long nonfinite_cells;  /* cells with a NaN partial density, momentum or energy before
+                                   repair */
+    long long limited_cells;    /* interior cells with a limiter factor theta < 1 in any pass */
+    long long steps;            /* SSP-RK3 steps run through wm_step */
+} wm_stats;
+
+typedef struct wm_handle wm_handle;
+
+/* Library version string and the last CUDA error message seen by any entry point. */
+const char *wm_version(void);
+const char *wm_last_error(void);
+
+/* Bytes of device workspace a handle needs for this grid and parameter set. */
+size_t wm_workspace_bytes(const wm_params *p, int nx, int ny, int g);
+
+/* Create a handle. With workspace == NULL the library allocates the workspace (cudaMalloc on the
+ * current device); otherwise it uses the caller's device buffer of workspace_bytes >=
+ * wm_workspace_bytes(), 256-byte aligned, which must outlive the handle. Replaces the buffer
+ * allocations of main() (SC:1843-1866). */
+int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t workspace_bytes,
+              wm_handle **out);
+void wm_destroy(wm_handle *h);
+
+/* ---- the reference's closures (SC:1894-1995), one call each ------------------------------- */
+/* apply_bc() SC:1899-1905: fill the g ghost layers of the nine cell arrays (not al_prim). */
+int wm_apply_bc(wm_handle *h, const wm_fields *q, void *stream);
+/* compute_fluxes() SC:1919-1935: Ducros sensor (SC only) and the high-order x and y face fluxes
+ * with the interface velocities, into the handle's workspace. */
+int wm_compute_fluxes(wm_handle *h, const wm_fields *q, void *stream);
+/* compute_low_fluxes() SC:1937-1947: first-order HLLC face fluxes into the workspace. */
+int wm_compute_low_fluxes(wm_handle *h, const wm_fields *q, void *stream);
+/* limit_fluxes(dt) SC:1949-1972: three Wong limiter passes blending the high-order fluxes toward
+ * the first-order ones in place. */
+int wm_limit_fluxes(wm_handle *h, const wm_fields *q, double dt, void *stream);
+/* rk3_update(alpha, beta, dt) SC:1974-1984: q = alpha*q_old + beta*(q - dt*R) on interior cells. */
+int wm_rk3_update(wm_handle *h, const wm_fields *q, const wm_fields *q_old, double alpha,
+                  double beta, double dt, void *stream);
+/* enforce_admissible() SC:1907-1911 (a no-op when emergency_repair is 0). */
+int wm_enforce_admissible(wm_handle *h, const wm_fields *q, void *stream);
+/* update_prims() SC:1913-1917: clamp alpha1, recover u, v, p, copy al_prim <- al. */
+int wm_update_prims(wm_handle *h, const wm_fields *q, void *stream);
+/* copy_old() SC:1894-1897: q_old <- q for the six conserved arrays (whole padded arrays). */
+int wm_copy_old(wm_handle *h, const wm_fields *q, const wm_fields *q_old, void *stream);
+/* get_dt() SC:1986-1995: CFL * min over interior cells of the acoustic time step. Blocks until
+ * the value is on the host, as the reference does. */
+int wm_get_dt(wm_handle *h, const wm_fields *q, double *dt, void *stream);
+
+/* ---- fused forms ---------------------------------------------------------------------------- */
+/* One SSP-RK3 stage: apply_bc, compute_fluxes, compute_low_fluxes, limit_fluxes(dt),
+ * rk3_update(alpha, beta, dt), enforce_admissible, update_prims -- the body of SC:2030-2055.
+ * q_old may be NULL when alpha == 0. */
+int wm_rhs_stage(wm_handle *h, const wm_fields *q, const wm_fields *q_old, double dt, double alpha,
+                 double beta, void *stream);
+/* One SSP-RK3 step (SC:2033-2059): copy_old, three stages with (alpha, beta) = (0,1), (3/4,1/4),
+ * (1/3,2/3), then get_dt. If dt > 0 it is the step's dt; if dt <= 0 the step uses the dt the
+ * handle computed at the end of the previous wm_step (or by wm_get_dt / wm_init_dt). The next dt
+ * stays on the device; if dt_next != NULL the call also waits for it and stores it there. */
+int wm_step(wm_handle *h, const wm_fields *q, const wm_fields *q_old, double dt, double *dt_next,
+            void *stream);
+/* Compute the time step of the current state on the device (no host wait) for the next wm_step
+ * with dt <= 0. */
+int wm_init_dt(wm_handle *h, const wm_fields *q, void *stream);
+
+/* ---- diagnostics ---------------------------------------------------------------------------- */
+/* Copy workspace array `which` (WM_WS_*) of the padded grid into the caller's device buffer dst
+ * (same padded shape, contiguous rows of ny + 2g). */
+#define WM_WS_FX 0      /* 7 arrays: high-order x fluxes 0..5 and srcx (after limit_fluxes: blended) */
+#define WM_WS_GY 7      /* 7 arrays: y fluxes and srcy */
+#define WM_WS_FXL 14    /* 7 arrays: first-order x fluxes and srcxl */
+#define WM_WS_GYL 21    /* 7 arrays: first-order y fluxes and srcyl */
+#define WM_WS_THETA 28  /* 3 arrays: cell limiter factor of pass 0, 1, 2 */
+#define WM_WS_SIGMA_X 31
+#define WM_WS_SIGMA_Y 32
+#define WM_WS_COUNT 33
+int wm_read_workspace(wm_handle *h, int which, double *dst, void *stream);
+/* Read (and optionally reset) the device counters; blocks on the stream. */
+int wm_status(wm_handle *h, wm_stats *out, int reset, void *stream);
+
+/* Kernel-group timing with CUDA events recorded on the launching stream around each group of
+ * launches (ghost fill, per-cell preparation, face sweeps, limiter, combine). Off by default;
+ * while on, every stage records two events per group. wm_profile_read waits for the recorded
+ * events and returns, per group, the summed milliseconds and the number of kernel launches. */
+#define WM_PROF_BC 0
+#define WM_PROF_PREP 1
+#define WM_PROF_FACES 2
+#define WM_PROF_LIMITER 3
+#define WM_PROF_FINAL 4
+#define WM_PROF_GROUPS 5
+int wm_profile(wm_handle *h, int enable);
+int wm_profile_read(wm_handle *h, double ms[WM_PROF_GROUPS], long long launches[WM_PROF_GROUPS],
+                    int reset);
+
+/* Measured FP64 FMA throughput of the current device in FLOP/s (a short on-device loop). */
+int wm_probe_fp64_flops(double *flops, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

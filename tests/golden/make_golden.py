@@ -363,15 +363,15 @@ def perturb(runner, rng, g1, p1, g2, p2, amp=0.05):
     a["u_p"][...], a["v_p"][...], a["p_p"][...] = u, v, p
 
 
-def stress_ic(runner, rng, g1, p1, g2, p2, vel, pmin, margin, flip_frac=0.3):
+def stress_ic(runner, rng, g1, p1, g2, p2, vel, pmin, margin, flip_frac=0.3, ar1_exp=(-13, -7)):
     """Near-vacuum, rough state that drives all three Wong limiter passes and the repairs.
 
-    Fluid-1 partial density 1e-13..1e-7, alpha within 1e-6 of 0 or 1, random velocities and
+    Fluid-1 partial density 10^ar1_exp (default 1e-13..1e-7), alpha within 1e-6 of 0 or 1, random velocities and
     pressures; cells that are mostly fluid 1 get a pressure close to -pinf_1 (small rho c~^2).
     """
     a = runner.a
     sh = a["al"].shape
-    ar1 = 10 ** rng.uniform(-13, -7, sh)
+    ar1 = 10 ** rng.uniform(ar1_exp[0], ar1_exp[1], sh)
     ar2 = np.abs(1.2 * (1 + 0.3 * rng.standard_normal(sh))) + 0.05
     al = 10 ** rng.uniform(-9.5, -6, sh)
     flip = rng.uniform(size=sh) < flip_frac
@@ -450,6 +450,10 @@ def run_case(name, ref_dir, out_dir):
         meta = dict(variant=variant, recon=recon, g1=g1, p1=p1, g2=g2, p2=p2,
                     steps=1 if name.endswith("rand") else 2)
     elif name in ("sc_mp5c6_stress", "m10_stress"):
+        # m10_stress is not part of the fixture set: M10's staged limiter switches hard at
+        # partial densities of 1e-11 (SC:233-237) and such near-vacuum states flip those
+        # switches under 1e-15 input noise, so the reference's own output is not reproducible
+        # to round-off there. It stays generable for inspection.
         variant = "m10" if name.startswith("m10") else "sc"
         recon = "mp5c6" if "mp5c6" in name else "shipped"
         mod = load_reference(m10 if variant == "m10" else sc, recon)
@@ -612,7 +616,7 @@ def run_units(ref_dir, out_dir):
 
 
 ALL_CASES = ("sc_ref_ic", "m10_ref_ic", "sc_cfg0", "sc_mp5c6_cfg0", "sc_mp5c6_rand",
-             "m10_cfg2", "m10_mp5c6_rand", "sc_mp5c6_triple", "sc_mp5c6_stress", "m10_stress")
+             "m10_cfg2", "m10_mp5c6_rand", "sc_mp5c6_triple", "sc_mp5c6_stress")
 
 
 def main():

@@ -1,0 +1,153 @@
+"""GPU parity of the CUDA RHS against the reference (golden vectors) and the CPU oracle.
+
+Every closure of the reference's stage (apply_bc, compute_fluxes, compute_low_fluxes,
+limit_fluxes, rk3_update, enforce_admissible, update_prims) is run through the C ABI on the
+golden inputs and compared with the arrays the reference's own kernels produced, at the FP64
+tolerance of 1e-10 relative in natural units (parity_util). The fused stage must equal the closure
+sequence bit for bit, and whole SSP-RK3 steps must match the reference's within 1e-9: two steps
+amplify round-off, and the reference's own output moves by up to 7e-11 under 1e-15 input noise
+(test_oracle_golden.test_cases_are_well_conditioned bounds that by 1e-10).
+"""
+import numpy as np
+import pytest
+
+import parity_util as pu
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA device", allow_module_level=True)
+
+import wavemp  # noqa: E402
+from wavemp import Solver, alloc_state  # noqa: E402
+
+
+def make_solver(d, **over):
+    return Solver(pu.params_from(d, **over), int(d["meta_nx"]), int(d["meta_ny"]), int(d["meta_g"]))
+
+
+def load_state(d, prefix):
+    nx, ny, g = int(d["meta_nx"]), int(d["meta_ny"]), int(d["meta_g"])
+    q = alloc_state(nx, ny, g)
+    for k in pu.ALL:
+        q[k].copy_(torch.from_numpy(np.ascontiguousarray(d[prefix + k])))
+    return q
+
+
+@pytest.fixture(scope="module", params=pu.CASES)
+def case(request):
+    return request.param, pu.load_case(request.param)
+
+
+RTOL_STEPS = 1e-9
+
+
+def got_of(q):
+    return {k: pu.host(v) for k, v in q.items()}
+
+
+def test_closures_match_reference(case):
+    name, d = case
+    sc = pu.case_scales(d)
+    fsc = sc["flux"]
+    s = make_solver(d)
+    q = load_state(d, "in_")
+    q_old = alloc_state(s.nx, s.ny, s.g, names=pu.FIELDS)
+    dt = float(d["dt0"])
+    s.copy_old(q, q_old)
+    s.apply_bc(q)
+    for k in pu.FIELDS + pu.PRIMS:
+        assert np.array_equal(pu.host(q[k]), d["s1_bc_" + k]), f"{name} apply_bc {k}"
+    s.compute_fluxes(q)
+    if "s1_sigma_x" in d.files:
+        pu.assert_abs(pu.host(s.workspace(wavemp._lib.WS_SIGMA_X)), d["s1_sigma_x"], f"{name} sigma_x", 1e-12)
+        pu.assert_abs(pu.host(s.workspace(wavemp._lib.WS_SIGMA_Y)), d["s1_sigma_y"], f"{name} sigma_y", 1e-12)
+    fx, gy = s.fluxes("high")
+    nx_ = [f"fx{c}" for c in range(6)] + ["srcx"]
+    ny_ = [f"gy{c}" for c in range(6)] + ["srcy"]
+    pu.assert_fluxes([pu.host(a) for a in fx], [pu.host(a) for a in gy],
+                     [d["s1_high_" + k] for k in nx_], [d["s1_high_" + k] for k in ny_], fsc,
+                     f"{name} high-order flux")
+    s.compute_low_fluxes(q)
+    fx, gy = s.fluxes("low")
+    lx = [f"fxl{c}" for c in range(6)] + ["srcxl"]
+    ly = [f"gyl{c}" for c in range(6)] + ["srcyl"]
+    pu.assert_fluxes([pu.host(a) for a in fx], [pu.host(a) for a in gy],
+                     [d["s1_low_" + k] for k in lx], [d["s1_low_" + k] for k in ly], fsc,
+                     f"{name} first-order flux")
+    s.limit_fluxes(q, dt)
+    for st in range(3):
+        pu.assert_abs(pu.host(s.workspace(wavemp._lib.WS_THETA + st)), d[f"s1_theta{st}"],
+                      f"{name} theta pass {st}", 1e-9)
+    fx, gy = s.fluxes("high")
+    pu.assert_fluxes([pu.host(a) for a in fx], [pu.host(a) for a in gy],
+                     [d["s1_lim_" + k] for k in nx_], [d["s1_lim_" + k] for k in ny_], fsc,
+                     f"{name} limited flux")
+    s.rk3_update(q, q_old, 0.0, 1.0, dt)
+    pu.assert_cells(got_of(q), {k: d["s1_rk3_" + k] for k in pu.FIELDS}, pu.FIELDS, sc, f"{name} rk3")
+    s.enforce_admissible(q)
+    pu.assert_cells(got_of(q), {k: d["s1_adm_" + k] for k in pu.FIELDS}, pu.FIELDS, sc,
+                    f"{name} admissible")
+    s.update_prims(q)
+    pu.assert_cells(got_of(q), {k: d["s1_out_" + k] for k in pu.ALL}, pu.ALL, sc, f"{name} update_prims")
+    assert s.get_dt(q) > 0
+
+
+def test_fused_stage_equals_closures(case):
+    """wm_rhs_stage runs the same kernels' arithmetic as the closure sequence: bitwise equal."""
+    name, d = case
+    s = make_solver(d)
+    q1, q2 = load_state(d, "in_"), load_state(d, "in_")
+    old = alloc_state(s.nx, s.ny, s.g, names=pu.FIELDS)
+    s.copy_old(q1, old)
+    dt = float(d["dt0"])
+    for alpha, beta in ((0.0, 1.0), (0.75, 0.25)):
+        s.apply_bc(q1)
+        s.compute_fluxes(q1)
+        s.compute_low_fluxes(q1)
+        s.limit_fluxes(q1, dt)
+        s.rk3_update(q1, old, alpha, beta, dt)
+        s.enforce_admissible(q1)
+        s.update_prims(q1)
+        s.rhs_stage(q2, old, dt, alpha, beta)
+        for k in pu.ALL:
+            a, b = pu.host(q1[k]), pu.host(q2[k])
+            assert np.array_equal(a, b, equal_nan=True), f"{name} fused vs closures {k} (alpha={alpha})"
+
+
+def test_steps_match_reference(case):
+    name, d = case
+    s = make_solver(d)
+    q = load_state(d, "in_")
+    old = alloc_state(s.nx, s.ny, s.g, names=pu.FIELDS)
+    sc = pu.case_scales(d)
+    dt = s.step(q, old, float(d["dt0"]))
+    pu.assert_cells(got_of(q), {k: d["step1_" + k] for k in pu.ALL}, pu.ALL, sc, f"{name} step 1",
+                    rtol=RTOL_STEPS)
+    assert abs(dt - float(d["dt1"])) <= 1e-10 * float(d["dt1"]), (dt, float(d["dt1"]))
+    for _ in range(1, int(d["meta_steps"])):
+        dt = s.step(q, old, None)  # device-resident dt
+    pu.assert_cells(got_of(q), {k: d["final_" + k] for k in pu.ALL}, pu.ALL, sc, f"{name} final",
+                    rtol=RTOL_STEPS)
+    assert abs(dt - float(d["dt_final"])) <= 1e-10 * float(d["dt_final"])
+
+
+def test_step_old_state_is_copy_old(case):
+    """wm_step fuses copy_old: q_old after a step equals the state at the start of the step,
+    ghost cells included (copy_old runs before apply_bc in the reference, SC:2033-2036)."""
+    name, d = case
+    s = make_solver(d)
+    q = load_state(d, "in_")
+    old = alloc_state(s.nx, s.ny, s.g, names=pu.FIELDS)
+    s.step(q, old, float(d["dt0"]))
+    for k in pu.FIELDS:
+        assert np.array_equal(pu.host(old[k]), d["in_" + k]), f"{name} q_old {k}"
+
+
+def test_init_dt_matches_get_dt(case):
+    name, d = case
+    s = make_solver(d)
+    q = load_state(d, "in_")
+    dt = s.get_dt(q)
+    assert abs(dt - float(d["dt0"])) <= 1e-12 * float(d["dt0"])

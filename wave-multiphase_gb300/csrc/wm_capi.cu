@@ -1,0 +1,539 @@
+// wm_capi.cu -- the C ABI of include/wavemp.h: handle, workspace layout and the launch sequences
+// of the reference's closures (SC:1894-1995) and of the fused stage / step.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/wavemp.h"
+#include "wm_kernels.cuh"
+
+using namespace wm;
+
+namespace {
+
+thread_local char g_last_error[512] = "";
+
+void set_error(const char *where, cudaError_t err)
+{
+    snprintf(g_last_error, sizeof g_last_error, "%s: %s", where, cudaGetErrorString(err));
+}
+
+int check_launch(const char *where)
+{
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) {
+        set_error(where, err);
+        return WM_ERR_CUDA;
+    }
+    return WM_OK;
+}
+
+constexpr int kFaceArrays = 28, kThetaArrays = 3, kPrepArrays = 11;
+constexpr int kArrays = kFaceArrays + kThetaArrays + kPrepArrays;
+constexpr size_t kAlign = 256;
+constexpr size_t kTailBytes = 256;  // counters and dt slots
+
+size_t array_bytes(int nx, int ny, int g)
+{
+    size_t n = (size_t)(nx + 2 * g) * (size_t)(ny + 2 * g) * sizeof(double);
+    return (n + kAlign - 1) / kAlign * kAlign;
+}
+
+bool valid_params(const wm_params *p, int nx, int ny, int g)
+{
+    if (!p || nx < 1 || ny < 1 || g < 4 || g > 64) return false;
+    if (!(p->gamma1 > 1.0) || !(p->gamma2 > 1.0) || !(p->dx > 0.0) || !(p->dy > 0.0)) return false;
+    if (!std::isfinite(p->pinf1) || !std::isfinite(p->pinf2) || !(p->cfl > 0.0)) return false;
+    if (p->variant != WM_VARIANT_SC && p->variant != WM_VARIANT_M10) return false;
+    if (p->recon != WM_RECON_SHIPPED && p->recon != WM_RECON_MP5C6) return false;
+    if (p->precision != WM_PREC_FP64) return false;  // the binary32 form has its own entry points
+    for (int k = 0; k < 4; ++k)
+        if (p->bc[k] != WM_BC_TRANSMISSIVE && p->bc[k] != WM_BC_SLIP) return false;
+    if ((double)(nx + 2 * g) * (double)(ny + 2 * g) > 4.0e9) return false;
+    return true;
+}
+
+}  // namespace
+
+struct wm_handle {
+    wm_params P;
+    Grid g;
+    Eos e;
+    void *ws = nullptr;
+    bool own_ws = false;
+    double *arr[kArrays];
+    Face7 fh, gh, fl, gl;
+    double *theta[3];
+    Prep prep;
+    Counters cnt;
+    unsigned long long *ctr_base = nullptr;
+    double *dt_dev[2];
+    int dt_cur = 0;
+    bool dt_valid = false;
+    long long steps = 0;
+    bool fluxes_ready = false, low_ready = false;
+    // kernel-group profiler (wm_profile)
+    bool prof = false;
+    struct Rec {
+        int group, launches;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> pool;
+    double prof_ms[WM_PROF_GROUPS] = {0};
+    long long prof_n[WM_PROF_GROUPS] = {0};
+};
+
+namespace {
+
+cudaEvent_t take_event(wm_handle *h)
+{
+    if (!h->pool.empty()) {
+        cudaEvent_t e = h->pool.back();
+        h->pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Brackets a group of launches with events when the profiler is on.
+struct ProfScope {
+    wm_handle *h;
+    int group, launches;
+    cudaStream_t s;
+    cudaEvent_t a = nullptr;
+    ProfScope(wm_handle *h_, int g, int n, cudaStream_t s_) : h(h_), group(g), launches(n), s(s_)
+    {
+        if (h->prof) {
+            a = take_event(h);
+            cudaEventRecord(a, s);
+        }
+    }
+    ~ProfScope()
+    {
+        if (h->prof && a) {
+            cudaEvent_t b = take_event(h);
+            cudaEventRecord(b, s);
+            h->recs.push_back({group, launches, a, b});
+        }
+    }
+};
+
+}  // namespace
+
+namespace {
+
+bool fields_ok(const wm_handle *h, const wm_fields *q, bool need_prims = true)
+{
+    if (!q || q->pitch < h->g.nyg) return false;
+    double *const f[10] = {q->ar1, q->ar2, q->ru, q->rv, q->E, q->al, q->u_p, q->v_p, q->p_p, q->al_prim};
+    for (int c = 0; c < (need_prims ? 10 : 6); ++c)
+        if (!f[c] || ((uintptr_t)f[c] & 7u)) return false;
+    return true;
+}
+
+Fields to_fields(const wm_fields *q)
+{
+    Fields F;
+    F.f[0] = q->ar1; F.f[1] = q->ar2; F.f[2] = q->ru; F.f[3] = q->rv; F.f[4] = q->E; F.f[5] = q->al;
+    F.f[6] = q->u_p; F.f[7] = q->v_p; F.f[8] = q->p_p; F.f[9] = q->al_prim;
+    F.pitch = q->pitch;
+    return F;
+}
+
+cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+unsigned final_flags(const wm_handle *h, double alpha)
+{
+    unsigned fl = FIN_RK3 | FIN_PRIM;
+    if (h->P.emergency_repair) fl |= FIN_ADMISSIBLE;
+    if (alpha != 0.0) fl |= FIN_OLD_READ;
+    return fl;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *wm_version(void) { return "wavemp 0.1 (sm_103a, fp64)"; }
+const char *wm_last_error(void) { return g_last_error; }
+
+size_t wm_workspace_bytes(const wm_params *p, int nx, int ny, int g)
+{
+    if (!valid_params(p, nx, ny, g)) return 0;
+    return (size_t)kArrays * array_bytes(nx, ny, g) + kTailBytes;
+}
+
+int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t workspace_bytes,
+              wm_handle **out)
+{
+    if (!out) return WM_ERR_INVALID;
+    *out = nullptr;
+    if (!valid_params(p, nx, ny, g)) return WM_ERR_INVALID;
+    size_t need = wm_workspace_bytes(p, nx, ny, g);
+    if (workspace && (workspace_bytes < need || ((uintptr_t)workspace % kAlign))) return WM_ERR_NOMEM;
+    wm_handle *h = new (std::nothrow) wm_handle();
+    if (!h) return WM_ERR_NOMEM;
+    h->P = *p;
+    Grid &G = h->g;
+    G.nx = nx; G.ny = ny; G.g = g; G.nxg = nx + 2 * g; G.nyg = ny + 2 * g; G.pitch = G.nyg;
+    G.dx = p->dx; G.dy = p->dy; G.inv_dx = 1.0 / p->dx; G.inv_dy = 1.0 / p->dy; G.cfl = p->cfl;
+    Eos &E = h->e;
+    E.g1 = p->gamma1; E.p1 = p->pinf1; E.g2 = p->gamma2; E.p2 = p->pinf2;
+    E.r1 = 1.0 / (p->gamma1 - 1.0); E.r2 = 1.0 / (p->gamma2 - 1.0);
+    E.k1 = p->gamma1 * p->pinf1 / (p->gamma1 - 1.0); E.k2 = p->gamma2 * p->pinf2 / (p->gamma2 - 1.0);
+    E.thinc_t1 = std::tanh(1.8 * 0.5);
+    E.thinc_inv_t1 = 1.0 / E.thinc_t1;
+
+    if (workspace) {
+        h->ws = workspace;
+    } else {
+        cudaError_t err = cudaMalloc(&h->ws, need);
+        if (err != cudaSuccess) {
+            set_error("wm_create cudaMalloc", err);
+            delete h;
+            return WM_ERR_NOMEM;
+        }
+        h->own_ws = true;
+    }
+    cudaError_t err = cudaMemset(h->ws, 0, need);
+    if (err != cudaSuccess) {
+        set_error("wm_create cudaMemset", err);
+        if (h->own_ws) cudaFree(h->ws);
+        delete h;
+        return WM_ERR_CUDA;
+    }
+    char *base = static_cast<char *>(h->ws);
+    size_t ab = array_bytes(nx, ny, g);
+    for (int a = 0; a < kArrays; ++a) h->arr[a] = reinterpret_cast<double *>(base + (size_t)a * ab);
+    for (int c = 0; c < 7; ++c) {
+        h->fh.f[c] = h->arr[WM_WS_FX + c];
+        h->gh.f[c] = h->arr[WM_WS_GY + c];
+        h->fl.f[c] = h->arr[WM_WS_FXL + c];
+        h->gl.f[c] = h->arr[WM_WS_GYL + c];
+    }
+    for (int s = 0; s < 3; ++s) h->theta[s] = h->arr[WM_WS_THETA + s];
+    Prep &P = h->prep;
+    P.sx = h->arr[WM_WS_SIGMA_X];
+    P.sy = h->arr[WM_WS_SIGMA_Y];
+    P.ent = h->arr[33]; P.cx = h->arr[34]; P.cy = h->arr[35];
+    P.lu = h->arr[36]; P.lv = h->arr[37]; P.lp = h->arr[38]; P.la = h->arr[39]; P.lc = h->arr[40];
+    P.lE = h->arr[41];
+    char *tail = base + (size_t)kArrays * ab;
+    h->ctr_base = reinterpret_cast<unsigned long long *>(tail);
+    h->cnt.repaired = h->ctr_base + 0;
+    h->cnt.nonfinite = h->ctr_base + 1;
+    h->cnt.limited = h->ctr_base + 2;
+    h->cnt.dt_bits = h->ctr_base + 3;
+    h->dt_dev[0] = reinterpret_cast<double *>(tail + 64);
+    h->dt_dev[1] = reinterpret_cast<double *>(tail + 72);
+    *out = h;
+    return WM_OK;
+}
+
+void wm_destroy(wm_handle *h)
+{
+    if (!h) return;
+    for (auto &r : h->recs) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    for (auto e : h->pool) cudaEventDestroy(e);
+    if (h->own_ws && h->ws) cudaFree(h->ws);
+    delete h;
+}
+
+int wm_profile(wm_handle *h, int enable)
+{
+    if (!h) return WM_ERR_INVALID;
+    h->prof = enable != 0;
+    return WM_OK;
+}
+
+int wm_profile_read(wm_handle *h, double ms[WM_PROF_GROUPS], long long launches[WM_PROF_GROUPS],
+                    int reset)
+{
+    if (!h || !ms || !launches) return WM_ERR_INVALID;
+    for (auto &r : h->recs) {
+        cudaError_t err = cudaEventSynchronize(r.b);
+        float t = 0.f;
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&t, r.a, r.b);
+        if (err != cudaSuccess) {
+            set_error("wm_profile_read", err);
+            return WM_ERR_CUDA;
+        }
+        h->prof_ms[r.group] += t;
+        h->prof_n[r.group] += r.launches;
+        h->pool.push_back(r.a);
+        h->pool.push_back(r.b);
+    }
+    h->recs.clear();
+    for (int g = 0; g < WM_PROF_GROUPS; ++g) {
+        ms[g] = h->prof_ms[g];
+        launches[g] = h->prof_n[g];
+        if (reset) {
+            h->prof_ms[g] = 0.0;
+            h->prof_n[g] = 0;
+        }
+    }
+    return WM_OK;
+}
+
+int wm_apply_bc(wm_handle *h, const wm_fields *q, void *stream)
+{
+    if (!h || !fields_ok(h, q)) return WM_ERR_INVALID;
+    Fields F = to_fields(q);
+    launch_bc(h->g, h->P.bc, F, nullptr, as_stream(stream));
+    return check_launch("wm_apply_bc");
+}
+
+int wm_compute_fluxes(wm_handle *h, const wm_fields *q, void *stream)
+{
+    if (!h || !fields_ok(h, q)) return WM_ERR_INVALID;
+    Fields F = to_fields(q);
+    cudaStream_t s = as_stream(stream);
+    launch_prep(h->g, h->e, F, h->prep, h->P.variant, s);
+    launch_faces(h->g, h->e, h->P.variant, h->P.recon, F, h->prep, h->fh, h->gh, h->fl, h->gl, true,
+                 false, s);
+    h->fluxes_ready = true;
+    return check_launch("wm_compute_fluxes");
+}
+
+int wm_compute_low_fluxes(wm_handle *h, const wm_fields *q, void *stream)
+{
+    if (!h || !fields_ok(h, q)) return WM_ERR_INVALID;
+    Fields F = to_fields(q);
+    cudaStream_t s = as_stream(stream);
+    launch_prep(h->g, h->e, F, h->prep, h->P.variant, s);
+    launch_faces(h->g, h->e, h->P.variant, h->P.recon, F, h->prep, h->fh, h->gh, h->fl, h->gl, false,
+                 true, s);
+    h->low_ready = true;
+    return check_launch("wm_compute_low_fluxes");
+}
+
+int wm_limit_fluxes(wm_handle *h, const wm_fields *q, double dt, void *stream)
+{
+    if (!h || !fields_ok(h, q) || !std::isfinite(dt)) return WM_ERR_INVALID;
+    if (!h->fluxes_ready || !h->low_ready) return WM_ERR_STATE;
+    launch_limiter(h->g, h->e, to_fields(q), h->fh, h->gh, h->fl, h->gl, h->theta, dt, nullptr, h->cnt,
+                   as_stream(stream));
+    return check_launch("wm_limit_fluxes");
+}
+
+int wm_rk3_update(wm_handle *h, const wm_fields *q, const wm_fields *q_old, double alpha,
+                  double beta, double dt, void *stream)
+{
+    if (!h || !fields_ok(h, q) || !std::isfinite(dt)) return WM_ERR_INVALID;
+    if (alpha != 0.0 && !fields_ok(h, q_old, false)) return WM_ERR_INVALID;
+    if (!h->fluxes_ready) return WM_ERR_STATE;
+    Fields F = to_fields(q), O = q_old ? to_fields(q_old) : F;
+    launch_final(h->g, h->e, FIN_RK3 | (alpha != 0.0 ? FIN_OLD_READ : 0u), F, O, h->fh, h->gh, dt,
+                 nullptr, alpha, beta, h->cnt, as_stream(stream));
+    return check_launch("wm_rk3_update");
+}
+
+int wm_enforce_admissible(wm_handle *h, const wm_fields *q, void *stream)
+{
+    if (!h || !fields_ok(h, q)) return WM_ERR_INVALID;
+    if (!h->P.emergency_repair) return WM_OK;
+    Fields F = to_fields(q);
+    launch_final(h->g, h->e, FIN_ADMISSIBLE, F, F, h->fh, h->gh, 0.0, nullptr, 0.0, 1.0, h->cnt,
+                 as_stream(stream));
+    return check_launch("wm_enforce_admissible");
+}
+
+int wm_update_prims(wm_handle *h, const wm_fields *q, void *stream)
+{
+    if (!h || !fields_ok(h, q)) return WM_ERR_INVALID;
+    Fields F = to_fields(q);
+    launch_final(h->g, h->e, FIN_PRIM, F, F, h->fh, h->gh, 0.0, nullptr, 0.0, 1.0, h->cnt,
+                 as_stream(stream));
+    return check_launch("wm_update_prims");
+}
+
+int wm_copy_old(wm_handle *h, const wm_fields *q, const wm_fields *q_old, void *stream)
+{
+    if (!h || !fields_ok(h, q, false) || !fields_ok(h, q_old, false)) return WM_ERR_INVALID;
+    launch_copy_old(h->g, to_fields(q), to_fields(q_old), as_stream(stream));
+    return check_launch("wm_copy_old");
+}
+
+int wm_init_dt(wm_handle *h, const wm_fields *q, void *stream)
+{
+    if (!h || !fields_ok(h, q)) return WM_ERR_INVALID;
+    cudaStream_t s = as_stream(stream);
+    launch_dt_reset(h->cnt, s);
+    launch_dt_cell(h->g, h->e, to_fields(q), h->cnt, s);
+    launch_dt_finalize(h->g, h->cnt, h->dt_dev[h->dt_cur], s);
+    h->dt_valid = true;
+    return check_launch("wm_init_dt");
+}
+
+int wm_get_dt(wm_handle *h, const wm_fields *q, double *dt, void *stream)
+{
+    if (!dt) return WM_ERR_INVALID;
+    int rc = wm_init_dt(h, q, stream);
+    if (rc) return rc;
+    cudaStream_t s = as_stream(stream);
+    cudaError_t err = cudaMemcpyAsync(dt, h->dt_dev[h->dt_cur], sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    if (err != cudaSuccess) {
+        set_error("wm_get_dt", err);
+        return WM_ERR_CUDA;
+    }
+    return WM_OK;
+}
+
+// One stage; `save_old` fuses copy_old, `dt_dev` (when non-null) replaces dt, `want_dt` appends
+// the time-step reduction of the updated state.
+static int run_stage(wm_handle *h, const Fields &F, const Fields &O, double dt, const double *dt_dev,
+                     double alpha, double beta, bool save_old, bool want_dt, cudaStream_t s)
+{
+    {
+        ProfScope ps(h, WM_PROF_BC, 2, s);
+        launch_bc(h->g, h->P.bc, F, save_old ? &O : nullptr, s);
+    }
+    {
+        ProfScope ps(h, WM_PROF_PREP, 2, s);
+        launch_prep(h->g, h->e, F, h->prep, h->P.variant, s);
+    }
+    {
+        ProfScope ps(h, WM_PROF_FACES, 2, s);
+        launch_faces(h->g, h->e, h->P.variant, h->P.recon, F, h->prep, h->fh, h->gh, h->fl, h->gl,
+                     true, true, s);
+    }
+    {
+        ProfScope ps(h, WM_PROF_LIMITER, 6, s);
+        launch_limiter(h->g, h->e, F, h->fh, h->gh, h->fl, h->gl, h->theta, dt, dt_dev, h->cnt, s);
+    }
+    unsigned flags = final_flags(h, alpha);
+    if (save_old) flags |= FIN_SAVE_OLD;
+    {
+        ProfScope ps(h, WM_PROF_FINAL, want_dt ? 2 : 1, s);
+        if (want_dt) {
+            flags |= FIN_DT;
+            launch_dt_reset(h->cnt, s);
+        }
+        launch_final(h->g, h->e, flags, F, O, h->fh, h->gh, dt, dt_dev, alpha, beta, h->cnt, s);
+    }
+    h->fluxes_ready = h->low_ready = true;
+    return check_launch("stage");
+}
+
+int wm_rhs_stage(wm_handle *h, const wm_fields *q, const wm_fields *q_old, double dt, double alpha,
+                 double beta, void *stream)
+{
+    if (!h || !fields_ok(h, q) || !std::isfinite(dt) || !std::isfinite(alpha) || !std::isfinite(beta))
+        return WM_ERR_INVALID;
+    if (alpha != 0.0 && !fields_ok(h, q_old, false)) return WM_ERR_INVALID;
+    Fields F = to_fields(q), O = (alpha != 0.0) ? to_fields(q_old) : F;
+    return run_stage(h, F, O, dt, nullptr, alpha, beta, false, false, as_stream(stream));
+}
+
+int wm_step(wm_handle *h, const wm_fields *q, const wm_fields *q_old, double dt, double *dt_next,
+            void *stream)
+{
+    if (!h || !fields_ok(h, q) || !fields_ok(h, q_old, false) || std::isnan(dt)) return WM_ERR_INVALID;
+    if (!(dt > 0.0) && !h->dt_valid) return WM_ERR_STATE;
+    cudaStream_t s = as_stream(stream);
+    Fields F = to_fields(q), O = to_fields(q_old);
+    const double *dd = dt > 0.0 ? nullptr : h->dt_dev[h->dt_cur];
+    int rc = run_stage(h, F, O, dt, dd, 0.0, 1.0, true, false, s);
+    if (!rc) rc = run_stage(h, F, O, dt, dd, 0.75, 0.25, false, false, s);
+    if (!rc) rc = run_stage(h, F, O, dt, dd, 1.0 / 3.0, 2.0 / 3.0, false, true, s);
+    if (rc) return rc;
+    int nxt = 1 - h->dt_cur;
+    {
+        ProfScope ps(h, WM_PROF_FINAL, 1, s);
+        launch_dt_finalize(h->g, h->cnt, h->dt_dev[nxt], s);
+    }
+    h->dt_cur = nxt;
+    h->dt_valid = true;
+    h->steps++;
+    rc = check_launch("wm_step");
+    if (rc) return rc;
+    if (dt_next) {
+        cudaError_t err = cudaMemcpyAsync(dt_next, h->dt_dev[h->dt_cur], sizeof(double),
+                                          cudaMemcpyDeviceToHost, s);
+        if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+        if (err != cudaSuccess) {
+            set_error("wm_step dt", err);
+            return WM_ERR_CUDA;
+        }
+    }
+    return WM_OK;
+}
+
+int wm_read_workspace(wm_handle *h, int which, double *dst, void *stream)
+{
+    if (!h || !dst || which < 0 || which >= WM_WS_COUNT) return WM_ERR_INVALID;
+    size_t n = (size_t)h->g.nxg * (size_t)h->g.nyg * sizeof(double);
+    cudaError_t err = cudaMemcpyAsync(dst, h->arr[which], n, cudaMemcpyDeviceToDevice, as_stream(stream));
+    if (err != cudaSuccess) {
+        set_error("wm_read_workspace", err);
+        return WM_ERR_CUDA;
+    }
+    return WM_OK;
+}
+
+int wm_status(wm_handle *h, wm_stats *out, int reset, void *stream)
+{
+    if (!h || !out) return WM_ERR_INVALID;
+    unsigned long long c[3];
+    cudaStream_t s = as_stream(stream);
+    cudaError_t err = cudaMemcpyAsync(c, h->ctr_base, sizeof c, cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess && reset) err = cudaMemsetAsync(h->ctr_base, 0, sizeof c, s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    if (err != cudaSuccess) {
+        set_error("wm_status", err);
+        return WM_ERR_CUDA;
+    }
+    out->repaired_cells = (long long)c[0];
+    out->nonfinite_cells = (long long)c[1];
+    out->limited_cells = (long long)c[2];
+    out->steps = h->steps;
+    if (reset) h->steps = 0;
+    return WM_OK;
+}
+
+int wm_probe_fp64_flops(double *flops, void *stream)
+{
+    if (!flops) return WM_ERR_INVALID;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    double *buf = nullptr;
+    cudaError_t err = cudaMalloc(&buf, (size_t)blocks * threads * sizeof(double));
+    if (err != cudaSuccess) {
+        set_error("wm_probe_fp64_flops", err);
+        return WM_ERR_NOMEM;
+    }
+    cudaStream_t s = as_stream(stream);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(e0, s);
+        launch_fp64_probe(buf, iters, s, blocks, threads);
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(buf);
+    int rc = check_launch("wm_probe_fp64_flops");
+    if (rc) return rc;
+    *flops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3);
+    return WM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,496 @@
+// wm_device.cuh -- device functions of the per-stage RHS (sm_103a).
+//
+// Each function states the reference device function it computes (SC = sainath_SC_it_works.py).
+// They are templated on the arithmetic type T of the face sweeps: double for the plain form,
+// float for the bulk of the precision form. Branch structure, thresholds and the order of the
+// operations that decide branches follow the reference; divisions by run-time constants are
+// replaced by multiplications with host-computed reciprocals, and divisions by the same value are
+// shared (a relative difference of a few ulp, far inside the 1e-10 parity tolerance).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace wm {
+
+// ------------------------------------------------------------------------------------------------
+// Launch-constant parameter blocks (passed by value as kernel arguments).
+// ------------------------------------------------------------------------------------------------
+struct Eos {
+    double g1, p1, g2, p2;  // gamma, p_inf of fluid 1 and 2
+    double r1, r2;          // 1/(g1-1), 1/(g2-1)
+    double k1, k2;          // g1*p1/(g1-1), g2*p2/(g2-1)
+    double thinc_t1;        // tanh(beta/2), beta = 1.8 (computed once on the host)
+    double thinc_inv_t1;    // 1/tanh(beta/2)
+};
+
+struct Grid {
+    int nx, ny, g;       // interior size and ghost width
+    int nxg, nyg;        // padded size
+    long long pitch;     // elements between x rows
+    double dx, dy, inv_dx, inv_dy, cfl;
+};
+
+// Reference constants (SC:44-70).
+constexpr double kTiny = 1.0e-20;
+constexpr double kEpsM = 1.0e-20;
+constexpr double kMp5Alpha = 4.0;
+constexpr double kB2 = 4.0 / 3.0;
+constexpr double kKappa = 1.0 / 3.0;
+constexpr double k1o60 = 1.0 / 60.0;
+constexpr double kYuxin = 0.9 * 0.35 * 1.0e-2 / (1.0 - 0.9 * 0.35);
+constexpr double kThincThresh = 0.35;
+constexpr double kPpRho = 1.0e-10;
+constexpr double kPpAlpha = 1.0e-10;
+constexpr double kPpCtilde = 1.0e-8;
+constexpr double kPpHsRho = 1.0e-11;
+constexpr double kPpHsAlpha = 1.0e-11;
+constexpr double kPpHsCtilde = 1.0e-9;
+constexpr double kSigmaSmooth = 0.01;
+constexpr double kPrimAlphaFloor = 1.0e-8;  // cons_to_prim clamp (SC:852-853)
+
+// Warp's float builtins: min/max as a<b?a:b / a>b?a:b; sign(x) = x<0 ? -1 : +1.
+template <typename T> __device__ __forceinline__ T wmin(T a, T b) { return a < b ? a : b; }
+template <typename T> __device__ __forceinline__ T wmax(T a, T b) { return a > b ? a : b; }
+template <typename T> __device__ __forceinline__ T wsign(T x) { return x < T(0) ? T(-1) : T(1); }
+__device__ __forceinline__ double wabs(double x) { return fabs(x); }
+__device__ __forceinline__ float wabs(float x) { return fabsf(x); }
+__device__ __forceinline__ bool wisnan(double x) { return isnan(x); }
+__device__ __forceinline__ bool wisnan(float x) { return isnan(x); }
+__device__ __forceinline__ double wsqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float wsqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double wtanh(double x) { return tanh(x); }
+__device__ __forceinline__ float wtanh(float x) { return tanhf(x); }
+__device__ __forceinline__ double wpow(double a, double b) { return pow(a, b); }
+__device__ __forceinline__ float wpow(float a, float b) { return powf(a, b); }
+
+template <typename T> struct S6 { T v[6]; };
+
+// ------------------------------------------------------------------------------------------------
+// Mixture stiffened-gas EOS (SC:83-110)
+// ------------------------------------------------------------------------------------------------
+// Gamma = sum a_k/(g_k-1), Pi = sum a_k g_k pi_k/(g_k-1)
+template <typename T>
+__device__ __forceinline__ void mix_gamma_pibig(const Eos &e, T a1, T &gb, T &pb)
+{
+    T a2 = T(1) - a1;
+    gb = a1 * T(e.r1) + a2 * T(e.r2);
+    pb = a1 * T(e.k1) + a2 * T(e.k2);
+}
+
+// mixture gamma and p_inf
+template <typename T>
+__device__ __forceinline__ void mix_gamma_pinf(const Eos &e, T a1, T &g, T &pi)
+{
+    T gb, pb;
+    mix_gamma_pibig(e, a1, gb, pb);
+    g = T(1) / gb + T(1);
+    pi = (g - T(1)) * pb / g;
+}
+
+// sound_speed(rho, p, a1) with 1/rho supplied
+template <typename T>
+__device__ __forceinline__ T sound_speed_r(const Eos &e, T inv_rho, T p, T a1)
+{
+    T g, pi;
+    mix_gamma_pinf(e, a1, g, pi);
+    T val = g * (p + pi) * inv_rho;
+    if (val < T(kTiny)) val = T(kTiny);
+    return wsqrt(val);
+}
+
+// prim_to_energy (SC:105-110)
+template <typename T>
+__device__ __forceinline__ T prim_to_energy(const Eos &e, T rho, T u, T v, T p, T a1)
+{
+    T gb, pb;
+    mix_gamma_pibig(e, a1, gb, pb);
+    return gb * p + pb + T(0.5) * rho * (u * u + v * v);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Positivity helpers (SC:112-292)
+// ------------------------------------------------------------------------------------------------
+template <typename T> __device__ __forceinline__ T clamp01_pp(T a1)
+{
+    T a = a1;
+    if (wisnan(a)) a = T(kPpAlpha);
+    if (a < T(kPpAlpha)) a = T(kPpAlpha);
+    if (a > T(1) - T(kPpAlpha)) a = T(1) - T(kPpAlpha);
+    return a;
+}
+
+__device__ __forceinline__ double pp_theta_lower(double base, double high, double floor_)
+{
+    double theta = 1.0;
+    if (isnan(base) || isnan(high)) {
+        theta = 0.0;
+    } else if (high < floor_) {
+        double denom = base - high;
+        theta = denom > kTiny ? (base - floor_) / denom : 0.0;
+    }
+    if (theta < 0.0) theta = 0.0;
+    if (theta > 1.0) theta = 1.0;
+    return theta;
+}
+
+template <typename T>
+__device__ __forceinline__ S6<T> blend_s6(const S6<T> &base, const S6<T> &high, T theta)
+{
+    S6<T> s;
+#pragma unroll
+    for (int f = 0; f < 6; ++f) s.v[f] = base.v[f] + theta * (high.v[f] - base.v[f]);
+    return s;
+}
+
+// rho c~^2 of an SC state [m1, m2, rho u, rho v, p, alpha] (SC:174-178)
+template <typename T> __device__ __forceinline__ T rho_ctilde2_sc(const Eos &e, const S6<T> &s)
+{
+    T g, pi;
+    mix_gamma_pinf(e, clamp01_pp(s.v[5]), g, pi);
+    return (s.v[4] + pi) / (g - T(1));
+}
+
+template <typename T> __device__ __forceinline__ S6<T> pp_floor_pressure_state(const Eos &e, S6<T> s)
+{
+    T a1 = clamp01_pp(s.v[5]);
+    T g, pi;
+    mix_gamma_pinf(e, a1, g, pi);
+    if (wisnan(s.v[4]) || rho_ctilde2_sc(e, s) < T(kPpCtilde)) s.v[4] = T(kPpCtilde) * (g - T(1)) - pi;
+    s.v[5] = a1;
+    return s;
+}
+
+template <typename T>
+__device__ __forceinline__ S6<T> wong_stage_lower_s6(const S6<T> &base, const S6<T> &high, T base_val,
+                                                     T high_val, T floor_)
+{
+    T theta = T(1);
+    if (wisnan(base_val) || wisnan(high_val) || base_val < floor_) {
+        theta = T(0);
+    } else if (high_val < floor_) {
+        T denom = base_val - high_val;
+        theta = denom > T(kTiny) ? (base_val - floor_) / denom : T(0);
+    }
+    return blend_s6(base, high, theta);
+}
+
+// Wong staged interpolation limiter on a reconstructed state (SC:217-240, used by M10:1007-1008)
+template <typename T>
+__device__ __forceinline__ S6<T> pp_limit_reconstructed_state(const Eos &e, const S6<T> &high,
+                                                              const S6<T> &base)
+{
+    S6<T> b = base;
+    b.v[5] = clamp01_pp(b.v[5]);
+    if (b.v[0] < T(kPpRho) || wisnan(b.v[0])) b.v[0] = T(kPpRho);
+    if (b.v[1] < T(kPpRho) || wisnan(b.v[1])) b.v[1] = T(kPpRho);
+    S6<T> s = high;
+    s = wong_stage_lower_s6(b, s, b.v[0], s.v[0], T(kPpRho));
+    s = wong_stage_lower_s6(b, s, b.v[1], s.v[1], T(kPpRho));
+    s = wong_stage_lower_s6(b, s, b.v[5], s.v[5], T(kPpAlpha));
+    s = wong_stage_lower_s6(b, s, T(1) - b.v[5], T(1) - s.v[5], T(kPpAlpha));
+    s = wong_stage_lower_s6(b, s, rho_ctilde2_sc(e, b), rho_ctilde2_sc(e, s), T(kPpCtilde));
+    if (s.v[0] < T(kPpHsRho) || s.v[1] < T(kPpHsRho) || s.v[5] < T(kPpHsAlpha) ||
+        s.v[5] > T(1) - T(kPpHsAlpha))
+        s = b;
+    if (rho_ctilde2_sc(e, s) < T(kPpHsCtilde) || wisnan(s.v[4])) s = b;
+    return s;
+}
+
+// rho c~^2 = E - kinetic - pi of a conserved state (SC:242-258); always binary64.
+__device__ __forceinline__ double rho_ctilde2_cons(const Eos &e, double m1, double m2, double mx,
+                                                   double my, double E, double a1_in)
+{
+    double a1 = clamp01_pp(a1_in);
+    double mm1 = m1, mm2 = m2;
+    if (mm1 < kPpRho || isnan(mm1)) mm1 = kPpRho;
+    if (mm2 < kPpRho || isnan(mm2)) mm2 = kPpRho;
+    double rho = mm1 + mm2;
+    double ir = 1.0 / rho;
+    double uu = mx * ir, vv = my * ir;
+    double kin = 0.5 * rho * (uu * uu + vv * vv);
+    double g, pi;
+    mix_gamma_pinf(e, a1, g, pi);
+    return E - kin - pi;
+}
+
+// Limiter factor of one cell for one pass (theta_cons_stage, SC:268-292); binary64.
+__device__ __forceinline__ double theta_cons_stage(const Eos &e, const double l[6], const double h[6],
+                                                   int stage)
+{
+    double theta = 1.0;
+    if (stage == 0) {
+        theta = wmin(theta, pp_theta_lower(l[0], h[0], kPpRho));
+        theta = wmin(theta, pp_theta_lower(l[1], h[1], kPpRho));
+    } else if (stage == 1) {
+        theta = wmin(theta, pp_theta_lower(l[5], h[5], kPpAlpha));
+        theta = wmin(theta, pp_theta_lower(1.0 - l[5], 1.0 - h[5], kPpAlpha));
+    } else {
+        double lc = rho_ctilde2_cons(e, l[0], l[1], l[2], l[3], l[4], l[5]);
+        double hc = rho_ctilde2_cons(e, h[0], h[1], h[2], h[3], h[4], h[5]);
+        theta = pp_theta_lower(lc, hc, kPpCtilde);
+    }
+    if (theta < 0.0 || isnan(theta)) theta = 0.0;
+    if (theta > 1.0) theta = 1.0;
+    return theta;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Limiters and sensors (SC:295-325)
+// ------------------------------------------------------------------------------------------------
+template <typename T> __device__ __forceinline__ T mm2(T x, T y)
+{
+    return T(0.5) * (wsign(x) + wsign(y)) * wmin(wabs(x), wabs(y));
+}
+
+template <typename T> __device__ __forceinline__ T mm4(T a, T b, T c, T d)
+{
+    T sa = wsign(a);
+    T s = sa + wsign(b);
+    return T(0.125) * s * wabs((sa + wsign(c)) * (sa + wsign(d))) *
+           wmin(wmin(wabs(a), wabs(b)), wmin(wabs(c), wabs(d)));
+}
+
+// p / rho^gamma(alpha) (SC:308-314)
+template <typename T> __device__ __forceinline__ T cell_entropy(const Eos &e, T ar1, T ar2, T p, T a1)
+{
+    T rho = ar1 + ar2;
+    if (rho < T(kTiny)) rho = T(kTiny);
+    T g, pi;
+    mix_gamma_pinf(e, a1, g, pi);
+    return p / wpow(rho, g);
+}
+
+// smoothness indicator (SC:318-325)
+template <typename T> __device__ __forceinline__ T cator2_val(T em2, T em1, T e0, T ep1, T ep2)
+{
+    T aa = T(0.25) * wabs(em2 - T(4) * em1 + T(3) * e0) + T(13.0 / 12.0) * wabs(e0 - T(2) * em1 + em2);
+    T bb = T(0.25) * wabs(T(3) * e0 - T(4) * ep1 + ep2) + T(13.0 / 12.0) * wabs(e0 - T(2) * ep1 + ep2);
+    return (T(2) * aa * bb + T(kYuxin)) / (aa * aa + bb * bb + T(kYuxin));
+}
+
+// ------------------------------------------------------------------------------------------------
+// Reconstructions (SC:327-446)
+// ------------------------------------------------------------------------------------------------
+template <typename T> __device__ __forceinline__ T thinc_ul(const Eos &e, T vm1, T v0, T v1)
+{
+    T result = v0;
+    if ((v1 - v0) * (v0 - vm1) > T(0)) {
+        T qa = T(0.5) * (v1 + vm1);
+        T qd = T(0.5) * (v1 - vm1);
+        T feng = (v0 - qa) / qd;
+        T T1 = T(e.thinc_t1);
+        T T2 = wtanh(feng * T(1.8) * T(0.5));
+        result = qa + qd * (T1 + T2 * T(e.thinc_inv_t1)) / (T(1) + T2);
+    }
+    return result;
+}
+
+template <typename T> __device__ __forceinline__ T thinc_ur(const Eos &e, T v0, T v1, T v2)
+{
+    T result = v1;
+    if ((v2 - v1) * (v1 - v0) > T(0)) {
+        T qa = T(0.5) * (v2 + v0);
+        T qd = T(0.5) * (v2 - v0);
+        T feng = (v1 - qa) / qd;
+        T T1 = T(e.thinc_t1);
+        T T2 = wtanh(feng * T(1.8) * T(0.5));
+        result = qa - qd * (T1 - T2 * T(e.thinc_inv_t1)) / (T(1) - T2);
+    }
+    return result;
+}
+
+// Suresh-Huynh MP5, left-biased value at i+1/2 from cells i-2..i+2 (SC:353-377)
+template <typename T> __device__ __forceinline__ T mp5_ul(T vm2, T vm1, T v0, T vp1, T vp2)
+{
+    T VOR = T(k1o60) * (T(2) * vm2 - T(13) * vm1 + T(47) * v0 + T(27) * vp1 - T(3) * vp2);
+    T VMP = v0 + mm2(vp1 - v0, T(kMp5Alpha) * (v0 - vm1));
+    T result = VOR;
+    if ((VOR - v0) * (VOR - VMP) >= T(kEpsM)) {
+        T DJM1 = vm2 - T(2) * vm1 + v0;
+        T DJ = vm1 - T(2) * v0 + vp1;
+        T DJP1 = v0 - T(2) * vp1 + vp2;
+        T DM4JPH = mm4(T(4) * DJ - DJP1, T(4) * DJP1 - DJ, DJ, DJP1);
+        T DM4JMH = mm4(T(4) * DJ - DJM1, T(4) * DJM1 - DJ, DJ, DJM1);
+        T VUL = v0 + T(kMp5Alpha) * (v0 - vm1);
+        T VAV = T(0.5) * (v0 + vp1);
+        T VMD = VAV - T(0.5) * DM4JPH;
+        T VLC = v0 + T(0.5) * (v0 - vm1) + T(kB2) * DM4JMH;
+        T VMIN = wmax(wmin(wmin(v0, vp1), VMD), wmin(wmin(v0, VUL), VLC));
+        T VMAX = wmin(wmax(wmax(v0, vp1), VMD), wmax(wmax(v0, VUL), VLC));
+        result = VOR + mm2(VMIN - VOR, VMAX - VOR);
+    }
+    return result;
+}
+
+// right-biased value at i+1/2 from cells i-1..i+3 (SC:379-405)
+template <typename T> __device__ __forceinline__ T mp5_ur(T vm1, T v0, T vp1, T vp2, T vp3)
+{
+    T VOR = T(k1o60) * (T(-3) * vm1 + T(27) * v0 + T(47) * vp1 - T(13) * vp2 + T(2) * vp3);
+    T VMP = vp1 + mm2(v0 - vp1, T(kMp5Alpha) * (vp1 - vp2));
+    T result = VOR;
+    if ((VOR - vp1) * (VOR - VMP) >= T(kEpsM)) {
+        T DJM1 = vm1 - T(2) * v0 + vp1;
+        T DJ = v0 - T(2) * vp1 + vp2;
+        T DJP1 = vp1 - T(2) * vp2 + vp3;
+        T DM4JPH = mm4(T(4) * DJ - DJP1, T(4) * DJP1 - DJ, DJ, DJP1);
+        T DM4JMH = mm4(T(4) * DJ - DJM1, T(4) * DJM1 - DJ, DJ, DJM1);
+        T VUL = vp1 + T(kMp5Alpha) * (vp1 - vp2);
+        T VAV = T(0.5) * (vp1 + v0);
+        T VMD = VAV - T(0.5) * DM4JMH;
+        T VLC = vp1 + T(0.5) * (vp1 - vp2) + T(kB2) * DM4JPH;
+        T VMIN = wmax(wmin(wmin(vp1, v0), VMD), wmin(wmin(vp1, VUL), VLC));
+        T VMAX = wmin(wmax(wmax(vp1, v0), VMD), wmax(wmax(vp1, VUL), VLC));
+        result = VOR + mm2(VMIN - VOR, VMAX - VOR);
+    }
+    return result;
+}
+
+// sixth-order central face value (SC:407-412)
+template <typename T> __device__ __forceinline__ T central6_avg(T vm2, T vm1, T v0, T vp1, T vp2, T vp3)
+{
+    T left = T(k1o60) * (T(2) * vm2 - T(13) * vm1 + T(47) * v0 + T(27) * vp1 - T(3) * vp2);
+    T right = T(k1o60) * (T(-3) * vm1 + T(27) * v0 + T(47) * vp1 - T(13) * vp2 + T(2) * vp3);
+    return T(0.5) * (left + right);
+}
+
+// fourth-order central face value (SC:1076-1082)
+template <typename T> __device__ __forceinline__ T central4(T wm1, T w0, T w1, T w2)
+{
+    return -T(1.0 / 12.0) * wm1 + T(7.0 / 12.0) * w0 + T(7.0 / 12.0) * w1 - T(1.0 / 12.0) * w2;
+}
+
+// MUSCL kappa=1/3 on a characteristic field (SC:430-446)
+template <typename T> __device__ __forceinline__ T muscl_char_ul(T vm1, T v0, T vp1)
+{
+    T dm = v0 - vm1;
+    T d0 = vp1 - v0;
+    return v0 + T(0.25) * (T(1.0 - kKappa) * mm2(dm, T(2) * d0) + T(1.0 + kKappa) * mm2(d0, T(2) * dm));
+}
+
+template <typename T> __device__ __forceinline__ T muscl_char_ur(T v0, T vp1, T vp2)
+{
+    T dp = vp2 - vp1;
+    T d0 = vp1 - v0;
+    return vp1 - T(0.25) * (T(1.0 - kKappa) * mm2(dp, T(2) * d0) + T(1.0 + kKappa) * mm2(d0, T(2) * dp));
+}
+
+// ------------------------------------------------------------------------------------------------
+// Characteristic projections with face-averaged eigenvectors (SC:447-589).
+// State order [ar1, ar2, rho u, rho v, p, alpha1]; DIR 0 = x faces, 1 = y faces.
+// ------------------------------------------------------------------------------------------------
+template <typename T> struct FaceBasis {
+    T c, c2, inv2c, inv2c2, Y1, Y2, Y1c2, Y2c2, u, v;
+};
+
+template <int DIR, typename T> __device__ __forceinline__ S6<T> to_char(const FaceBasis<T> &b, const T u[6])
+{
+    S6<T> s;
+    if (DIR == 0) {  // to_char_x (SC:480-499)
+        T un = b.u, ut = b.v;
+        s.v[0] = un * b.inv2c * u[0] + un * b.inv2c * u[1] - b.inv2c * u[2] + b.inv2c2 * u[4];
+        s.v[1] = u[0] - b.Y1c2 * u[4];
+        s.v[2] = u[1] - b.Y2c2 * u[4];
+        s.v[3] = -ut * u[0] - ut * u[1] + u[3];
+        s.v[4] = u[5];
+        s.v[5] = -un * b.inv2c * u[0] - un * b.inv2c * u[1] + b.inv2c * u[2] + b.inv2c2 * u[4];
+    } else {  // to_char_y (SC:537-556)
+        T un = b.v, ut_f = -b.u;
+        s.v[0] = un * b.inv2c * u[0] + un * b.inv2c * u[1] - b.inv2c * u[3] + b.inv2c2 * u[4];
+        s.v[1] = u[0] - b.Y1c2 * u[4];
+        s.v[2] = u[1] - b.Y2c2 * u[4];
+        s.v[3] = -ut_f * u[0] - ut_f * u[1] - u[2];
+        s.v[4] = u[5];
+        s.v[5] = -un * b.inv2c * u[0] - un * b.inv2c * u[1] + b.inv2c * u[3] + b.inv2c2 * u[4];
+    }
+    return s;
+}
+
+template <int DIR, typename T> __device__ __forceinline__ S6<T> to_phys(const FaceBasis<T> &b, const T w[6])
+{
+    S6<T> s;
+    s.v[0] = b.Y1 * (w[0] + w[5]) + w[1];
+    s.v[1] = b.Y2 * (w[0] + w[5]) + w[2];
+    if (DIR == 0) {  // to_phys_x (SC:504-534)
+        s.v[2] = (b.u - b.c) * w[0] + b.u * w[1] + b.u * w[2] + (b.u + b.c) * w[5];
+        s.v[3] = b.v * (w[0] + w[1] + w[2] + w[5]) + w[3];
+    } else {  // to_phys_y (SC:559-589)
+        s.v[2] = b.u * (w[0] + w[1] + w[2] + w[5]) - w[3];
+        s.v[3] = (b.v - b.c) * w[0] + b.v * w[1] + b.v * w[2] + (b.v + b.c) * w[5];
+    }
+    s.v[4] = b.c2 * (w[0] + w[5]);
+    s.v[5] = w[4];
+    return s;
+}
+
+// ------------------------------------------------------------------------------------------------
+// HLLC flux and interface velocity (SC:594-771). One side's state with its sound speed and energy.
+// ------------------------------------------------------------------------------------------------
+template <typename T> struct Side {
+    T ar1, ar2, rho, un, ut, p, a, c, E;
+};
+
+// Flux f[0..5] in SC component order and the interface velocity u* for the alpha source.
+// hllc_x/hllc_y and hllc_x_src/hllc_y_src of the reference recompute the same wave speeds; here
+// they are computed once.
+template <int DIR, typename T>
+__device__ __forceinline__ void hllc(const Side<T> &L, const Side<T> &R, T f[6], T &ustar)
+{
+    constexpr int N = DIR == 0 ? 2 : 3;  // normal momentum component
+    constexpr int Tc = DIR == 0 ? 3 : 2; // tangential momentum component
+    T n_avg = T(0.5) * (L.un + R.un);
+    T c_avg = T(0.5) * (L.c + R.c);
+    T SL = wmin(L.un - L.c, n_avg - c_avg);
+    T SR = wmax(R.un + R.c, n_avg + c_avg);
+    T denom = L.rho * (SL - L.un) - R.rho * (SR - R.un);
+    if (wabs(denom) < T(kTiny)) denom = T(kTiny);
+    T SP = (R.p - L.p + L.rho * L.un * (SL - L.un) - R.rho * R.un * (SR - R.un)) / denom;
+    T ratioL = (SL - L.un) / (SL - SP);
+    T ratioR = (SR - R.un) / (SR - SP);
+
+    if (SL > T(0)) {
+        f[0] = L.ar1 * L.un;
+        f[1] = L.ar2 * L.un;
+        f[N] = L.rho * L.un * L.un + L.p;
+        f[Tc] = L.rho * L.un * L.ut;
+        f[4] = (L.E + L.p) * L.un;
+        f[5] = L.a * L.un;
+    } else if (SL <= T(0) && T(0) < SP) {
+        T ratio = ratioL;
+        T E_star = L.E + (SP - L.un) * (SP * L.rho + L.p / (SL - L.un));
+        f[0] = L.ar1 * L.un + SL * (L.ar1 * ratio - L.ar1);
+        f[1] = L.ar2 * L.un + SL * (L.ar2 * ratio - L.ar2);
+        f[N] = (L.rho * L.un * L.un + L.p) + SL * (L.rho * SP * ratio - L.rho * L.un);
+        f[Tc] = (L.rho * L.un * L.ut) + SL * (L.rho * L.ut * ratio - L.rho * L.ut);
+        f[4] = (L.E + L.p) * L.un + SL * (E_star * ratio - L.E);
+        f[5] = L.a * L.un + SL * (L.a * ratio - L.a);
+    } else if (SP <= T(0) && T(0) <= SR) {
+        T ratio = ratioR;
+        T E_star = R.E + (SP - R.un) * (SP * R.rho + R.p / (SR - R.un));
+        f[0] = R.ar1 * R.un + SR * (R.ar1 * ratio - R.ar1);
+        f[1] = R.ar2 * R.un + SR * (R.ar2 * ratio - R.ar2);
+        f[N] = (R.rho * R.un * R.un + R.p) + SR * (R.rho * SP * ratio - R.rho * R.un);
+        f[Tc] = (R.rho * R.un * R.ut) + SR * (R.rho * R.ut * ratio - R.rho * R.ut);
+        f[4] = (R.E + R.p) * R.un + SR * (E_star * ratio - R.E);
+        f[5] = R.a * R.un + SR * (R.a * ratio - R.a);
+    } else {
+        f[0] = R.ar1 * R.un;
+        f[1] = R.ar2 * R.un;
+        f[N] = R.rho * R.un * R.un + R.p;
+        f[Tc] = R.rho * R.un * R.ut;
+        f[4] = (R.E + R.p) * R.un;
+        f[5] = R.a * R.un;
+    }
+    T left_part = L.un + wmin(T(0), SL) * (ratioL - T(1));
+    T right_part = R.un + wmax(T(0), SR) * (ratioR - T(1));
+    T sp_sign = wsign(SP);
+    ustar = T(0.5) * (T(1) + sp_sign) * left_part + T(0.5) * (T(1) - sp_sign) * right_part;
+}
+
+// Blend of a high-order face value toward the first-order one (pp_blend_*_flux_kernel body,
+// SC:1506-1512). Shared by the in-place limiter and the fused stage so both round alike.
+__device__ __forceinline__ double face_blend(double low, double high, double theta)
+{
+    return low + theta * (high - low);
+}
+
+}  // namespace wm

@@ -1,0 +1,65 @@
+// wm_kernels.cuh -- kernels of the per-stage RHS and their launch-argument blocks.
+#pragma once
+#include "wm_device.cuh"
+
+namespace wm {
+
+enum { kSC = 0, kM10 = 1 };
+enum { kMuscl = 0, kMp5 = 1 };
+
+// The ten per-cell arrays of the reference (ar1, ar2, ru, rv, E, al, u_p, v_p, p_p, al_prim).
+struct Fields {
+    double *f[10];
+    long long pitch;
+};
+enum { F_AR1 = 0, F_AR2, F_RU, F_RV, F_E, F_AL, F_U, F_V, F_P, F_ALP };
+
+struct Face7 {
+    double *f[7];  // six flux components and the interface velocity
+};
+
+// Per-cell data computed once per stage and shared by the faces that use it.
+struct Prep {
+    double *ent;            // cell entropy p / rho^gamma (8 faces per direction read it)
+    double *cx, *cy;        // smoothness indicator along x and y
+    double *sx, *sy;        // Ducros x pressure sensor (SC only)
+    double *lu, *lv, *lp, *la, *lc, *lE;  // first-order HLLC cell state: velocity, floored
+                                          // pressure, clamped alpha, sound speed, energy
+};
+
+struct Counters {
+    unsigned long long *repaired, *nonfinite, *limited;
+    unsigned long long *dt_bits;  // atomic min of the positive dt candidates (bit pattern)
+};
+
+// Flags of final_kernel.
+enum : unsigned {
+    FIN_RK3 = 1u,         // rk3_update on interior cells
+    FIN_ADMISSIBLE = 2u,  // enforce_admissible on every cell
+    FIN_PRIM = 4u,        // cons_to_prim + al_prim copy on every cell
+    FIN_SAVE_OLD = 8u,    // copy the pre-update interior state to q_old (copy_old fused)
+    FIN_DT = 16u,         // accumulate the time-step candidate of interior cells
+    FIN_OLD_READ = 32u,   // rk3 reads q_old (alpha != 0)
+};
+
+void launch_bc(const Grid &g, const int bc[4], const Fields &q, const Fields *save_old,
+               cudaStream_t s);
+void launch_prep(const Grid &g, const Eos &e, const Fields &q, const Prep &p, int variant,
+                 cudaStream_t s);
+void launch_faces(const Grid &g, const Eos &e, int variant, int recon, const Fields &q,
+                  const Prep &p, const Face7 &fh, const Face7 &gh, const Face7 &fl, const Face7 &gl,
+                  bool high, bool low, cudaStream_t s);
+void launch_limiter(const Grid &g, const Eos &e, const Fields &q, const Face7 &fh, const Face7 &gh,
+                    const Face7 &fl, const Face7 &gl, double *const theta[3], double dt,
+                    const double *dt_dev, const Counters &cnt, cudaStream_t s);
+void launch_final(const Grid &g, const Eos &e, unsigned flags, const Fields &q, const Fields &old,
+                  const Face7 &fh, const Face7 &gh, double dt, const double *dt_dev, double alpha,
+                  double beta, const Counters &cnt, cudaStream_t s);
+void launch_copy_old(const Grid &g, const Fields &q, const Fields &old, cudaStream_t s);
+void launch_dt_reset(const Counters &cnt, cudaStream_t s);
+void launch_dt_cell(const Grid &g, const Eos &e, const Fields &q, const Counters &cnt,
+                    cudaStream_t s);
+void launch_dt_finalize(const Grid &g, const Counters &cnt, double *dt_out, cudaStream_t s);
+void launch_fp64_probe(double *out, int iters, cudaStream_t s, int blocks, int threads);
+
+}  // namespace wm

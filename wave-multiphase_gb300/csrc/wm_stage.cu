@@ -1,0 +1,447 @@
+// wm_stage.cu -- ghost fill, per-cell preparation, Wong limiter passes, RK3 combine with repair and
+// primitive recovery, and the time-step reduction (sm_103a, binary64).
+//
+// Thread mapping: threadIdx.x runs along j (the contiguous axis of every array) so that each warp
+// reads and writes 256-byte rows; blocks are 32 x 4 threads.
+#include "wm_kernels.cuh"
+
+namespace wm {
+
+namespace {
+
+constexpr int BX = 32, BY = 4;
+
+__device__ __forceinline__ long long kf_of(const Fields &q, int i, int j)
+{
+    return (long long)i * q.pitch + j;
+}
+__device__ __forceinline__ long long kw_of(const Grid &g, int i, int j)
+{
+    return (long long)i * g.nyg + j;
+}
+
+// Warp-aggregated counter increment (one atomic per warp).
+__device__ __forceinline__ void count_if(unsigned long long *ctr, bool pred)
+{
+    unsigned mask = __activemask();
+    unsigned b = __ballot_sync(mask, pred);
+    if (b && (threadIdx.x & 31) == (__ffs(mask) - 1)) atomicAdd(ctr, (unsigned long long)__popc(b));
+}
+
+// ------------------------------------------------------------------------------ ghost fill ----
+// bc_x_kernel (SC:1616-1646) generalised per side; kind 1 negates the normal momentum and velocity.
+__global__ void bc_x_kernel(Grid g, int bl, int br, Fields q, Fields old, int save)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int k = blockIdx.y * blockDim.y + threadIdx.y;
+    if (j >= g.nyg || k >= g.g) return;
+    int li = g.g - 1 - k, ri = g.g + g.nx + k;
+    long long kl = kf_of(q, li, j), kr = kf_of(q, ri, j);
+    long long sl = kf_of(q, g.g, j), sr = kf_of(q, g.g + g.nx - 1, j);
+#pragma unroll
+    for (int c = 0; c < 9; ++c) {
+        double *a = q.f[c];
+        if (save && c < 6) {  // copy_old of the ghost cells, before they are overwritten
+            old.f[c][(long long)li * old.pitch + j] = a[kl];
+            old.f[c][(long long)ri * old.pitch + j] = a[kr];
+        }
+        double vl = a[sl], vr = a[sr];
+        if (c == F_RU || c == F_U) {
+            if (bl == 1) vl = -1.0 * vl;
+            if (br == 1) vr = -1.0 * vr;
+        }
+        a[kl] = vl;
+        a[kr] = vr;
+    }
+}
+
+// bc_y_kernel (SC:1650-1682); runs after the x pass, so corners take the y rule.
+__global__ void bc_y_kernel(Grid g, int bb, int bt, Fields q, Fields old, int save)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (k >= g.g || i >= g.nxg) return;
+    int bj = g.g - 1 - k, tj = g.g + g.ny + k;
+    long long kb = kf_of(q, i, bj), kt = kf_of(q, i, tj);
+    long long sb = kf_of(q, i, g.g), st = kf_of(q, i, g.g + g.ny - 1);
+    bool save_here = save && i >= g.g && i < g.g + g.nx;  // corners were saved by the x pass
+#pragma unroll
+    for (int c = 0; c < 9; ++c) {
+        double *a = q.f[c];
+        if (save_here && c < 6) {
+            old.f[c][(long long)i * old.pitch + bj] = a[kb];
+            old.f[c][(long long)i * old.pitch + tj] = a[kt];
+        }
+        double vb = a[sb], vt = a[st];
+        if (c == F_RV || c == F_V) {
+            if (bb == 1) vb = -1.0 * vb;
+            if (bt == 1) vt = -1.0 * vt;
+        }
+        a[kb] = vb;
+        a[kt] = vt;
+    }
+}
+
+// --------------------------------------------------------------------------- per-cell prep ----
+// Entropy (SC:308-314) and the first-order HLLC cell state of fx_low_kernel (SC:1309-1327), both
+// pure functions of one cell, computed once per cell instead of once per face that reads them.
+__global__ void __launch_bounds__(BX *BY) prep_kernel(Grid g, Eos e, Fields q, Prep p)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.nxg || j >= g.nyg) return;
+    long long kf = kf_of(q, i, j), kw = kw_of(g, i, j);
+    double ar1 = q.f[F_AR1][kf], ar2 = q.f[F_AR2][kf], ru = q.f[F_RU][kf], rv = q.f[F_RV][kf];
+    double pp = q.f[F_P][kf], al = q.f[F_AL][kf];
+
+    double ge, pie;
+    mix_gamma_pinf(e, al, ge, pie);
+    double rho_e = ar1 + ar2;
+    if (rho_e < kTiny) rho_e = kTiny;
+    p.ent[kw] = pp / pow(rho_e, ge);
+
+    double rho = ar1 + ar2;
+    double ir = 1.0 / rho;
+    double a = clamp01_pp(al);
+    double gg = ge, pi = pie;
+    if (!(a == al)) mix_gamma_pinf(e, a, gg, pi);
+    double pl = pp;
+    if (isnan(pl) || (pl + pi) / (gg - 1.0) < kPpCtilde) pl = kPpCtilde * (gg - 1.0) - pi;
+    double u = ru * ir, v = rv * ir;
+    p.lu[kw] = u;
+    p.lv[kw] = v;
+    p.lp[kw] = pl;
+    p.la[kw] = a;
+    p.lc[kw] = sound_speed_r(e, ir, pl, a);
+    p.lE[kw] = prim_to_energy(e, rho, u, v, pl, a);
+}
+
+// Smoothness indicator per cell and direction (cator2_val, SC:318-325) and the Ducros x pressure
+// sensor (ducros_kernel, SC:875-916).
+__global__ void __launch_bounds__(BX *BY) sensor_kernel(Grid g, Fields q, Prep p, int sc)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.nxg || j >= g.nyg) return;
+    long long kw = kw_of(g, i, j);
+    const long long W = g.nyg;
+    const double *en = p.ent;
+    if (i >= 2 && i < g.nxg - 2)
+        p.cx[kw] = cator2_val(en[kw - 2 * W], en[kw - W], en[kw], en[kw + W], en[kw + 2 * W]);
+    if (j >= 2 && j < g.nyg - 2)
+        p.cy[kw] = cator2_val(en[kw - 2], en[kw - 1], en[kw], en[kw + 1], en[kw + 2]);
+    if (!sc) return;
+    if (i < 2 || i >= g.nxg - 2 || j < 2 || j >= g.nyg - 2) {
+        p.sx[kw] = 1.0;
+        p.sy[kw] = 1.0;
+        return;
+    }
+    const double *U = q.f[F_U], *V = q.f[F_V], *P = q.f[F_P];
+    long long kf = kf_of(q, i, j), Q = q.pitch;
+    double der_ux = 0.5 * (-U[kf - Q] + U[kf + Q]);
+    double der_vx = 0.5 * (-V[kf - Q] + V[kf + Q]);
+    double der_uy = 0.5 * (-U[kf - 1] + U[kf + 1]);
+    double der_vy = 0.5 * (-V[kf - 1] + V[kf + 1]);
+    double div_u = der_ux + der_vy;
+    double curl_u = der_vx - der_uy;
+    double ducros = div_u * div_u / (div_u * div_u + curl_u * curl_u + 1.0e-30);
+    double p0 = P[kf];
+    double pm2 = P[kf - 2 * Q], pm1 = P[kf - Q], pp1 = P[kf + Q], pp2 = P[kf + 2 * Q];
+    double aa = fabs(-pm2 + 16.0 * pm1 - 30.0 * p0 + 16.0 * pp1 - pp2);
+    double bb = fabs(pm2 + 16.0 * pm1 + 30.0 * p0 + 16.0 * pp1 + pp2);
+    p.sx[kw] = (aa / (bb + 1.0e-30)) * ducros;
+    pm2 = P[kf - 2];
+    pm1 = P[kf - 1];
+    pp1 = P[kf + 1];
+    pp2 = P[kf + 2];
+    aa = fabs(-pm2 + 16.0 * pm1 - 30.0 * p0 + 16.0 * pp1 - pp2);
+    bb = fabs(pm2 + 16.0 * pm1 + 30.0 * p0 + 16.0 * pp1 + pp2);
+    p.sy[kw] = (aa / (bb + 1.0e-30)) * ducros;
+}
+
+// --------------------------------------------------------------------------- Wong limiter ----
+// pp_cell_theta_kernel (SC:1397-1476): residuals of the current (partly blended) high-order and of
+// the first-order fluxes, bound solve of this pass.
+__global__ void __launch_bounds__(BX *BY)
+theta_kernel(Grid g, Eos e, Fields q, Face7 fh, Face7 gh, Face7 fl, Face7 gl, double *theta,
+             double dt, const double *dt_dev, int stage, unsigned long long *limited)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x + g.g;
+    int i = blockIdx.y * blockDim.y + threadIdx.y + g.g;
+    if (i >= g.g + g.nx || j >= g.g + g.ny) return;
+    if (dt_dev) dt = *dt_dev;
+    long long kf = kf_of(q, i, j), kw = kw_of(g, i, j), kx = kw - g.nyg, ky = kw - 1;
+    double a = q.f[F_ALP][kf];
+    double l[6], h[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        double rh = (fh.f[c][kw] - fh.f[c][kx]) * g.inv_dx + (gh.f[c][kw] - gh.f[c][ky]) * g.inv_dy;
+        double rl = (fl.f[c][kw] - fl.f[c][kx]) * g.inv_dx + (gl.f[c][kw] - gl.f[c][ky]) * g.inv_dy;
+        if (c == 5) {
+            rh = rh - a * (fh.f[6][kw] - fh.f[6][kx]) * g.inv_dx - a * (gh.f[6][kw] - gh.f[6][ky]) * g.inv_dy;
+            rl = rl - a * (fl.f[6][kw] - fl.f[6][kx]) * g.inv_dx - a * (gl.f[6][kw] - gl.f[6][ky]) * g.inv_dy;
+        }
+        double qc = q.f[c][kf];
+        l[c] = qc - dt * rl;
+        h[c] = qc - dt * rh;
+    }
+    double th = theta_cons_stage(e, l, h, stage);
+    theta[kw] = th;
+    if (limited) count_if(limited, th < 1.0);
+}
+
+// pp_blend_x_flux_kernel + pp_blend_y_flux_kernel (SC:1479-1548) in one launch: the thread at
+// (i, j) blends x-face (i, j) and y-face (i, j) when they exist. Face theta is the min over its
+// interior neighbours.
+__global__ void __launch_bounds__(BX *BY)
+blend_kernel(Grid g, Face7 fh, Face7 gh, Face7 fl, Face7 gl, const double *theta)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x + g.g - 1;
+    int i = blockIdx.y * blockDim.y + threadIdx.y + g.g - 1;
+    if (i >= g.g + g.nx || j >= g.g + g.ny) return;
+    long long kw = kw_of(g, i, j);
+    bool ii = i >= g.g, ji = j >= g.g;  // cell (i, j) interior along x / y
+    if (ji) {                           // x face between (i, j) and (i+1, j)
+        double th = 1.0;
+        if (ii) th = wmin(th, theta[kw]);
+        if (i + 1 < g.g + g.nx) th = wmin(th, theta[kw + g.nyg]);
+#pragma unroll
+        for (int c = 0; c < 7; ++c) fh.f[c][kw] = face_blend(fl.f[c][kw], fh.f[c][kw], th);
+    }
+    if (ii) {  // y face between (i, j) and (i, j+1)
+        double th = 1.0;
+        if (ji) th = wmin(th, theta[kw]);
+        if (j + 1 < g.g + g.ny) th = wmin(th, theta[kw + 1]);
+#pragma unroll
+        for (int c = 0; c < 7; ++c) gh.f[c][kw] = face_blend(gl.f[c][kw], gh.f[c][kw], th);
+    }
+}
+
+// ------------------------------------------------------- RK3 combine + repair + primitives ----
+// rk3_kernel (SC:1553-1611) on interior cells, then enforce_admissible_kernel (SC:918-958) and
+// cons_to_prim_kernel (SC:840-864) + al_prim copy on every cell, then the dt candidate of
+// timestep_kernel (SC:1686-1705) -- each step selected by `flags`.
+__global__ void __launch_bounds__(BX *BY)
+final_kernel(Grid g, Eos e, unsigned flags, Fields q, Fields old, Face7 fh, Face7 gh, double dt,
+             const double *dt_dev, double alpha, double beta, Counters cnt)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.y * blockDim.y + threadIdx.y;
+    bool inb = i < g.nxg && j < g.nyg;
+    bool interior = inb && i >= g.g && i < g.g + g.nx && j >= g.g && j < g.g + g.ny;
+    unsigned long long dt_bits = ~0ull;
+    if (inb && (interior || (flags & (FIN_ADMISSIBLE | FIN_PRIM)))) {
+        long long kf = kf_of(q, i, j);
+        double Q[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) Q[c] = q.f[c][kf];
+        bool wrote_q = false;
+        if (interior && (flags & FIN_SAVE_OLD)) {
+            long long ko = (long long)i * old.pitch + j;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) old.f[c][ko] = Q[c];
+        }
+        if (interior && (flags & FIN_RK3)) {
+            if (dt_dev) dt = *dt_dev;
+            long long kw = kw_of(g, i, j), kx = kw - g.nyg, ky = kw - 1;
+            double ap = q.f[F_ALP][kf];
+            double res[6];
+#pragma unroll
+            for (int c = 0; c < 5; ++c)
+                res[c] = (fh.f[c][kw] - fh.f[c][kx]) * g.inv_dx + (gh.f[c][kw] - gh.f[c][ky]) * g.inv_dy;
+            double src6x = ap * (fh.f[6][kw] - fh.f[6][kx]) * g.inv_dx;
+            double src6y = ap * (gh.f[6][kw] - gh.f[6][ky]) * g.inv_dy;
+            res[5] = (fh.f[5][kw] - fh.f[5][kx]) * g.inv_dx + (gh.f[5][kw] - gh.f[5][ky]) * g.inv_dy -
+                     src6x - src6y;
+            long long ko = (long long)i * old.pitch + j;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                double base = beta * (Q[c] - dt * res[c]);
+                Q[c] = (flags & FIN_OLD_READ) ? alpha * old.f[c][ko] + base : base;
+            }
+            wrote_q = true;
+        }
+        if (flags & FIN_ADMISSIBLE) {
+            double a1 = clamp01_pp(Q[F_AL]);
+            double m1 = Q[0], m2 = Q[1], mx = Q[2], my = Q[3], E = Q[4];
+            bool nonfinite = isnan(m1) || isnan(m2) || isnan(mx) || isnan(my) || isnan(E);
+            if (isnan(m1) || m1 < kPpRho) m1 = kPpRho;
+            if (isnan(m2) || m2 < kPpRho) m2 = kPpRho;
+            if (isnan(mx)) mx = 0.0;
+            if (isnan(my)) my = 0.0;
+            double rho = m1 + m2;
+            double ir = 1.0 / rho;
+            double uu = mx * ir, vv = my * ir;
+            double kin = 0.5 * rho * (uu * uu + vv * vv);
+            double gb, pb, gg, pi;
+            mix_gamma_pibig(e, a1, gb, pb);
+            double p = (E - pb - kin) / gb;
+            mix_gamma_pinf(e, a1, gg, pi);
+            double p_min = kPpCtilde * (gg - 1.0) - pi;
+            bool repair = isnan(E) || isnan(p) || (E - kin - pi) < kPpCtilde;
+            if (repair) E = gb * p_min + pb + kin;
+            Q[0] = m1;
+            Q[1] = m2;
+            Q[2] = mx;
+            Q[3] = my;
+            Q[4] = E;
+            Q[5] = a1;
+            wrote_q = true;
+            if (cnt.repaired) {
+                count_if(cnt.repaired, repair);
+                count_if(cnt.nonfinite, nonfinite);
+            }
+        }
+        if (flags & FIN_PRIM) {
+            double a1 = Q[F_AL];
+            if (a1 < kPrimAlphaFloor) a1 = kPrimAlphaFloor;
+            if (a1 > 1.0 - kPrimAlphaFloor) a1 = 1.0 - kPrimAlphaFloor;
+            Q[F_AL] = a1;
+            double rho = Q[0] + Q[1];
+            double ir = 1.0 / rho;
+            double uu = Q[2] * ir, vv = Q[3] * ir;
+            double gb, pb;
+            mix_gamma_pibig(e, a1, gb, pb);
+            double pp = (Q[4] - pb - 0.5 * rho * (uu * uu + vv * vv)) / gb;
+            q.f[F_U][kf] = uu;
+            q.f[F_V][kf] = vv;
+            q.f[F_P][kf] = pp;
+            q.f[F_ALP][kf] = a1;
+            q.f[F_AL][kf] = a1;
+            if (interior && (flags & FIN_DT)) {
+                double c = sound_speed_r(e, ir, pp, a1);
+                double sx = g.dx / (fabs(uu) + c);
+                double sy = g.dy / (fabs(vv) + c);
+                double d = sx * sy / (sx + sy);
+                dt_bits = (unsigned long long)__double_as_longlong(d);
+            }
+        }
+        if (wrote_q) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) q.f[c][kf] = Q[c];
+        }
+    }
+    if (flags & FIN_DT) {
+        for (int o = 16; o > 0; o >>= 1) {
+            unsigned long long other = __shfl_down_sync(0xffffffffu, dt_bits, o);
+            dt_bits = other < dt_bits ? other : dt_bits;
+        }
+        if ((threadIdx.x & 31) == 0 && dt_bits != ~0ull) atomicMin(cnt.dt_bits, dt_bits);
+    }
+}
+
+__global__ void copy_old_kernel(Grid g, Fields q, Fields old)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.nxg || j >= g.nyg) return;
+    long long kf = kf_of(q, i, j), ko = (long long)i * old.pitch + j;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) old.f[c][ko] = q.f[c][kf];
+}
+
+// timestep_kernel (SC:1686-1705) on the current primitives.
+__global__ void dt_cell_kernel(Grid g, Eos e, Fields q, unsigned long long *dt_bits)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x + g.g;
+    int i = blockIdx.y * blockDim.y + threadIdx.y + g.g;
+    unsigned long long bits = ~0ull;
+    if (i < g.g + g.nx && j < g.g + g.ny) {
+        long long kf = kf_of(q, i, j);
+        double rho = q.f[F_AR1][kf] + q.f[F_AR2][kf];
+        double c = sound_speed_r(e, 1.0 / rho, q.f[F_P][kf], q.f[F_AL][kf]);
+        double sx = g.dx / (fabs(q.f[F_U][kf]) + c);
+        double sy = g.dy / (fabs(q.f[F_V][kf]) + c);
+        bits = (unsigned long long)__double_as_longlong(sx * sy / (sx + sy));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long other = __shfl_down_sync(0xffffffffu, bits, o);
+        bits = other < bits ? other : bits;
+    }
+    if ((threadIdx.x & 31) == 0 && bits != ~0ull) atomicMin(dt_bits, bits);
+}
+
+__global__ void dt_reset_kernel(unsigned long long *dt_bits)
+{
+    *dt_bits = (unsigned long long)__double_as_longlong(1.0e30);  // get_dt's initial value
+}
+
+__global__ void dt_finalize_kernel(const unsigned long long *dt_bits, double cfl, double *dt_out)
+{
+    *dt_out = cfl * __longlong_as_double((long long)*dt_bits);
+}
+
+__global__ void fp64_probe_kernel(double *out, int iters)
+{
+    double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5,
+           x6 = x0 + 6, x7 = x0 + 7;
+    const double a = 0.999999, b = 1e-7;
+    for (int k = 0; k < iters; ++k) {
+        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+dim3 grid2(int nj, int ni) { return dim3((nj + BX - 1) / BX, (ni + BY - 1) / BY); }
+
+}  // namespace
+
+void launch_bc(const Grid &g, const int bc[4], const Fields &q, const Fields *save_old,
+               cudaStream_t s)
+{
+    Fields old = save_old ? *save_old : q;
+    int save = save_old != nullptr;
+    bc_x_kernel<<<dim3((g.nyg + 63) / 64, g.g), dim3(64, 1), 0, s>>>(g, bc[0], bc[1], q, old, save);
+    bc_y_kernel<<<dim3((g.g + 7) / 8, (g.nxg + 31) / 32), dim3(8, 32), 0, s>>>(g, bc[2], bc[3], q, old, save);
+}
+
+void launch_prep(const Grid &g, const Eos &e, const Fields &q, const Prep &p, int variant,
+                 cudaStream_t s)
+{
+    prep_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, e, q, p);
+    sensor_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, q, p, variant == kSC);
+}
+
+void launch_limiter(const Grid &g, const Eos &e, const Fields &q, const Face7 &fh, const Face7 &gh,
+                    const Face7 &fl, const Face7 &gl, double *const theta[3], double dt,
+                    const double *dt_dev, const Counters &cnt, cudaStream_t s)
+{
+    for (int st = 0; st < 3; ++st) {
+        theta_kernel<<<grid2(g.ny, g.nx), dim3(BX, BY), 0, s>>>(g, e, q, fh, gh, fl, gl, theta[st],
+                                                                dt, dt_dev, st, cnt.limited);
+        blend_kernel<<<grid2(g.ny + 1, g.nx + 1), dim3(BX, BY), 0, s>>>(g, fh, gh, fl, gl, theta[st]);
+    }
+}
+
+void launch_final(const Grid &g, const Eos &e, unsigned flags, const Fields &q, const Fields &old,
+                  const Face7 &fh, const Face7 &gh, double dt, const double *dt_dev, double alpha,
+                  double beta, const Counters &cnt, cudaStream_t s)
+{
+    final_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, e, flags, q, old, fh, gh, dt,
+                                                              dt_dev, alpha, beta, cnt);
+}
+
+void launch_copy_old(const Grid &g, const Fields &q, const Fields &old, cudaStream_t s)
+{
+    copy_old_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, q, old);
+}
+
+void launch_dt_reset(const Counters &cnt, cudaStream_t s) { dt_reset_kernel<<<1, 1, 0, s>>>(cnt.dt_bits); }
+
+void launch_dt_cell(const Grid &g, const Eos &e, const Fields &q, const Counters &cnt, cudaStream_t s)
+{
+    dt_cell_kernel<<<grid2(g.ny, g.nx), dim3(BX, BY), 0, s>>>(g, e, q, cnt.dt_bits);
+}
+
+void launch_dt_finalize(const Grid &g, const Counters &cnt, double *dt_out, cudaStream_t s)
+{
+    dt_finalize_kernel<<<1, 1, 0, s>>>(cnt.dt_bits, g.cfl, dt_out);
+}
+
+void launch_fp64_probe(double *out, int iters, cudaStream_t s, int blocks, int threads)
+{
+    fp64_probe_kernel<<<blocks, threads, 0, s>>>(out, iters);
+}
+
+}  // namespace wm

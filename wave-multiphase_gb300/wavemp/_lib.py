@@ -1,0 +1,98 @@
+"""ctypes binding of libwavemp.so (include/wavemp.h). Raises if the library is missing."""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import _build
+
+WM_OK = 0
+WM_ERR = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory / workspace too small",
+          -4: "call out of order"}
+
+VARIANT = {"sc": 0, "m10": 1}
+RECON = {"shipped": 0, "mp5c6": 1}
+BC = {"transmissive": 0, "slip": 1, "reflective": 1}
+PRECISION = {"fp64": 0, "fp32": 1}
+
+WS_FX, WS_GY, WS_FXL, WS_GYL, WS_THETA, WS_SIGMA_X, WS_SIGMA_Y = 0, 7, 14, 21, 28, 31, 32
+
+
+class WmParams(ctypes.Structure):
+    _fields_ = [("gamma1", ctypes.c_double), ("pinf1", ctypes.c_double),
+                ("gamma2", ctypes.c_double), ("pinf2", ctypes.c_double),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("cfl", ctypes.c_double),
+                ("variant", ctypes.c_int), ("recon", ctypes.c_int), ("bc", ctypes.c_int * 4),
+                ("emergency_repair", ctypes.c_int), ("precision", ctypes.c_int)]
+
+
+class WmFields(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in
+                ("ar1", "ar2", "ru", "rv", "E", "al", "u_p", "v_p", "p_p", "al_prim")] + \
+               [("pitch", ctypes.c_longlong)]
+
+
+class WmStats(ctypes.Structure):
+    _fields_ = [("repaired_cells", ctypes.c_longlong), ("nonfinite_cells", ctypes.c_longlong),
+                ("limited_cells", ctypes.c_longlong), ("steps", ctypes.c_longlong)]
+
+
+EXPORTS = ("wm_version", "wm_last_error", "wm_workspace_bytes", "wm_create", "wm_destroy",
+           "wm_apply_bc", "wm_compute_fluxes", "wm_compute_low_fluxes", "wm_limit_fluxes",
+           "wm_rk3_update", "wm_enforce_admissible", "wm_update_prims", "wm_copy_old",
+           "wm_get_dt", "wm_rhs_stage", "wm_step", "wm_init_dt", "wm_read_workspace", "wm_status",
+           "wm_profile", "wm_profile_read", "wm_probe_fp64_flops")
+PROF_GROUPS = ("bc", "prep", "faces", "limiter", "final")
+
+_lib = None
+
+
+class WavempError(RuntimeError):
+    pass
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load libwavemp.so; build it first if it is missing or older than its sources."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if build_if_missing:
+        path = _build.build()
+    if not os.path.exists(path):
+        raise WavempError(f"libwavemp.so not found at {path}; run wavemp._build.build()")
+    L = ctypes.CDLL(path)
+    vp, i, d = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    P, F = ctypes.POINTER(WmParams), ctypes.POINTER(WmFields)
+    L.wm_version.restype = ctypes.c_char_p
+    L.wm_last_error.restype = ctypes.c_char_p
+    L.wm_workspace_bytes.argtypes = [P, i, i, i]
+    L.wm_workspace_bytes.restype = ctypes.c_size_t
+    L.wm_create.argtypes = [P, i, i, i, vp, ctypes.c_size_t, ctypes.POINTER(vp)]
+    L.wm_destroy.argtypes = [vp]
+    L.wm_destroy.restype = None
+    for name in ("wm_apply_bc", "wm_compute_fluxes", "wm_compute_low_fluxes",
+                 "wm_enforce_admissible", "wm_update_prims", "wm_init_dt"):
+        getattr(L, name).argtypes = [vp, F, vp]
+    L.wm_limit_fluxes.argtypes = [vp, F, d, vp]
+    L.wm_rk3_update.argtypes = [vp, F, F, d, d, d, vp]
+    L.wm_copy_old.argtypes = [vp, F, F, vp]
+    L.wm_get_dt.argtypes = [vp, F, ctypes.POINTER(d), vp]
+    L.wm_rhs_stage.argtypes = [vp, F, F, d, d, d, vp]
+    L.wm_step.argtypes = [vp, F, F, d, ctypes.POINTER(d), vp]
+    L.wm_read_workspace.argtypes = [vp, i, vp, vp]
+    L.wm_status.argtypes = [vp, ctypes.POINTER(WmStats), i, vp]
+    L.wm_probe_fp64_flops.argtypes = [ctypes.POINTER(d), vp]
+    L.wm_profile.argtypes = [vp, i]
+    L.wm_profile_read.argtypes = [vp, ctypes.POINTER(d * 5), ctypes.POINTER(ctypes.c_longlong * 5), i]
+    for name in EXPORTS:
+        if name not in ("wm_version", "wm_last_error", "wm_workspace_bytes", "wm_destroy"):
+            getattr(L, name).restype = i
+    _lib = L
+    return L
+
+
+def check(rc: int, what: str):
+    if rc != WM_OK:
+        msg = _lib.wm_last_error().decode() if _lib is not None else ""
+        raise WavempError(f"{what} failed: {WM_ERR.get(rc, rc)} {msg}")

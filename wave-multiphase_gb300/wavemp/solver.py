@@ -1,0 +1,202 @@
+"""Python front end of the GB300 RHS: the reference's closures over torch float64 CUDA tensors.
+
+The reference keeps 47 module-level Warp arrays and drives them with closures inside ``main()``
+(SC:1839-1995). ``Solver`` owns the workspace those closures need (fluxes, limiter factors,
+sensors) and exposes each closure as a method with the reference's name and argument meaning.
+The state is a dict of the ten per-cell arrays ``ar1, ar2, ru, rv, E, al, u_p, v_p, p_p, al_prim``
+(SC:1839-1841), each a ``torch.float64`` CUDA tensor of shape ``(nx + 2g, ny + 2g)``, x first,
+y contiguous -- the reference's layout. Every call is enqueued on torch's current CUDA stream.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _lib
+from .params import SolverParams
+
+FIELDS = ("ar1", "ar2", "ru", "rv", "E", "al")
+PRIMS = ("u_p", "v_p", "p_p")
+ALL = FIELDS + PRIMS + ("al_prim",)
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def alloc_state(nx: int, ny: int, g: int = 5, device="cuda", names=ALL) -> dict:
+    """Zeroed state arrays, one contiguous (10, nx+2g, ny+2g) block viewed per field."""
+    block = torch.zeros((len(names), nx + 2 * g, ny + 2 * g), dtype=torch.float64, device=device)
+    return {k: block[c] for c, k in enumerate(names)}
+
+
+class Solver:
+    """Per-stage RHS of the 2-D five-equation stiffened-gas model on one GPU.
+
+    ``Solver(params, nx, ny, g=5)`` allocates its workspace with torch on the current CUDA
+    device. Methods mirror the reference's closures (``apply_bc``, ``compute_fluxes``,
+    ``compute_low_fluxes``, ``limit_fluxes``, ``rk3_update``, ``enforce_admissible``,
+    ``update_prims``, ``copy_old``, ``get_dt``) and add the fused ``rhs_stage`` and ``step``.
+    """
+
+    def __init__(self, params: SolverParams, nx: int, ny: int, g: int = 5, device=None):
+        if not torch.cuda.is_available():
+            raise _lib.WavempError("wavemp needs a CUDA device (there is no CPU path)")
+        self.L = _lib.load()
+        self.params = params
+        self.nx, self.ny, self.g = nx, ny, g
+        self.nxg, self.nyg = nx + 2 * g, ny + 2 * g
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self._cp = params.to_c()
+        nbytes = self.L.wm_workspace_bytes(ctypes.byref(self._cp), nx, ny, g)
+        if nbytes == 0:
+            raise ValueError("invalid solver parameters or grid size")
+        with torch.cuda.device(self.device):
+            self._ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+            h = ctypes.c_void_p()
+            _lib.check(self.L.wm_create(ctypes.byref(self._cp), nx, ny, g,
+                                        ctypes.c_void_p(self._ws.data_ptr()), nbytes,
+                                        ctypes.byref(h)), "wm_create")
+        self._h = h
+        self._dt_host = ctypes.c_double(0.0)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self.L.wm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- argument marshalling ------------------------------------------------------------------
+    def _fields(self, q: dict, need_prims: bool = True) -> _lib.WmFields:
+        f = _lib.WmFields()
+        pitch = None
+        for k in ALL:
+            t = q.get(k)
+            if t is None:
+                if need_prims or k in FIELDS:
+                    raise ValueError(f"state is missing field {k!r}")
+                continue
+            if t.dtype != torch.float64 or not t.is_cuda or t.dim() != 2:
+                raise ValueError(f"{k}: expected a 2-D torch.float64 CUDA tensor")
+            if tuple(t.shape) != (self.nxg, self.nyg) or t.stride(1) != 1:
+                raise ValueError(f"{k}: expected shape {(self.nxg, self.nyg)} with contiguous rows")
+            if pitch is None:
+                pitch = t.stride(0)
+            elif t.stride(0) != pitch:
+                raise ValueError("all fields must share one row pitch")
+            setattr(f, k, t.data_ptr())
+        f.pitch = pitch
+        return f
+
+    # -- the reference's closures (SC:1894-1995) ------------------------------------------------
+    def apply_bc(self, q):
+        _lib.check(self.L.wm_apply_bc(self._h, ctypes.byref(self._fields(q)), _stream()), "apply_bc")
+
+    def compute_fluxes(self, q):
+        _lib.check(self.L.wm_compute_fluxes(self._h, ctypes.byref(self._fields(q)), _stream()),
+                   "compute_fluxes")
+
+    def compute_low_fluxes(self, q):
+        _lib.check(self.L.wm_compute_low_fluxes(self._h, ctypes.byref(self._fields(q)), _stream()),
+                   "compute_low_fluxes")
+
+    def limit_fluxes(self, q, dt: float):
+        _lib.check(self.L.wm_limit_fluxes(self._h, ctypes.byref(self._fields(q)), float(dt),
+                                          _stream()), "limit_fluxes")
+
+    def rk3_update(self, q, q_old, alpha: float, beta: float, dt: float):
+        old = self._fields(q_old, need_prims=False) if q_old is not None else None
+        _lib.check(self.L.wm_rk3_update(self._h, ctypes.byref(self._fields(q)),
+                                        ctypes.byref(old) if old is not None else None,
+                                        float(alpha), float(beta), float(dt), _stream()),
+                   "rk3_update")
+
+    def enforce_admissible(self, q):
+        _lib.check(self.L.wm_enforce_admissible(self._h, ctypes.byref(self._fields(q)), _stream()),
+                   "enforce_admissible")
+
+    def update_prims(self, q):
+        _lib.check(self.L.wm_update_prims(self._h, ctypes.byref(self._fields(q)), _stream()),
+                   "update_prims")
+
+    def copy_old(self, q, q_old):
+        _lib.check(self.L.wm_copy_old(self._h, ctypes.byref(self._fields(q, need_prims=False)),
+                                      ctypes.byref(self._fields(q_old, need_prims=False)),
+                                      _stream()), "copy_old")
+
+    def get_dt(self, q) -> float:
+        _lib.check(self.L.wm_get_dt(self._h, ctypes.byref(self._fields(q)),
+                                    ctypes.byref(self._dt_host), _stream()), "get_dt")
+        return self._dt_host.value
+
+    def initialize(self, q):
+        """The reference's start-up sequence (SC:1998-2007 minus I/O): enforce_admissible,
+        apply_bc, update_prims, apply_bc."""
+        self.enforce_admissible(q)
+        self.apply_bc(q)
+        self.update_prims(q)
+        self.apply_bc(q)
+
+    # -- fused forms ----------------------------------------------------------------------------
+    def rhs_stage(self, q, q_old, dt: float, alpha: float, beta: float):
+        """One SSP-RK3 stage (SC:2030-2055 body); updates q in place."""
+        old = self._fields(q_old, need_prims=False) if q_old is not None else None
+        _lib.check(self.L.wm_rhs_stage(self._h, ctypes.byref(self._fields(q)),
+                                       ctypes.byref(old) if old is not None else None,
+                                       float(dt), float(alpha), float(beta), _stream()),
+                   "rhs_stage")
+
+    def init_dt(self, q):
+        """Compute the next step's dt on the device (no host wait)."""
+        _lib.check(self.L.wm_init_dt(self._h, ctypes.byref(self._fields(q)), _stream()), "init_dt")
+
+    def step(self, q, q_old, dt: float | None = None, sync: bool = True):
+        """One SSP-RK3 step (SC:2033-2059). dt=None uses the device-resident dt of the previous
+        step (or of init_dt). Returns the next dt as a float when sync, else None."""
+        out = ctypes.byref(self._dt_host) if sync else None
+        _lib.check(self.L.wm_step(self._h, ctypes.byref(self._fields(q)),
+                                  ctypes.byref(self._fields(q_old, need_prims=False)),
+                                  float(dt) if dt is not None else 0.0, out, _stream()), "step")
+        return self._dt_host.value if sync else None
+
+    # -- diagnostics ----------------------------------------------------------------------------
+    def workspace(self, which: int) -> torch.Tensor:
+        out = torch.empty((self.nxg, self.nyg), dtype=torch.float64, device=self.device)
+        _lib.check(self.L.wm_read_workspace(self._h, int(which), ctypes.c_void_p(out.data_ptr()),
+                                            _stream()), "read_workspace")
+        return out
+
+    def fluxes(self, which: str = "high") -> tuple[list, list]:
+        base_x, base_y = (_lib.WS_FX, _lib.WS_GY) if which == "high" else (_lib.WS_FXL, _lib.WS_GYL)
+        return ([self.workspace(base_x + c) for c in range(7)],
+                [self.workspace(base_y + c) for c in range(7)])
+
+    def profile(self, enable: bool = True):
+        """Record CUDA events around each kernel group of every stage (see profile_read)."""
+        _lib.check(self.L.wm_profile(self._h, int(bool(enable))), "profile")
+
+    def profile_read(self, reset: bool = True) -> dict:
+        """{group: (milliseconds, launches)} summed since the last reset."""
+        ms = (ctypes.c_double * 5)()
+        n = (ctypes.c_longlong * 5)()
+        _lib.check(self.L.wm_profile_read(self._h, ctypes.byref(ms), ctypes.byref(n), int(reset)),
+                   "profile_read")
+        return {g: (ms[i], n[i]) for i, g in enumerate(_lib.PROF_GROUPS)}
+
+    def status(self, reset: bool = False) -> dict:
+        st = _lib.WmStats()
+        _lib.check(self.L.wm_status(self._h, ctypes.byref(st), int(reset), _stream()), "status")
+        return {k: getattr(st, k) for k, _ in _lib.WmStats._fields_}
+
+
+def probe_fp64_flops() -> float:
+    L = _lib.load()
+    v = ctypes.c_double()
+    _lib.check(L.wm_probe_fp64_flops(ctypes.byref(v), _stream()), "probe_fp64_flops")
+    return v.value
