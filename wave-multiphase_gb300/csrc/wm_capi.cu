@@ -57,6 +57,11 @@ bool valid_params(const wm_params *p, int nx, int ny, int g)
 
 }  // namespace
 
+namespace wm {
+// Sets the text returned by wm_last_error() (used by entry points defined in other files).
+void set_error_text(const char *msg) { snprintf(g_last_error, sizeof g_last_error, "%s", msg); }
+}  // namespace wm
+
 struct wm_handle {
     wm_params P;
     Grid g;

@@ -1,0 +1,170 @@
+// wm_static.cu -- one RHS stage whose workspace is a statically allocated device array.
+//
+// Some callers cannot allocate device memory: a host application that hands out every byte of
+// device memory from its own pool and does not let libraries call cudaMalloc, or a loop that must
+// never wait on the allocator. For them wm_rhs_stage_static runs the same stage as wm_rhs_stage
+// (same kernels, same arithmetic) without a handle and without allocating: the face fluxes,
+// limiter factors and per-cell sensors live in wm_stage_scratch below, a file-scope device array
+// sized for grids of at most WM_STATIC_MAX_CELLS padded cells. Every GPU that loads this library
+// keeps that array (about 10.5 MiB) until the process exits.
+//
+// The array is shared by every call on a device and keeps the previous call's contents. Nothing
+// in it needs to start at zero: each entry a stage reads is written earlier in the same stage.
+// Two calls that overlap on the GPU (different streams, or different host threads) race on it.
+#include <cmath>
+#include <cstdio>
+#include <mutex>
+
+#include "../../include/wavemp.h"
+#include "wm_kernels.cuh"
+
+namespace wm {
+void set_error_text(const char *msg);  // wm_capi.cu: the text returned by wm_last_error()
+}
+
+using namespace wm;
+
+namespace {
+
+constexpr int kArrays = 42;  // 28 face arrays, 3 limiter factors, 11 per-cell arrays
+constexpr size_t kArrayBytes = ((size_t)WM_STATIC_MAX_CELLS * sizeof(double) + 255) / 256 * 256;
+constexpr size_t kScratchBytes = (size_t)kArrays * kArrayBytes;
+
+static __device__ __align__(256) unsigned char wm_stage_scratch[kScratchBytes];
+
+constexpr int kMaxDevices = 64;
+void *g_scratch[kMaxDevices] = {nullptr};
+std::mutex g_scratch_mutex;
+
+// Device address of wm_stage_scratch on the current device. The host-side name of the array is
+// only a stand-in for it, so the address is looked up once per device, with that device current.
+int scratch_address(void **out)
+{
+    int dev = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        set_error_text("wm_rhs_stage_static: no usable current CUDA device");
+        return WM_ERR_CUDA;
+    }
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch[dev]) {
+        void *p = nullptr;
+        err = cudaGetSymbolAddress(&p, wm_stage_scratch);
+        if (err != cudaSuccess || !p) {
+            char msg[256];
+            snprintf(msg, sizeof msg, "wm_rhs_stage_static: cudaGetSymbolAddress failed: %s",
+                     cudaGetErrorString(err));
+            set_error_text(msg);
+            return WM_ERR_CUDA;
+        }
+        g_scratch[dev] = p;
+    }
+    *out = g_scratch[dev];
+    return WM_OK;
+}
+
+bool params_ok(const wm_params *p, int nx, int ny, int g)
+{
+    if (!p || nx < 1 || ny < 1 || g < 4 || g > 64) return false;
+    if (!(p->gamma1 > 1.0) || !(p->gamma2 > 1.0) || !(p->dx > 0.0) || !(p->dy > 0.0)) return false;
+    if (!std::isfinite(p->pinf1) || !std::isfinite(p->pinf2) || !(p->cfl > 0.0)) return false;
+    if (p->variant != WM_VARIANT_SC && p->variant != WM_VARIANT_M10) return false;
+    if (p->recon != WM_RECON_SHIPPED && p->recon != WM_RECON_MP5C6) return false;
+    if (p->precision != WM_PREC_FP64) return false;
+    for (int k = 0; k < 4; ++k)
+        if (p->bc[k] != WM_BC_TRANSMISSIVE && p->bc[k] != WM_BC_SLIP) return false;
+    return true;
+}
+
+bool fields_ok(const wm_fields *q, int nyg, bool need_prims)
+{
+    if (!q || q->pitch < nyg) return false;
+    double *const f[10] = {q->ar1, q->ar2, q->ru, q->rv, q->E, q->al, q->u_p, q->v_p, q->p_p, q->al_prim};
+    for (int c = 0; c < (need_prims ? 10 : 6); ++c)
+        if (!f[c] || ((uintptr_t)f[c] & 7u)) return false;
+    return true;
+}
+
+Fields fields_of(const wm_fields *q)
+{
+    Fields F;
+    F.f[0] = q->ar1; F.f[1] = q->ar2; F.f[2] = q->ru; F.f[3] = q->rv; F.f[4] = q->E; F.f[5] = q->al;
+    F.f[6] = q->u_p; F.f[7] = q->v_p; F.f[8] = q->p_p; F.f[9] = q->al_prim;
+    F.pitch = q->pitch;
+    return F;
+}
+
+}  // namespace
+
+extern "C" int wm_rhs_stage_static(const wm_params *p, int nx, int ny, int g, const wm_fields *q,
+                                   const wm_fields *q_old, double dt, double alpha, double beta,
+                                   void *stream)
+{
+    if (!params_ok(p, nx, ny, g)) {
+        set_error_text("wm_rhs_stage_static: invalid parameters");
+        return WM_ERR_INVALID;
+    }
+    const long long cells = (long long)(nx + 2 * g) * (long long)(ny + 2 * g);
+    if (cells > (long long)WM_STATIC_MAX_CELLS) {
+        char msg[256];
+        snprintf(msg, sizeof msg,
+                 "wm_rhs_stage_static: grid of %lld padded cells exceeds the static scratch limit "
+                 "of %d padded cells; use wm_create + wm_rhs_stage",
+                 cells, (int)WM_STATIC_MAX_CELLS);
+        set_error_text(msg);
+        return WM_ERR_INVALID;
+    }
+    if (!fields_ok(q, ny + 2 * g, true) || !std::isfinite(dt) || !std::isfinite(alpha) ||
+        !std::isfinite(beta) || (alpha != 0.0 && !fields_ok(q_old, ny + 2 * g, false))) {
+        set_error_text("wm_rhs_stage_static: invalid field pointers, pitch or coefficients");
+        return WM_ERR_INVALID;
+    }
+    void *base = nullptr;
+    int rc = scratch_address(&base);
+    if (rc) return rc;
+
+    Grid G;
+    G.nx = nx; G.ny = ny; G.g = g; G.nxg = nx + 2 * g; G.nyg = ny + 2 * g; G.pitch = G.nyg;
+    G.dx = p->dx; G.dy = p->dy; G.inv_dx = 1.0 / p->dx; G.inv_dy = 1.0 / p->dy; G.cfl = p->cfl;
+    Eos E;
+    E.g1 = p->gamma1; E.p1 = p->pinf1; E.g2 = p->gamma2; E.p2 = p->pinf2;
+    E.r1 = 1.0 / (p->gamma1 - 1.0); E.r2 = 1.0 / (p->gamma2 - 1.0);
+    E.k1 = p->gamma1 * p->pinf1 / (p->gamma1 - 1.0); E.k2 = p->gamma2 * p->pinf2 / (p->gamma2 - 1.0);
+    E.thinc_t1 = std::tanh(1.8 * 0.5);
+    E.thinc_inv_t1 = 1.0 / E.thinc_t1;
+
+    double *arr[kArrays];
+    for (int a = 0; a < kArrays; ++a)
+        arr[a] = reinterpret_cast<double *>(static_cast<unsigned char *>(base) + (size_t)a * kArrayBytes);
+    Face7 fh, gh, fl, gl;
+    for (int c = 0; c < 7; ++c) {
+        fh.f[c] = arr[c];
+        gh.f[c] = arr[7 + c];
+        fl.f[c] = arr[14 + c];
+        gl.f[c] = arr[21 + c];
+    }
+    double *theta[3] = {arr[28], arr[29], arr[30]};
+    Prep P;
+    P.sx = arr[31]; P.sy = arr[32]; P.ent = arr[33]; P.cx = arr[34]; P.cy = arr[35];
+    P.lu = arr[36]; P.lv = arr[37]; P.lp = arr[38]; P.la = arr[39]; P.lc = arr[40]; P.lE = arr[41];
+    Counters none = {nullptr, nullptr, nullptr, nullptr};
+
+    Fields F = fields_of(q), O = alpha != 0.0 ? fields_of(q_old) : F;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    launch_bc(G, p->bc, F, nullptr, s);
+    launch_prep(G, E, F, P, p->variant, s);
+    launch_faces(G, E, p->variant, p->recon, F, P, fh, gh, fl, gl, true, true, s);
+    launch_limiter(G, E, F, fh, gh, fl, gl, theta, dt, nullptr, none, s);
+    unsigned flags = FIN_RK3 | FIN_PRIM;
+    if (p->emergency_repair) flags |= FIN_ADMISSIBLE;
+    if (alpha != 0.0) flags |= FIN_OLD_READ;
+    launch_final(G, E, flags, F, O, fh, gh, dt, nullptr, alpha, beta, none, s);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) {
+        char msg[256];
+        snprintf(msg, sizeof msg, "wm_rhs_stage_static: %s", cudaGetErrorString(err));
+        set_error_text(msg);
+        return WM_ERR_CUDA;
+    }
+    return WM_OK;
+}

@@ -41,7 +41,8 @@ EXPORTS = ("wm_version", "wm_last_error", "wm_workspace_bytes", "wm_create", "wm
            "wm_apply_bc", "wm_compute_fluxes", "wm_compute_low_fluxes", "wm_limit_fluxes",
            "wm_rk3_update", "wm_enforce_admissible", "wm_update_prims", "wm_copy_old",
            "wm_get_dt", "wm_rhs_stage", "wm_step", "wm_init_dt", "wm_read_workspace", "wm_status",
-           "wm_profile", "wm_profile_read", "wm_probe_fp64_flops")
+           "wm_profile", "wm_profile_read", "wm_probe_fp64_flops", "wm_rhs_stage_static")
+STATIC_MAX_CELLS = 32768
 PROF_GROUPS = ("bc", "prep", "faces", "limiter", "final")
 
 _lib = None
@@ -84,6 +85,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.wm_status.argtypes = [vp, ctypes.POINTER(WmStats), i, vp]
     L.wm_probe_fp64_flops.argtypes = [ctypes.POINTER(d), vp]
     L.wm_profile.argtypes = [vp, i]
+    L.wm_rhs_stage_static.argtypes = [P, i, i, i, F, F, d, d, d, vp]
     L.wm_profile_read.argtypes = [vp, ctypes.POINTER(d * 5), ctypes.POINTER(ctypes.c_longlong * 5), i]
     for name in EXPORTS:
         if name not in ("wm_version", "wm_last_error", "wm_workspace_bytes", "wm_destroy"):
