@@ -82,9 +82,33 @@ def test_ragged_tiny_grids_vs_oracle(nx, ny):
     assert_state(q, o, params, f"{nx}x{ny}")
 
 
+def oracle_self_sensitivity(state, nx, ny, params, steps):
+    """Largest natural-unit change of the oracle's result when its input gets 1e-15 relative noise."""
+    P = orc.make_params(params.dx, params.dy, params.gamma1, params.pinf1, params.gamma2,
+                        params.pinf2)
+    outs = []
+    for seed in (None, 1, 2):
+        o = orc.OracleSolver(nx, ny, P)
+        if seed is None:
+            o.load(state)
+        else:
+            r = np.random.default_rng(seed)
+            o.load({k: v * (1 + 1e-15 * r.standard_normal(v.shape)) for k, v in state.items()})
+        o.init_sequence()
+        dt = o.get_dt()
+        for _ in range(steps):
+            dt = o.step(dt)
+        outs.append({k: o.f[k].copy() for k in pu.ALL})
+    sc = pu.natural_scales(outs[0], params.gamma1, params.pinf1, params.gamma2, params.pinf2)
+    return max(pu.cell_err(x, outs[0], k, sc) for x in outs[1:] for k in pu.ALL)
+
+
 def test_poisoned_cells_are_repaired_like_the_reference():
     """NaN in the input state: the reference's isnan guards and the emergency repair decide the
-    outcome; the GPU must make the same decisions as the oracle."""
+    outcome; the GPU must make the same decisions as the oracle. A repaired cell sits at the
+    pressure floor (rho c~^2 = 1e-8, sound speed ~0), which makes its neighbours' Riemann problems
+    nearly singular: the oracle's own result moves by ~2e-9 under 1e-15 input noise here, so the
+    tolerance is ten times that measured sensitivity (at least 1e-9)."""
     nx, ny = 24, 16
     params = SolverParams(dx=0.01, dy=0.01, gamma1=4.4, pinf1=6e8)
     rng = np.random.default_rng(3)
@@ -92,11 +116,13 @@ def test_poisoned_cells_are_repaired_like_the_reference():
     st["E"][12, 9] = np.nan
     st["ar2"][14, 12] = np.nan
     st["ru"][8, 15] = np.nan
+    tol = max(1e-9, 10.0 * oracle_self_sensitivity(st, nx, ny, params, steps=1))
+    assert tol < 1e-7
     o, q, _, _ = run_both(st, nx, ny, params, steps=1)
     for k in pu.ALL:
         a, b = pu.host(q[k]), o.f[k]
         assert np.array_equal(np.isnan(a), np.isnan(b)), f"NaN pattern {k}"
-    assert_state(q, o, params, "poisoned")
+    assert_state(q, o, params, "poisoned", rtol=tol)
 
 
 # ---------------------------------------------------------------- properties at full size -----
