@@ -37,8 +37,8 @@ for _p in (ROOT, os.path.join(ROOT, "wave-multiphase_gb300")):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
-WORKLOAD = "triple_point_7168x3072"
 NX, NY, G = 7168, 3072, 5
+WORKLOAD = f"triple_point_{NX}x{NY}"
 ALG_BYTES_PER_CELL_STAGE = 128.0     # read stage state + step-start state, write new state (avg)
 SAMPLE_NX, SAMPLE_NY = 3584, 1536    # CPU sample: a quarter of the cells of the same problem
 # Face-sweep binary64 work per face (x or y) and traffic per cell-stage, from the ncu captures
@@ -47,9 +47,10 @@ FP64_FLOP_PER_FACE = None
 DRAM_BYTES_PER_CELL_STAGE = None
 
 
-def params(nx=NX, ny=NY):
+def params(nx=None, ny=None):
     import wavemp
 
+    nx, ny = nx or NX, ny or NY
     return wavemp.SolverParams(dx=7.0 / nx, dy=3.0 / ny, gamma1=1.5, pinf1=0.0, gamma2=1.4,
                                pinf2=0.0, variant="sc", recon="mp5c6", bc=("slip",) * 4, cfl=0.4)
 
@@ -314,7 +315,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grid", default=None,
+                    help="NXxNY: a smaller case of the same problem (profiling captures only)")
     args = ap.parse_args()
+    if args.grid:
+        global NX, NY, WORKLOAD
+        NX, NY = (int(v) for v in args.grid.lower().split("x"))
+        WORKLOAD = f"triple_point_{NX}x{NY}"
     if args.warmup < 3:
         print("note: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
