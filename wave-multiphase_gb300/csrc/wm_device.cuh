@@ -77,14 +77,17 @@ __device__ __forceinline__ void mix_gamma_pibig(const Eos &e, T a1, T &gb, T &pb
     pb = a1 * T(e.k1) + a2 * T(e.k2);
 }
 
-// mixture gamma and p_inf
+// mixture gamma and p_inf: g = 1/Gamma + 1, p_inf = (g-1) Pi / g = Pi / (1 + Gamma), with the two
+// reciprocals taken from one division 1 / (Gamma (1 + Gamma)).
 template <typename T>
 __device__ __forceinline__ void mix_gamma_pinf(const Eos &e, T a1, T &g, T &pi)
 {
     T gb, pb;
     mix_gamma_pibig(e, a1, gb, pb);
-    g = T(1) / gb + T(1);
-    pi = (g - T(1)) * pb / g;
+    const T gp1 = T(1) + gb;
+    const T inv = T(1) / (gb * gp1);
+    g = gp1 * inv + T(1);
+    pi = pb * (gb * inv);
 }
 
 // sound_speed(rho, p, a1) with 1/rho supplied
@@ -211,6 +214,25 @@ __device__ __forceinline__ double rho_ctilde2_cons(const Eos &e, double m1, doub
     double g, pi;
     mix_gamma_pinf(e, a1, g, pi);
     return E - kin - pi;
+}
+
+// Limiter factor of pass 2 (the rho c~^2 bound of theta_cons_stage, SC:283-286) evaluating the
+// low-order bound value only when it can change the result: pp_theta_lower returns 1 when the
+// high-order value is at or above the floor and neither value is NaN, and the low-order value
+// lc = E - kin - p_inf can only be NaN when one of l[2..4] is not finite.
+__device__ __forceinline__ double theta_ctilde(const Eos &e, const double l[6], const double h[6])
+{
+    double hc = rho_ctilde2_cons(e, h[0], h[1], h[2], h[3], h[4], h[5]);
+    double theta;
+    if (!isnan(hc) && !(hc < kPpCtilde) && isfinite(l[2]) && isfinite(l[3]) && isfinite(l[4])) {
+        theta = 1.0;
+    } else {
+        double lc = rho_ctilde2_cons(e, l[0], l[1], l[2], l[3], l[4], l[5]);
+        theta = pp_theta_lower(lc, hc, kPpCtilde);
+    }
+    if (theta < 0.0 || isnan(theta)) theta = 0.0;
+    if (theta > 1.0) theta = 1.0;
+    return theta;
 }
 
 // Limiter factor of one cell for one pass (theta_cons_stage, SC:268-292); binary64.

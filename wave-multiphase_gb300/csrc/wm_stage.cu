@@ -161,23 +161,27 @@ __global__ void __launch_bounds__(BX *BY) sensor_kernel(Grid g, Fields q, Prep p
 
 // --------------------------------------------------------------------------- Wong limiter ----
 // pp_cell_theta_kernel (SC:1397-1476): residuals of the current (partly blended) high-order and of
-// the first-order fluxes, bound solve of this pass.
+// the first-order fluxes, bound solve of this pass. Pass 0 bounds the partial densities, pass 1
+// alpha and 1 - alpha, pass 2 rho c~^2 (theta_cons_stage, SC:268-292); each pass forms only the
+// residual components its bound uses.
+template <int STAGE>
 __global__ void __launch_bounds__(BX *BY)
 theta_kernel(Grid g, Eos e, Fields q, Face7 fh, Face7 gh, Face7 fl, Face7 gl, double *theta,
-             double dt, const double *dt_dev, int stage, unsigned long long *limited)
+             double dt, const double *dt_dev, unsigned long long *limited)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x + g.g;
     int i = blockIdx.y * blockDim.y + threadIdx.y + g.g;
     if (i >= g.g + g.nx || j >= g.g + g.ny) return;
     if (dt_dev) dt = *dt_dev;
     long long kf = kf_of(q, i, j), kw = kw_of(g, i, j), kx = kw - g.nyg, ky = kw - 1;
-    double a = q.f[F_ALP][kf];
     double l[6], h[6];
+    constexpr int C0 = STAGE == 1 ? 5 : 0, C1 = STAGE == 0 ? 2 : 6;
 #pragma unroll
-    for (int c = 0; c < 6; ++c) {
+    for (int c = C0; c < C1; ++c) {
         double rh = (fh.f[c][kw] - fh.f[c][kx]) * g.inv_dx + (gh.f[c][kw] - gh.f[c][ky]) * g.inv_dy;
         double rl = (fl.f[c][kw] - fl.f[c][kx]) * g.inv_dx + (gl.f[c][kw] - gl.f[c][ky]) * g.inv_dy;
         if (c == 5) {
+            double a = q.f[F_ALP][kf];
             rh = rh - a * (fh.f[6][kw] - fh.f[6][kx]) * g.inv_dx - a * (gh.f[6][kw] - gh.f[6][ky]) * g.inv_dy;
             rl = rl - a * (fl.f[6][kw] - fl.f[6][kx]) * g.inv_dx - a * (gl.f[6][kw] - gl.f[6][ky]) * g.inv_dy;
         }
@@ -185,7 +189,12 @@ theta_kernel(Grid g, Eos e, Fields q, Face7 fh, Face7 gh, Face7 fl, Face7 gl, do
         l[c] = qc - dt * rl;
         h[c] = qc - dt * rh;
     }
-    double th = theta_cons_stage(e, l, h, stage);
+    double th;
+    if (STAGE == 2) {
+        th = theta_ctilde(e, l, h);
+    } else {
+        th = theta_cons_stage(e, l, h, STAGE);
+    }
     theta[kw] = th;
     if (limited) count_if(limited, th < 1.0);
 }
@@ -407,11 +416,13 @@ void launch_limiter(const Grid &g, const Eos &e, const Fields &q, const Face7 &f
                     const Face7 &fl, const Face7 &gl, double *const theta[3], double dt,
                     const double *dt_dev, const Counters &cnt, cudaStream_t s)
 {
-    for (int st = 0; st < 3; ++st) {
-        theta_kernel<<<grid2(g.ny, g.nx), dim3(BX, BY), 0, s>>>(g, e, q, fh, gh, fl, gl, theta[st],
-                                                                dt, dt_dev, st, cnt.limited);
-        blend_kernel<<<grid2(g.ny + 1, g.nx + 1), dim3(BX, BY), 0, s>>>(g, fh, gh, fl, gl, theta[st]);
-    }
+    const dim3 gt = grid2(g.ny, g.nx), gb = grid2(g.ny + 1, g.nx + 1), bl(BX, BY);
+    theta_kernel<0><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, theta[0], dt, dt_dev, cnt.limited);
+    blend_kernel<<<gb, bl, 0, s>>>(g, fh, gh, fl, gl, theta[0]);
+    theta_kernel<1><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, theta[1], dt, dt_dev, cnt.limited);
+    blend_kernel<<<gb, bl, 0, s>>>(g, fh, gh, fl, gl, theta[1]);
+    theta_kernel<2><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, theta[2], dt, dt_dev, cnt.limited);
+    blend_kernel<<<gb, bl, 0, s>>>(g, fh, gh, fl, gl, theta[2]);
 }
 
 void launch_final(const Grid &g, const Eos &e, unsigned flags, const Fields &q, const Fields &old,
