@@ -47,12 +47,81 @@ FP64_FLOP_PER_FACE = 1020.0  # profiles/face_kernel_triple_point_2048x1024_fp64.
 DRAM_BYTES_PER_CELL_STAGE = None
 
 
-def params(nx=None, ny=None):
+def params(nx=None, ny=None, precision="fp64"):
     import wavemp
 
     nx, ny = nx or NX, ny or NY
     return wavemp.SolverParams(dx=7.0 / nx, dy=3.0 / ny, gamma1=1.5, pinf1=0.0, gamma2=1.4,
-                               pinf2=0.0, variant="sc", recon="mp5c6", bc=("slip",) * 4, cfl=0.4)
+                               pinf2=0.0, variant="sc", recon="mp5c6", bc=("slip",) * 4, cfl=0.4,
+                               precision=precision)
+
+
+def time_form(precision, steps, warmup, dev):
+    """Device-timed steps of one form on the workload; returns (ms, kernel-group profile)."""
+    import torch
+
+    import wavemp
+
+    s = wavemp.Solver(params(precision=precision), NX, NY)
+    q = wavemp.ic.triple_point(NX, NY, device=dev)
+    old = wavemp.alloc_state(NX, NY, names=wavemp.FIELDS, device=dev)
+    s.initialize(q)
+    s.init_dt(q)
+    for _ in range(warmup):
+        s.step(q, old, None, sync=False)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.profile(True)
+    s.profile_read(reset=True)
+    e0.record(stream)
+    for _ in range(steps):
+        s.step(q, old, None, sync=False)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    prof = s.profile_read(reset=True)
+    s.profile(False)
+    ms = e0.elapsed_time(e1)
+    finite = all(bool(torch.isfinite(q[k]).all()) for k in wavemp.FIELDS)
+    del s, q, old
+    torch.cuda.empty_cache()
+    return ms, prof, finite
+
+
+def precision_errors(steps, dev):
+    """Per-field L1 / Linf difference of the precision form from the plain binary64 form after
+    `steps` steps from the same state with the same dt (interior cells, relative to the binary64
+    field's L1 norm and max)."""
+    import torch
+
+    import wavemp
+
+    out = {}
+    solvers = {}
+    for prec in ("fp64", "fp32"):
+        s = wavemp.Solver(params(precision=prec), NX, NY)
+        q = wavemp.ic.triple_point(NX, NY, device=dev)
+        old = wavemp.alloc_state(NX, NY, names=wavemp.FIELDS, device=dev)
+        s.initialize(q)
+        solvers[prec] = (s, q, old)
+    dt = solvers["fp64"][0].get_dt(solvers["fp64"][1])
+    for _ in range(steps):
+        for prec in ("fp64", "fp32"):
+            s, q, old = solvers[prec]
+            s.step(q, old, dt, sync=False)
+    torch.cuda.synchronize()
+    a, b = solvers["fp32"][1], solvers["fp64"][1]
+    sl = (slice(G, -G), slice(G, -G))
+    rho_a = (a["ar1"] + a["ar2"])[sl]
+    rho_b = (b["ar1"] + b["ar2"])[sl]
+    pairs = [("rho", rho_a, rho_b)] + [(k, a[k][sl], b[k][sl]) for k in ("ar1", "ar2", "ru", "rv", "E", "al", "p_p")]
+    for k, x, y in pairs:
+        d = (x - y).abs()
+        out[k] = {"l1": float(d.sum() / y.abs().sum().clamp_min(1e-300)),
+                  "linf": float(d.max() / y.abs().max().clamp_min(1e-300))}
+    del solvers
+    torch.cuda.empty_cache()
+    return out
 
 
 def measured_peaks():
@@ -293,6 +362,26 @@ def run_ours(args):
                 "d2h_bytes_per_step": h2d, "steps": ke},
         "gpu_launches": launches, "kernels": kernels, "clocks": clk, "finite": finite,
     }
+    # ---- precision form (binary32 face sweep, binary64 recovery / bound solves / accumulation) ----
+    del q, old, host, s
+    torch.cuda.empty_cache()
+    ms32, prof32, finite32 = time_form("fp32", args.steps, args.warmup, dev)
+    if world > 1:
+        t = torch.tensor([ms32], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms32 = float(t.item())
+    v32 = cells * 3 * args.steps * world / (ms32 * 1e-3) / 1e6
+    err_steps = 10
+    line["forms"] = {"precision_fp32": {
+        "value": round(v32, 3), "unit": "Mcell-stage/s", "ms_per_step": round(ms32 / args.steps, 3),
+        "speedup_vs_plain": round(v32 / value, 3), "finite": finite32,
+        "kernels": {g: {"ms_per_launch": round(t / max(n, 1), 4), "launches": n} for g, (t, n) in prof32.items()},
+        "error_vs_fp64": {"steps": err_steps, "dt": "fixed, CFL 0.4 of the initial state",
+                          "fields": precision_errors(err_steps, dev)},
+        "roofline": {"bound": "hbm", "achieved": round(ALG_BYTES_PER_CELL_STAGE * cells / (ms32 / args.steps / 3 * 1e-3) / 1e9, 2),
+                     "peak": hbm, "unit": "GB/s",
+                     "frac": round(ALG_BYTES_PER_CELL_STAGE * cells / (ms32 / args.steps / 3 * 1e-3) / 1e9 / hbm, 5)},
+    }}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         os.environ.setdefault("OMP_NUM_THREADS", str(cores))

@@ -32,13 +32,24 @@ int check_launch(const char *where)
 
 constexpr int kFaceArrays = 28, kThetaArrays = 3, kPrepArrays = 11;
 constexpr int kArrays = kFaceArrays + kThetaArrays + kPrepArrays;
+constexpr int kCellCopies = 8;  // binary32 cell copies of the precision form
 constexpr size_t kAlign = 256;
 constexpr size_t kTailBytes = 256;  // counters and dt slots
 
-size_t array_bytes(int nx, int ny, int g)
+size_t array_bytes(int nx, int ny, int g, size_t elem = sizeof(double))
 {
-    size_t n = (size_t)(nx + 2 * g) * (size_t)(ny + 2 * g) * sizeof(double);
+    size_t n = (size_t)(nx + 2 * g) * (size_t)(ny + 2 * g) * elem;
     return (n + kAlign - 1) / kAlign * kAlign;
+}
+
+// Workspace of the plain form: 42 binary64 arrays. Precision form: 28 binary32 face arrays, 3
+// binary64 limiter factors, 11 binary32 per-cell arrays and 8 binary32 cell copies.
+size_t layout_bytes(int precision, int nx, int ny, int g)
+{
+    if (precision == WM_PREC_FP32)
+        return (size_t)(kFaceArrays + kPrepArrays + kCellCopies) * array_bytes(nx, ny, g, sizeof(float)) +
+               (size_t)kThetaArrays * array_bytes(nx, ny, g) + kTailBytes;
+    return (size_t)kArrays * array_bytes(nx, ny, g) + kTailBytes;
 }
 
 bool valid_params(const wm_params *p, int nx, int ny, int g)
@@ -48,7 +59,7 @@ bool valid_params(const wm_params *p, int nx, int ny, int g)
     if (!std::isfinite(p->pinf1) || !std::isfinite(p->pinf2) || !(p->cfl > 0.0)) return false;
     if (p->variant != WM_VARIANT_SC && p->variant != WM_VARIANT_M10) return false;
     if (p->recon != WM_RECON_SHIPPED && p->recon != WM_RECON_MP5C6) return false;
-    if (p->precision != WM_PREC_FP64) return false;  // the binary32 form has its own entry points
+    if (p->precision != WM_PREC_FP64 && p->precision != WM_PREC_FP32) return false;
     for (int k = 0; k < 4; ++k)
         if (p->bc[k] != WM_BC_TRANSMISSIVE && p->bc[k] != WM_BC_SLIP) return false;
     if ((double)(nx + 2 * g) * (double)(ny + 2 * g) > 4.0e9) return false;
@@ -68,10 +79,15 @@ struct wm_handle {
     Eos e;
     void *ws = nullptr;
     bool own_ws = false;
-    double *arr[kArrays];
+    bool fp32 = false;
+    double *arr[kArrays];  // binary64 arrays (plain form) by WM_WS_* index
+    float *arr32[kArrays]; // binary32 arrays (precision form) by WM_WS_* index; theta stays binary64
     Face7 fh, gh, fl, gl;
+    Face<float> fh32, gh32, fl32, gl32;
     double *theta[3];
     Prep prep;
+    PrepT<float> prep32;
+    Cells32 cells32;
     Counters cnt;
     unsigned long long *ctr_base = nullptr;
     double *dt_dev[2];
@@ -164,13 +180,13 @@ unsigned final_flags(const wm_handle *h, double alpha)
 
 extern "C" {
 
-const char *wm_version(void) { return "wavemp 0.1 (sm_103a, fp64)"; }
+const char *wm_version(void) { return "wavemp 0.2 (sm_103a; fp64 plain and fp32 precision forms)"; }
 const char *wm_last_error(void) { return g_last_error; }
 
 size_t wm_workspace_bytes(const wm_params *p, int nx, int ny, int g)
 {
     if (!valid_params(p, nx, ny, g)) return 0;
-    return (size_t)kArrays * array_bytes(nx, ny, g) + kTailBytes;
+    return layout_bytes(p->precision, nx, ny, g);
 }
 
 int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t workspace_bytes,
@@ -213,22 +229,62 @@ int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t
         return WM_ERR_CUDA;
     }
     char *base = static_cast<char *>(h->ws);
-    size_t ab = array_bytes(nx, ny, g);
-    for (int a = 0; a < kArrays; ++a) h->arr[a] = reinterpret_cast<double *>(base + (size_t)a * ab);
-    for (int c = 0; c < 7; ++c) {
-        h->fh.f[c] = h->arr[WM_WS_FX + c];
-        h->gh.f[c] = h->arr[WM_WS_GY + c];
-        h->fl.f[c] = h->arr[WM_WS_FXL + c];
-        h->gl.f[c] = h->arr[WM_WS_GYL + c];
+    char *tail;
+    h->fp32 = p->precision == WM_PREC_FP32;
+    if (!h->fp32) {
+        size_t ab = array_bytes(nx, ny, g);
+        for (int a = 0; a < kArrays; ++a) h->arr[a] = reinterpret_cast<double *>(base + (size_t)a * ab);
+        for (int c = 0; c < 7; ++c) {
+            h->fh.f[c] = h->arr[WM_WS_FX + c];
+            h->gh.f[c] = h->arr[WM_WS_GY + c];
+            h->fl.f[c] = h->arr[WM_WS_FXL + c];
+            h->gl.f[c] = h->arr[WM_WS_GYL + c];
+        }
+        for (int s = 0; s < 3; ++s) h->theta[s] = h->arr[WM_WS_THETA + s];
+        Prep &P = h->prep;
+        P.sx = h->arr[WM_WS_SIGMA_X];
+        P.sy = h->arr[WM_WS_SIGMA_Y];
+        P.ent = h->arr[33]; P.cx = h->arr[34]; P.cy = h->arr[35];
+        P.lu = h->arr[36]; P.lv = h->arr[37]; P.lp = h->arr[38]; P.la = h->arr[39]; P.lc = h->arr[40];
+        P.lE = h->arr[41];
+        tail = base + (size_t)kArrays * ab;
+    } else {
+        size_t ab4 = array_bytes(nx, ny, g, sizeof(float)), ab8 = array_bytes(nx, ny, g);
+        char *cur = base;
+        for (int a = 0; a < kArrays; ++a) {
+            if (a >= WM_WS_THETA && a < WM_WS_THETA + 3) {
+                h->arr[a] = reinterpret_cast<double *>(cur);
+                h->arr32[a] = nullptr;
+                cur += ab8;
+            } else {
+                h->arr32[a] = reinterpret_cast<float *>(cur);
+                h->arr[a] = nullptr;
+                cur += ab4;
+            }
+        }
+        float *copies[kCellCopies];
+        for (int c = 0; c < kCellCopies; ++c) {
+            copies[c] = reinterpret_cast<float *>(cur);
+            cur += ab4;
+        }
+        for (int c = 0; c < 7; ++c) {
+            h->fh32.f[c] = h->arr32[WM_WS_FX + c];
+            h->gh32.f[c] = h->arr32[WM_WS_GY + c];
+            h->fl32.f[c] = h->arr32[WM_WS_FXL + c];
+            h->gl32.f[c] = h->arr32[WM_WS_GYL + c];
+        }
+        for (int s = 0; s < 3; ++s) h->theta[s] = h->arr[WM_WS_THETA + s];
+        PrepT<float> &P = h->prep32;
+        P.sx = h->arr32[WM_WS_SIGMA_X];
+        P.sy = h->arr32[WM_WS_SIGMA_Y];
+        P.ent = h->arr32[33]; P.cx = h->arr32[34]; P.cy = h->arr32[35];
+        P.lu = h->arr32[36]; P.lv = h->arr32[37]; P.lp = h->arr32[38]; P.la = h->arr32[39];
+        P.lc = h->arr32[40]; P.lE = h->arr32[41];
+        Cells32 &C = h->cells32;
+        C.ar1 = copies[0]; C.ar2 = copies[1]; C.ru = copies[2]; C.rv = copies[3];
+        C.p = copies[4]; C.al = copies[5]; C.u = copies[6]; C.v = copies[7];
+        tail = cur;
     }
-    for (int s = 0; s < 3; ++s) h->theta[s] = h->arr[WM_WS_THETA + s];
-    Prep &P = h->prep;
-    P.sx = h->arr[WM_WS_SIGMA_X];
-    P.sy = h->arr[WM_WS_SIGMA_Y];
-    P.ent = h->arr[33]; P.cx = h->arr[34]; P.cy = h->arr[35];
-    P.lu = h->arr[36]; P.lv = h->arr[37]; P.lp = h->arr[38]; P.la = h->arr[39]; P.lc = h->arr[40];
-    P.lE = h->arr[41];
-    char *tail = base + (size_t)kArrays * ab;
     h->ctr_base = reinterpret_cast<unsigned long long *>(tail);
     h->cnt.repaired = h->ctr_base + 0;
     h->cnt.nonfinite = h->ctr_base + 1;
@@ -301,9 +357,15 @@ int wm_compute_fluxes(wm_handle *h, const wm_fields *q, void *stream)
     if (!h || !fields_ok(h, q)) return WM_ERR_INVALID;
     Fields F = to_fields(q);
     cudaStream_t s = as_stream(stream);
-    launch_prep(h->g, h->e, F, h->prep, h->P.variant, s);
-    launch_faces(h->g, h->e, h->P.variant, h->P.recon, F, h->prep, h->fh, h->gh, h->fl, h->gl, true,
-                 false, s);
+    if (h->fp32) {
+        launch_prep32(h->g, h->e, F, h->prep32, h->cells32, h->P.variant, s);
+        launch_faces32(h->g, h->e, h->P.variant, h->P.recon, h->cells32, h->prep32, h->fh32, h->gh32,
+                       h->fl32, h->gl32, true, false, s);
+    } else {
+        launch_prep(h->g, h->e, F, h->prep, h->P.variant, s);
+        launch_faces(h->g, h->e, h->P.variant, h->P.recon, F, h->prep, h->fh, h->gh, h->fl, h->gl,
+                     true, false, s);
+    }
     h->fluxes_ready = true;
     return check_launch("wm_compute_fluxes");
 }
@@ -313,9 +375,15 @@ int wm_compute_low_fluxes(wm_handle *h, const wm_fields *q, void *stream)
     if (!h || !fields_ok(h, q)) return WM_ERR_INVALID;
     Fields F = to_fields(q);
     cudaStream_t s = as_stream(stream);
-    launch_prep(h->g, h->e, F, h->prep, h->P.variant, s);
-    launch_faces(h->g, h->e, h->P.variant, h->P.recon, F, h->prep, h->fh, h->gh, h->fl, h->gl, false,
-                 true, s);
+    if (h->fp32) {
+        launch_prep32(h->g, h->e, F, h->prep32, h->cells32, h->P.variant, s);
+        launch_faces32(h->g, h->e, h->P.variant, h->P.recon, h->cells32, h->prep32, h->fh32, h->gh32,
+                       h->fl32, h->gl32, false, true, s);
+    } else {
+        launch_prep(h->g, h->e, F, h->prep, h->P.variant, s);
+        launch_faces(h->g, h->e, h->P.variant, h->P.recon, F, h->prep, h->fh, h->gh, h->fl, h->gl,
+                     false, true, s);
+    }
     h->low_ready = true;
     return check_launch("wm_compute_low_fluxes");
 }
@@ -324,8 +392,12 @@ int wm_limit_fluxes(wm_handle *h, const wm_fields *q, double dt, void *stream)
 {
     if (!h || !fields_ok(h, q) || !std::isfinite(dt)) return WM_ERR_INVALID;
     if (!h->fluxes_ready || !h->low_ready) return WM_ERR_STATE;
-    launch_limiter(h->g, h->e, to_fields(q), h->fh, h->gh, h->fl, h->gl, h->theta, dt, nullptr, h->cnt,
-                   as_stream(stream));
+    if (h->fp32)
+        launch_limiter(h->g, h->e, to_fields(q), h->fh32, h->gh32, h->fl32, h->gl32, h->theta, dt,
+                       nullptr, h->cnt, as_stream(stream));
+    else
+        launch_limiter(h->g, h->e, to_fields(q), h->fh, h->gh, h->fl, h->gl, h->theta, dt, nullptr,
+                       h->cnt, as_stream(stream));
     return check_launch("wm_limit_fluxes");
 }
 
@@ -336,8 +408,13 @@ int wm_rk3_update(wm_handle *h, const wm_fields *q, const wm_fields *q_old, doub
     if (alpha != 0.0 && !fields_ok(h, q_old, false)) return WM_ERR_INVALID;
     if (!h->fluxes_ready) return WM_ERR_STATE;
     Fields F = to_fields(q), O = q_old ? to_fields(q_old) : F;
-    launch_final(h->g, h->e, FIN_RK3 | (alpha != 0.0 ? FIN_OLD_READ : 0u), F, O, h->fh, h->gh, dt,
-                 nullptr, alpha, beta, h->cnt, as_stream(stream));
+    const unsigned fl = FIN_RK3 | (alpha != 0.0 ? FIN_OLD_READ : 0u);
+    if (h->fp32)
+        launch_final(h->g, h->e, fl, F, O, h->fh32, h->gh32, dt, nullptr, alpha, beta, h->cnt,
+                     as_stream(stream));
+    else
+        launch_final(h->g, h->e, fl, F, O, h->fh, h->gh, dt, nullptr, alpha, beta, h->cnt,
+                     as_stream(stream));
     return check_launch("wm_rk3_update");
 }
 
@@ -404,16 +481,27 @@ static int run_stage(wm_handle *h, const Fields &F, const Fields &O, double dt, 
     }
     {
         ProfScope ps(h, WM_PROF_PREP, 2, s);
-        launch_prep(h->g, h->e, F, h->prep, h->P.variant, s);
+        if (h->fp32)
+            launch_prep32(h->g, h->e, F, h->prep32, h->cells32, h->P.variant, s);
+        else
+            launch_prep(h->g, h->e, F, h->prep, h->P.variant, s);
     }
     {
         ProfScope ps(h, WM_PROF_FACES, 2, s);
-        launch_faces(h->g, h->e, h->P.variant, h->P.recon, F, h->prep, h->fh, h->gh, h->fl, h->gl,
-                     true, true, s);
+        if (h->fp32)
+            launch_faces32(h->g, h->e, h->P.variant, h->P.recon, h->cells32, h->prep32, h->fh32,
+                           h->gh32, h->fl32, h->gl32, true, true, s);
+        else
+            launch_faces(h->g, h->e, h->P.variant, h->P.recon, F, h->prep, h->fh, h->gh, h->fl, h->gl,
+                         true, true, s);
     }
     {
         ProfScope ps(h, WM_PROF_LIMITER, 6, s);
-        launch_limiter(h->g, h->e, F, h->fh, h->gh, h->fl, h->gl, h->theta, dt, dt_dev, h->cnt, s);
+        if (h->fp32)
+            launch_limiter(h->g, h->e, F, h->fh32, h->gh32, h->fl32, h->gl32, h->theta, dt, dt_dev,
+                           h->cnt, s);
+        else
+            launch_limiter(h->g, h->e, F, h->fh, h->gh, h->fl, h->gl, h->theta, dt, dt_dev, h->cnt, s);
     }
     unsigned flags = final_flags(h, alpha);
     if (save_old) flags |= FIN_SAVE_OLD;
@@ -423,7 +511,10 @@ static int run_stage(wm_handle *h, const Fields &F, const Fields &O, double dt, 
             flags |= FIN_DT;
             launch_dt_reset(h->cnt, s);
         }
-        launch_final(h->g, h->e, flags, F, O, h->fh, h->gh, dt, dt_dev, alpha, beta, h->cnt, s);
+        if (h->fp32)
+            launch_final(h->g, h->e, flags, F, O, h->fh32, h->gh32, dt, dt_dev, alpha, beta, h->cnt, s);
+        else
+            launch_final(h->g, h->e, flags, F, O, h->fh, h->gh, dt, dt_dev, alpha, beta, h->cnt, s);
     }
     h->fluxes_ready = h->low_ready = true;
     return check_launch("stage");
@@ -477,6 +568,10 @@ int wm_read_workspace(wm_handle *h, int which, double *dst, void *stream)
 {
     if (!h || !dst || which < 0 || which >= WM_WS_COUNT) return WM_ERR_INVALID;
     size_t n = (size_t)h->g.nxg * (size_t)h->g.nyg * sizeof(double);
+    if (!h->arr[which]) {  // binary32 array of the precision form: widen into dst
+        launch_widen(h->arr32[which], dst, (long long)h->g.nxg * h->g.nyg, as_stream(stream));
+        return check_launch("wm_read_workspace");
+    }
     cudaError_t err = cudaMemcpyAsync(dst, h->arr[which], n, cudaMemcpyDeviceToDevice, as_stream(stream));
     if (err != cudaSuccess) {
         set_error("wm_read_workspace", err);

@@ -220,13 +220,38 @@ __device__ __forceinline__ double rho_ctilde2_cons(const Eos &e, double m1, doub
 // low-order bound value only when it can change the result: pp_theta_lower returns 1 when the
 // high-order value is at or above the floor and neither value is NaN, and the low-order value
 // lc = E - kin - p_inf can only be NaN when one of l[2..4] is not finite.
+// True when rho c~^2 = E - kin - p_inf of the conserved state (m1, m2, mx, my, E, a1_in) is
+// certainly >= `floor_`, decided without a division: with rho > 0 and 1 + Gamma > 0,
+//   E - (mx^2 + my^2) / (2 rho) - Pi / (1 + Gamma) >= floor
+//   <=>  2 rho (1 + Gamma) (E - floor) - (1 + Gamma) (mx^2 + my^2) - 2 rho Pi >= 0,
+// and a margin of 1e-12 of the terms' magnitude keeps every case that round-off could decide
+// either way for the exact formula (rho_ctilde2_cons).
+__device__ __forceinline__ bool ctilde_surely_above(const Eos &e, double m1, double m2, double mx,
+                                                    double my, double E, double a1_in, double floor_)
+{
+    double a1 = clamp01_pp(a1_in);
+    double mm1 = m1, mm2 = m2;
+    if (mm1 < kPpRho || isnan(mm1)) mm1 = kPpRho;
+    if (mm2 < kPpRho || isnan(mm2)) mm2 = kPpRho;
+    double rho = mm1 + mm2;
+    double gb, pb;
+    mix_gamma_pibig(e, a1, gb, pb);
+    double gp1 = 1.0 + gb;
+    double t1 = 2.0 * rho * gp1 * (E - floor_);
+    double t2 = gp1 * (mx * mx + my * my);
+    double t3 = 2.0 * rho * pb;
+    double sgn = t1 - t2 - t3;
+    return sgn > 1e-12 * (fabs(t1) + t2 + fabs(t3));  // false for NaN
+}
+
 __device__ __forceinline__ double theta_ctilde(const Eos &e, const double l[6], const double h[6])
 {
-    double hc = rho_ctilde2_cons(e, h[0], h[1], h[2], h[3], h[4], h[5]);
     double theta;
-    if (!isnan(hc) && !(hc < kPpCtilde) && isfinite(l[2]) && isfinite(l[3]) && isfinite(l[4])) {
+    if (ctilde_surely_above(e, h[0], h[1], h[2], h[3], h[4], h[5], kPpCtilde) && isfinite(l[2]) &&
+        isfinite(l[3]) && isfinite(l[4])) {
         theta = 1.0;
     } else {
+        double hc = rho_ctilde2_cons(e, h[0], h[1], h[2], h[3], h[4], h[5]);
         double lc = rho_ctilde2_cons(e, l[0], l[1], l[2], l[3], l[4], l[5]);
         theta = pp_theta_lower(lc, hc, kPpCtilde);
     }
@@ -511,6 +536,10 @@ __device__ __forceinline__ void hllc(const Side<T> &L, const Side<T> &R, T f[6],
 // Blend of a high-order face value toward the first-order one (pp_blend_*_flux_kernel body,
 // SC:1506-1512). Shared by the in-place limiter and the fused stage so both round alike.
 __device__ __forceinline__ double face_blend(double low, double high, double theta)
+{
+    return low + theta * (high - low);
+}
+__device__ __forceinline__ float face_blend(float low, float high, float theta)
 {
     return low + theta * (high - low);
 }

@@ -1,6 +1,7 @@
 // wm_faces.cu -- face sweeps of the per-stage RHS: the high-order flux of fx_kernel / gy_kernel
 // (SC:966-1301, M10:868-1222) and the first-order flux of fx_low_kernel / gy_low_kernel
-// (SC:1303-1394) for one face per thread, binary64.
+// (SC:1303-1394) for one face per thread: binary64 in the plain form, binary32 in the precision
+// form (which reads the binary32 cell copies and per-cell data of prep32_kernel).
 //
 // Per face: stencil load of six cells along the sweep, face-averaged eigenvectors, projection of
 // the six cells to characteristic variables, MUSCL or MP5 / THINC / central reconstruction of the
@@ -15,64 +16,84 @@ namespace {
 
 constexpr int FBX = 32, FBY = 4;
 
-template <int DIR, int VAR, int REC>
+// Cell-state sources of the sweep: the caller's binary64 arrays (row pitch of the fields) or the
+// binary32 copies in the workspace (row pitch of the padded grid).
+struct Src64 {
+    Fields q;
+    __device__ __forceinline__ long long pitch() const { return q.pitch; }
+    __device__ __forceinline__ void load(long long k, double u[6]) const
+    {
+        u[0] = q.f[F_AR1][k]; u[1] = q.f[F_AR2][k]; u[2] = q.f[F_RU][k];
+        u[3] = q.f[F_RV][k]; u[4] = q.f[F_P][k]; u[5] = q.f[F_AL][k];
+    }
+};
+struct Src32 {
+    Cells32 c;
+    long long nyg;
+    __device__ __forceinline__ long long pitch() const { return nyg; }
+    __device__ __forceinline__ void load(long long k, float u[6]) const
+    {
+        u[0] = c.ar1[k]; u[1] = c.ar2[k]; u[2] = c.ru[k];
+        u[3] = c.rv[k]; u[4] = c.p[k]; u[5] = c.al[k];
+    }
+};
+
+template <int DIR, int VAR, int REC, typename T, typename CS, typename FT>
 __global__ void __launch_bounds__(FBX *FBY, 2)
-face_kernel(Grid g, Eos e, Fields q, Prep p, Face7 hi, Face7 lo, int do_high, int do_low)
+face_kernel(Grid g, Eos e, CS cs, PrepT<T> p, Face<FT> hi, Face<FT> lo, int do_high, int do_low)
 {
-    using T = double;
     const int j = blockIdx.x * blockDim.x + threadIdx.x + (DIR == 0 ? g.g : g.g - 1);
     const int i = blockIdx.y * blockDim.y + threadIdx.y + (DIR == 0 ? g.g - 1 : g.g);
     if (i >= g.g + g.nx || j >= g.g + g.ny) return;
     constexpr int N = DIR == 0 ? 2 : 3;   // normal momentum field
     constexpr int TG = DIR == 0 ? 3 : 2;  // tangential momentum field
-    const long long sf = DIR == 0 ? q.pitch : 1;  // stride along the sweep, fields
-    const long long sw = DIR == 0 ? g.nyg : 1;    // stride along the sweep, workspace
-    const long long kf = (long long)i * q.pitch + j;
+    const long long sf = DIR == 0 ? cs.pitch() : 1;  // stride along the sweep, cell arrays
+    const long long sw = DIR == 0 ? g.nyg : 1;       // stride along the sweep, workspace
+    const long long kf = (long long)i * cs.pitch() + j;
     const long long kw = (long long)i * g.nyg + j;
-    const double *ar1 = q.f[F_AR1], *ar2 = q.f[F_AR2], *ru = q.f[F_RU], *rv = q.f[F_RV];
-    const double *pp = q.f[F_P], *al = q.f[F_AL];
 
     // Cells 0 and 1 of the face (i and i+1 along the sweep).
-    const T ar1_0 = ar1[kf], ar1_1 = ar1[kf + sf];
-    const T ar2_0 = ar2[kf], ar2_1 = ar2[kf + sf];
+    T U0[6], U1[6];
+    cs.load(kf, U0);
+    cs.load(kf + sf, U1);
 
     if (do_low) {  // first-order HLLC of the two cell states (fx_low_kernel, SC:1303-1347)
         Side<T> L, R;
-        const double *un = DIR == 0 ? p.lu : p.lv, *ut = DIR == 0 ? p.lv : p.lu;
-        L.ar1 = ar1_0; L.ar2 = ar2_0; L.rho = ar1_0 + ar2_0;
+        const T *un = DIR == 0 ? p.lu : p.lv, *ut = DIR == 0 ? p.lv : p.lu;
+        L.ar1 = U0[0]; L.ar2 = U0[1]; L.rho = U0[0] + U0[1];
         L.un = un[kw]; L.ut = ut[kw]; L.p = p.lp[kw]; L.a = p.la[kw]; L.c = p.lc[kw]; L.E = p.lE[kw];
-        R.ar1 = ar1_1; R.ar2 = ar2_1; R.rho = ar1_1 + ar2_1;
+        R.ar1 = U1[0]; R.ar2 = U1[1]; R.rho = U1[0] + U1[1];
         R.un = un[kw + sw]; R.ut = ut[kw + sw]; R.p = p.lp[kw + sw]; R.a = p.la[kw + sw];
         R.c = p.lc[kw + sw]; R.E = p.lE[kw + sw];
         T f[6], us;
         hllc<DIR>(L, R, f, us);
 #pragma unroll
-        for (int c = 0; c < 6; ++c) lo.f[c][kw] = f[c];
-        lo.f[6][kw] = us;
+        for (int c = 0; c < 6; ++c) lo.f[c][kw] = FT(f[c]);
+        lo.f[6][kw] = FT(us);
     }
     if (!do_high) return;
 
     // --- sensors (per-cell, computed by sensor_kernel) -------------------------------------------
-    const double *cs = DIR == 0 ? p.cx : p.cy;
-    const T c_m1 = cs[kw - sw], c_0 = cs[kw], c_p1 = cs[kw + sw], c_p2 = cs[kw + 2 * sw];
+    const T *ci = DIR == 0 ? p.cx : p.cy;
+    const T c_m1 = ci[kw - sw], c_0 = ci[kw], c_p1 = ci[kw + sw], c_p2 = ci[kw + 2 * sw];
     const bool use_thinc = wmin(wmin(c_m1, c_0), wmin(c_p1, c_p2)) < T(kThincThresh);
     bool smooth = false;
     if (VAR == kSC) {
-        const double *sg = DIR == 0 ? p.sx : p.sy;
+        const T *sg = DIR == 0 ? p.sx : p.sy;
         const T smax = wmax(wmax(sg[kw - sw], sg[kw]), wmax(sg[kw + sw], sg[kw + 2 * sw]));
         smooth = smax < T(kSigmaSmooth);
     }
 
     // --- face-averaged state and eigenvector basis (SC:1039-1048) ------------------------------
-    const T ar1a = T(0.5) * (ar1_0 + ar1_1);
-    const T ar2a = T(0.5) * (ar2_0 + ar2_1);
-    const T a1a = T(0.5) * (al[kf] + al[kf + sf]);
-    const T pa = T(0.5) * (pp[kf] + pp[kf + sf]);
+    const T ar1a = T(0.5) * (U0[0] + U1[0]);
+    const T ar2a = T(0.5) * (U0[1] + U1[1]);
+    const T a1a = T(0.5) * (U0[5] + U1[5]);
+    const T pa = T(0.5) * (U0[4] + U1[4]);
     const T rhoa = ar1a + ar2a;
     const T irhoa = T(1) / rhoa;
     FaceBasis<T> b;
-    b.u = T(0.5) * (ru[kf] + ru[kf + sf]) * irhoa;
-    b.v = T(0.5) * (rv[kf] + rv[kf + sf]) * irhoa;
+    b.u = T(0.5) * (U0[2] + U1[2]) * irhoa;
+    b.v = T(0.5) * (U0[3] + U1[3]) * irhoa;
     const T ca = sound_speed_r(e, irhoa, pa, a1a);
     {
         const T ic = T(1) / ca;
@@ -91,8 +112,16 @@ face_kernel(Grid g, Eos e, Fields q, Prep p, Face7 hi, Face7 lo, int do_high, in
     T W[6][6];
 #pragma unroll
     for (int o = O0; o < O1; ++o) {
-        const long long k = kf + (o - 2) * sf;
-        T u[6] = {ar1[k], ar2[k], ru[k], rv[k], pp[k], al[k]};
+        T u[6];
+        if (o == 2) {
+#pragma unroll
+            for (int f = 0; f < 6; ++f) u[f] = U0[f];
+        } else if (o == 3) {
+#pragma unroll
+            for (int f = 0; f < 6; ++f) u[f] = U1[f];
+        } else {
+            cs.load(kf + (o - 2) * sf, u);
+        }
         S6<T> w = to_char<DIR>(b, u);
 #pragma unroll
         for (int f = 0; f < 6; ++f) W[o][f] = w.v[f];
@@ -167,26 +196,37 @@ face_kernel(Grid g, Eos e, Fields q, Prep p, Face7 hi, Face7 lo, int do_high, in
     T f[6], us;
     hllc<DIR>(S[0], S[1], f, us);
 #pragma unroll
-    for (int c = 0; c < 6; ++c) hi.f[c][kw] = f[c];
-    hi.f[6][kw] = us;
+    for (int c = 0; c < 6; ++c) hi.f[c][kw] = FT(f[c]);
+    hi.f[6][kw] = FT(us);
 }
 
-template <int DIR, int VAR, int REC>
-void launch_one(const Grid &g, const Eos &e, const Fields &q, const Prep &p, const Face7 &hi,
-                const Face7 &lo, bool high, bool low, cudaStream_t s)
+template <int DIR, int VAR, int REC, typename T, typename CS, typename FT>
+void launch_one(const Grid &g, const Eos &e, const CS &cs, const PrepT<T> &p, const Face<FT> &hi,
+                const Face<FT> &lo, bool high, bool low, cudaStream_t s)
 {
     const int nj = DIR == 0 ? g.ny : g.ny + 1, ni = DIR == 0 ? g.nx + 1 : g.nx;
     dim3 grid((nj + FBX - 1) / FBX, (ni + FBY - 1) / FBY);
-    face_kernel<DIR, VAR, REC><<<grid, dim3(FBX, FBY), 0, s>>>(g, e, q, p, hi, lo, high, low);
+    face_kernel<DIR, VAR, REC, T, CS, FT><<<grid, dim3(FBX, FBY), 0, s>>>(g, e, cs, p, hi, lo, high, low);
 }
 
-template <int VAR, int REC>
-void launch_pair(const Grid &g, const Eos &e, const Fields &q, const Prep &p, const Face7 &fh,
-                 const Face7 &gh, const Face7 &fl, const Face7 &gl, bool high, bool low,
+template <int VAR, int REC, typename T, typename CS, typename FT>
+void launch_pair(const Grid &g, const Eos &e, const CS &cs, const PrepT<T> &p, const Face<FT> &fh,
+                 const Face<FT> &gh, const Face<FT> &fl, const Face<FT> &gl, bool high, bool low,
                  cudaStream_t s)
 {
-    launch_one<0, VAR, REC>(g, e, q, p, fh, fl, high, low, s);
-    launch_one<1, VAR, REC>(g, e, q, p, gh, gl, high, low, s);
+    launch_one<0, VAR, REC, T>(g, e, cs, p, fh, fl, high, low, s);
+    launch_one<1, VAR, REC, T>(g, e, cs, p, gh, gl, high, low, s);
+}
+
+template <typename T, typename CS, typename FT>
+void dispatch(const Grid &g, const Eos &e, int variant, int recon, const CS &cs, const PrepT<T> &p,
+              const Face<FT> &fh, const Face<FT> &gh, const Face<FT> &fl, const Face<FT> &gl,
+              bool high, bool low, cudaStream_t s)
+{
+    if (variant == kSC && recon == kMuscl) launch_pair<kSC, kMuscl, T>(g, e, cs, p, fh, gh, fl, gl, high, low, s);
+    if (variant == kSC && recon == kMp5) launch_pair<kSC, kMp5, T>(g, e, cs, p, fh, gh, fl, gl, high, low, s);
+    if (variant == kM10 && recon == kMuscl) launch_pair<kM10, kMuscl, T>(g, e, cs, p, fh, gh, fl, gl, high, low, s);
+    if (variant == kM10 && recon == kMp5) launch_pair<kM10, kMp5, T>(g, e, cs, p, fh, gh, fl, gl, high, low, s);
 }
 
 }  // namespace
@@ -195,10 +235,15 @@ void launch_faces(const Grid &g, const Eos &e, int variant, int recon, const Fie
                   const Prep &p, const Face7 &fh, const Face7 &gh, const Face7 &fl, const Face7 &gl,
                   bool high, bool low, cudaStream_t s)
 {
-    if (variant == kSC && recon == kMuscl) launch_pair<kSC, kMuscl>(g, e, q, p, fh, gh, fl, gl, high, low, s);
-    if (variant == kSC && recon == kMp5) launch_pair<kSC, kMp5>(g, e, q, p, fh, gh, fl, gl, high, low, s);
-    if (variant == kM10 && recon == kMuscl) launch_pair<kM10, kMuscl>(g, e, q, p, fh, gh, fl, gl, high, low, s);
-    if (variant == kM10 && recon == kMp5) launch_pair<kM10, kMp5>(g, e, q, p, fh, gh, fl, gl, high, low, s);
+    dispatch<double>(g, e, variant, recon, Src64{q}, p, fh, gh, fl, gl, high, low, s);
+}
+
+void launch_faces32(const Grid &g, const Eos &e, int variant, int recon, const Cells32 &c,
+                    const PrepT<float> &p, const Face<float> &fh, const Face<float> &gh,
+                    const Face<float> &fl, const Face<float> &gl, bool high, bool low,
+                    cudaStream_t s)
+{
+    dispatch<float>(g, e, variant, recon, Src32{c, g.nyg}, p, fh, gh, fl, gl, high, low, s);
 }
 
 }  // namespace wm

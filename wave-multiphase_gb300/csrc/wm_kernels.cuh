@@ -14,17 +14,26 @@ struct Fields {
 };
 enum { F_AR1 = 0, F_AR2, F_RU, F_RV, F_E, F_AL, F_U, F_V, F_P, F_ALP };
 
-struct Face7 {
-    double *f[7];  // six flux components and the interface velocity
+// Six flux components and the interface velocity of one sweep direction; FT is the storage type
+// (double in the plain form, float in the precision form).
+template <typename FT> struct Face {
+    FT *f[7];
 };
+using Face7 = Face<double>;
 
 // Per-cell data computed once per stage and shared by the faces that use it.
-struct Prep {
-    double *ent;            // cell entropy p / rho^gamma (8 faces per direction read it)
-    double *cx, *cy;        // smoothness indicator along x and y
-    double *sx, *sy;        // Ducros x pressure sensor (SC only)
-    double *lu, *lv, *lp, *la, *lc, *lE;  // first-order HLLC cell state: velocity, floored
-                                          // pressure, clamped alpha, sound speed, energy
+template <typename PT> struct PrepT {
+    PT *ent;                          // cell entropy p / rho^gamma
+    PT *cx, *cy;                      // smoothness indicator along x and y
+    PT *sx, *sy;                      // Ducros x pressure sensor (SC only)
+    PT *lu, *lv, *lp, *la, *lc, *lE;  // first-order HLLC cell state: velocity, floored
+                                      // pressure, clamped alpha, sound speed, energy
+};
+using Prep = PrepT<double>;
+
+// Binary32 copies of the cell state read by the precision form's face sweep (workspace pitch).
+struct Cells32 {
+    float *ar1, *ar2, *ru, *rv, *p, *al, *u, *v;
 };
 
 struct Counters {
@@ -49,17 +58,29 @@ void launch_prep(const Grid &g, const Eos &e, const Fields &q, const Prep &p, in
 void launch_faces(const Grid &g, const Eos &e, int variant, int recon, const Fields &q,
                   const Prep &p, const Face7 &fh, const Face7 &gh, const Face7 &fl, const Face7 &gl,
                   bool high, bool low, cudaStream_t s);
-void launch_limiter(const Grid &g, const Eos &e, const Fields &q, const Face7 &fh, const Face7 &gh,
-                    const Face7 &fl, const Face7 &gl, double *const theta[3], double dt,
-                    const double *dt_dev, const Counters &cnt, cudaStream_t s);
+template <typename FT>
+void launch_limiter(const Grid &g, const Eos &e, const Fields &q, const Face<FT> &fh,
+                    const Face<FT> &gh, const Face<FT> &fl, const Face<FT> &gl,
+                    double *const theta[3], double dt, const double *dt_dev, const Counters &cnt,
+                    cudaStream_t s);
+template <typename FT>
 void launch_final(const Grid &g, const Eos &e, unsigned flags, const Fields &q, const Fields &old,
-                  const Face7 &fh, const Face7 &gh, double dt, const double *dt_dev, double alpha,
-                  double beta, const Counters &cnt, cudaStream_t s);
+                  const Face<FT> &fh, const Face<FT> &gh, double dt, const double *dt_dev,
+                  double alpha, double beta, const Counters &cnt, cudaStream_t s);
 void launch_copy_old(const Grid &g, const Fields &q, const Fields &old, cudaStream_t s);
 void launch_dt_reset(const Counters &cnt, cudaStream_t s);
 void launch_dt_cell(const Grid &g, const Eos &e, const Fields &q, const Counters &cnt,
                     cudaStream_t s);
 void launch_dt_finalize(const Grid &g, const Counters &cnt, double *dt_out, cudaStream_t s);
 void launch_fp64_probe(double *out, int iters, cudaStream_t s, int blocks, int threads);
+
+// Precision form (binary32 face sweep).
+void launch_prep32(const Grid &g, const Eos &e, const Fields &q, const PrepT<float> &p,
+                   const Cells32 &c, int variant, cudaStream_t s);
+void launch_faces32(const Grid &g, const Eos &e, int variant, int recon, const Cells32 &c,
+                    const PrepT<float> &p, const Face<float> &fh, const Face<float> &gh,
+                    const Face<float> &fl, const Face<float> &gl, bool high, bool low,
+                    cudaStream_t s);
+void launch_widen(const float *src, double *dst, long long n, cudaStream_t s);
 
 }  // namespace wm

@@ -164,30 +164,31 @@ __global__ void __launch_bounds__(BX *BY) sensor_kernel(Grid g, Fields q, Prep p
 // the first-order fluxes, bound solve of this pass. Pass 0 bounds the partial densities, pass 1
 // alpha and 1 - alpha, pass 2 rho c~^2 (theta_cons_stage, SC:268-292); each pass forms only the
 // residual components its bound uses.
-template <int STAGE>
+template <int STAGE, typename FT>
 __global__ void __launch_bounds__(BX *BY)
-theta_kernel(Grid g, Eos e, Fields q, Face7 fh, Face7 gh, Face7 fl, Face7 gl, double *theta,
-             double dt, const double *dt_dev, unsigned long long *limited)
+theta_kernel(Grid g, Eos e, Fields q, Face<FT> fh, Face<FT> gh, Face<FT> fl, Face<FT> gl,
+             double *theta, double dt, const double *dt_dev, unsigned long long *limited)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x + g.g;
     int i = blockIdx.y * blockDim.y + threadIdx.y + g.g;
     if (i >= g.g + g.nx || j >= g.g + g.ny) return;
     if (dt_dev) dt = *dt_dev;
     long long kf = kf_of(q, i, j), kw = kw_of(g, i, j), kx = kw - g.nyg, ky = kw - 1;
+    const FT idx = FT(g.inv_dx), idy = FT(g.inv_dy);
     double l[6], h[6];
     constexpr int C0 = STAGE == 1 ? 5 : 0, C1 = STAGE == 0 ? 2 : 6;
 #pragma unroll
     for (int c = C0; c < C1; ++c) {
-        double rh = (fh.f[c][kw] - fh.f[c][kx]) * g.inv_dx + (gh.f[c][kw] - gh.f[c][ky]) * g.inv_dy;
-        double rl = (fl.f[c][kw] - fl.f[c][kx]) * g.inv_dx + (gl.f[c][kw] - gl.f[c][ky]) * g.inv_dy;
+        FT rh = (fh.f[c][kw] - fh.f[c][kx]) * idx + (gh.f[c][kw] - gh.f[c][ky]) * idy;
+        FT rl = (fl.f[c][kw] - fl.f[c][kx]) * idx + (gl.f[c][kw] - gl.f[c][ky]) * idy;
         if (c == 5) {
-            double a = q.f[F_ALP][kf];
-            rh = rh - a * (fh.f[6][kw] - fh.f[6][kx]) * g.inv_dx - a * (gh.f[6][kw] - gh.f[6][ky]) * g.inv_dy;
-            rl = rl - a * (fl.f[6][kw] - fl.f[6][kx]) * g.inv_dx - a * (gl.f[6][kw] - gl.f[6][ky]) * g.inv_dy;
+            FT a = FT(q.f[F_ALP][kf]);
+            rh = rh - a * (fh.f[6][kw] - fh.f[6][kx]) * idx - a * (gh.f[6][kw] - gh.f[6][ky]) * idy;
+            rl = rl - a * (fl.f[6][kw] - fl.f[6][kx]) * idx - a * (gl.f[6][kw] - gl.f[6][ky]) * idy;
         }
         double qc = q.f[c][kf];
-        l[c] = qc - dt * rl;
-        h[c] = qc - dt * rh;
+        l[c] = qc - dt * double(rl);
+        h[c] = qc - dt * double(rh);
     }
     double th;
     if (STAGE == 2) {
@@ -202,8 +203,9 @@ theta_kernel(Grid g, Eos e, Fields q, Face7 fh, Face7 gh, Face7 fl, Face7 gl, do
 // pp_blend_x_flux_kernel + pp_blend_y_flux_kernel (SC:1479-1548) in one launch: the thread at
 // (i, j) blends x-face (i, j) and y-face (i, j) when they exist. Face theta is the min over its
 // interior neighbours.
+template <typename FT>
 __global__ void __launch_bounds__(BX *BY)
-blend_kernel(Grid g, Face7 fh, Face7 gh, Face7 fl, Face7 gl, const double *theta)
+blend_kernel(Grid g, Face<FT> fh, Face<FT> gh, Face<FT> fl, Face<FT> gl, const double *theta)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x + g.g - 1;
     int i = blockIdx.y * blockDim.y + threadIdx.y + g.g - 1;
@@ -214,15 +216,17 @@ blend_kernel(Grid g, Face7 fh, Face7 gh, Face7 fl, Face7 gl, const double *theta
         double th = 1.0;
         if (ii) th = wmin(th, theta[kw]);
         if (i + 1 < g.g + g.nx) th = wmin(th, theta[kw + g.nyg]);
+        const FT t = FT(th);
 #pragma unroll
-        for (int c = 0; c < 7; ++c) fh.f[c][kw] = face_blend(fl.f[c][kw], fh.f[c][kw], th);
+        for (int c = 0; c < 7; ++c) fh.f[c][kw] = face_blend(fl.f[c][kw], fh.f[c][kw], t);
     }
     if (ii) {  // y face between (i, j) and (i, j+1)
         double th = 1.0;
         if (ji) th = wmin(th, theta[kw]);
         if (j + 1 < g.g + g.ny) th = wmin(th, theta[kw + 1]);
+        const FT t = FT(th);
 #pragma unroll
-        for (int c = 0; c < 7; ++c) gh.f[c][kw] = face_blend(gl.f[c][kw], gh.f[c][kw], th);
+        for (int c = 0; c < 7; ++c) gh.f[c][kw] = face_blend(gl.f[c][kw], gh.f[c][kw], t);
     }
 }
 
@@ -230,8 +234,9 @@ blend_kernel(Grid g, Face7 fh, Face7 gh, Face7 fl, Face7 gl, const double *theta
 // rk3_kernel (SC:1553-1611) on interior cells, then enforce_admissible_kernel (SC:918-958) and
 // cons_to_prim_kernel (SC:840-864) + al_prim copy on every cell, then the dt candidate of
 // timestep_kernel (SC:1686-1705) -- each step selected by `flags`.
+template <typename FT>
 __global__ void __launch_bounds__(BX *BY)
-final_kernel(Grid g, Eos e, unsigned flags, Fields q, Fields old, Face7 fh, Face7 gh, double dt,
+final_kernel(Grid g, Eos e, unsigned flags, Fields q, Fields old, Face<FT> fh, Face<FT> gh, double dt,
              const double *dt_dev, double alpha, double beta, Counters cnt)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -253,23 +258,27 @@ final_kernel(Grid g, Eos e, unsigned flags, Fields q, Fields old, Face7 fh, Face
         if (interior && (flags & FIN_RK3)) {
             if (dt_dev) dt = *dt_dev;
             long long kw = kw_of(g, i, j), kx = kw - g.nyg, ky = kw - 1;
-            double ap = q.f[F_ALP][kf];
-            double res[6];
+            const FT idx = FT(g.inv_dx), idy = FT(g.inv_dy);
+            FT ap = FT(q.f[F_ALP][kf]);
+            FT res[6];
 #pragma unroll
             for (int c = 0; c < 5; ++c)
-                res[c] = (fh.f[c][kw] - fh.f[c][kx]) * g.inv_dx + (gh.f[c][kw] - gh.f[c][ky]) * g.inv_dy;
-            double src6x = ap * (fh.f[6][kw] - fh.f[6][kx]) * g.inv_dx;
-            double src6y = ap * (gh.f[6][kw] - gh.f[6][ky]) * g.inv_dy;
-            res[5] = (fh.f[5][kw] - fh.f[5][kx]) * g.inv_dx + (gh.f[5][kw] - gh.f[5][ky]) * g.inv_dy -
+                res[c] = (fh.f[c][kw] - fh.f[c][kx]) * idx + (gh.f[c][kw] - gh.f[c][ky]) * idy;
+            FT src6x = ap * (fh.f[6][kw] - fh.f[6][kx]) * idx;
+            FT src6y = ap * (gh.f[6][kw] - gh.f[6][ky]) * idy;
+            res[5] = (fh.f[5][kw] - fh.f[5][kx]) * idx + (gh.f[5][kw] - gh.f[5][ky]) * idy -
                      src6x - src6y;
             long long ko = (long long)i * old.pitch + j;
 #pragma unroll
             for (int c = 0; c < 6; ++c) {
-                double base = beta * (Q[c] - dt * res[c]);
+                double base = beta * (Q[c] - dt * double(res[c]));
                 Q[c] = (flags & FIN_OLD_READ) ? alpha * old.f[c][ko] + base : base;
             }
             wrote_q = true;
         }
+        // 1/(rho Gamma) of the admissibility check, reused by the primitive recovery when alpha
+        // is unchanged by the second clamp
+        double rg_a1 = -1.0, rg_rho = 0.0, rg_inv = 0.0, rg_gb = 0.0, rg_pb = 0.0;
         if (flags & FIN_ADMISSIBLE) {
             double a1 = clamp01_pp(Q[F_AL]);
             double m1 = Q[0], m2 = Q[1], mx = Q[2], my = Q[3], E = Q[4];
@@ -279,16 +288,23 @@ final_kernel(Grid g, Eos e, unsigned flags, Fields q, Fields old, Face7 fh, Face
             if (isnan(mx)) mx = 0.0;
             if (isnan(my)) my = 0.0;
             double rho = m1 + m2;
-            double ir = 1.0 / rho;
+            double gb, pb;
+            mix_gamma_pibig(e, a1, gb, pb);
+            const double inv = 1.0 / (rho * gb);
+            const double ir = gb * inv;
             double uu = mx * ir, vv = my * ir;
             double kin = 0.5 * rho * (uu * uu + vv * vv);
-            double gb, pb, gg, pi;
-            mix_gamma_pibig(e, a1, gb, pb);
-            double p = (E - pb - kin) / gb;
-            mix_gamma_pinf(e, a1, gg, pi);
-            double p_min = kPpCtilde * (gg - 1.0) - pi;
-            bool repair = isnan(E) || isnan(p) || (E - kin - pi) < kPpCtilde;
-            if (repair) E = gb * p_min + pb + kin;
+            double p = (E - pb - kin) * (rho * inv);
+            // E - kin - p_inf < floor with p_inf = Pi / (1 + Gamma), multiplied by 1 + Gamma > 0
+            const double gp1 = 1.0 + gb;
+            bool repair = isnan(E) || isnan(p) || ((E - kin) * gp1 - pb < kPpCtilde * gp1);
+            if (repair) {
+                double gg, pi;
+                mix_gamma_pinf(e, a1, gg, pi);
+                double p_min = kPpCtilde * (gg - 1.0) - pi;
+                E = gb * p_min + pb + kin;
+            }
+            rg_a1 = a1; rg_rho = rho; rg_inv = inv; rg_gb = gb; rg_pb = pb;
             Q[0] = m1;
             Q[1] = m2;
             Q[2] = mx;
@@ -307,11 +323,16 @@ final_kernel(Grid g, Eos e, unsigned flags, Fields q, Fields old, Face7 fh, Face
             if (a1 > 1.0 - kPrimAlphaFloor) a1 = 1.0 - kPrimAlphaFloor;
             Q[F_AL] = a1;
             double rho = Q[0] + Q[1];
-            double ir = 1.0 / rho;
+            double gb, pb, inv;
+            if (a1 == rg_a1 && rho == rg_rho) {
+                gb = rg_gb; pb = rg_pb; inv = rg_inv;
+            } else {
+                mix_gamma_pibig(e, a1, gb, pb);
+                inv = 1.0 / (rho * gb);
+            }
+            double ir = gb * inv;
             double uu = Q[2] * ir, vv = Q[3] * ir;
-            double gb, pb;
-            mix_gamma_pibig(e, a1, gb, pb);
-            double pp = (Q[4] - pb - 0.5 * rho * (uu * uu + vv * vv)) / gb;
+            double pp = (Q[4] - pb - 0.5 * rho * (uu * uu + vv * vv)) * (rho * inv);
             q.f[F_U][kf] = uu;
             q.f[F_V][kf] = vv;
             q.f[F_P][kf] = pp;
@@ -337,6 +358,110 @@ final_kernel(Grid g, Eos e, unsigned flags, Fields q, Fields old, Face7 fh, Face
         }
         if ((threadIdx.x & 31) == 0 && dt_bits != ~0ull) atomicMin(cnt.dt_bits, dt_bits);
     }
+}
+
+// ------------------------------------------------------------- precision form: prep ---------
+// Binary32 copies of the cell state for the face sweep, the entropy in binary32, and the
+// first-order HLLC cell state whose pressure floor and sound speed are recovered in binary64
+// (the stiffened-gas p + p_inf cancels to round-off of p_inf ~ 6e8 in binary32).
+__global__ void __launch_bounds__(BX *BY)
+prep32_kernel(Grid g, Eos e, Fields q, PrepT<float> p, Cells32 c)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.nxg || j >= g.nyg) return;
+    long long kf = kf_of(q, i, j), kw = kw_of(g, i, j);
+    const double ar1 = q.f[F_AR1][kf], ar2 = q.f[F_AR2][kf], ru = q.f[F_RU][kf], rv = q.f[F_RV][kf];
+    const double pp = q.f[F_P][kf], al = q.f[F_AL][kf];
+    const float ar1f = float(ar1), ar2f = float(ar2), ruf = float(ru), rvf = float(rv);
+    const float pf = float(pp), alf = float(al);
+    c.ar1[kw] = ar1f;
+    c.ar2[kw] = ar2f;
+    c.ru[kw] = ruf;
+    c.rv[kw] = rvf;
+    c.p[kw] = pf;
+    c.al[kw] = alf;
+    c.u[kw] = float(q.f[F_U][kf]);
+    c.v[kw] = float(q.f[F_V][kf]);
+
+    float ge, pie;
+    mix_gamma_pinf(e, alf, ge, pie);
+    float rho_e = ar1f + ar2f;
+    if (rho_e < float(kTiny)) rho_e = float(kTiny);
+    p.ent[kw] = pf / powf(rho_e, ge);
+
+    // With g = 1 + 1/Gamma and p_inf = Pi / (1 + Gamma): (p + p_inf) / (g - 1) < floor  <=>
+    // ((1 + Gamma) p + Pi) Gamma < floor (1 + Gamma), and c^2 = ((1 + Gamma) p + Pi) / (Gamma rho).
+    const double rho = ar1 + ar2;
+    const double a = clamp01_pp(al);
+    double gb, pb;
+    mix_gamma_pibig(e, a, gb, pb);
+    const double gp1 = 1.0 + gb;
+    double pl = pp;
+    if (isnan(pl) || (gp1 * pl + pb) * gb < kPpCtilde * gp1) {
+        double gg, pi;
+        mix_gamma_pinf(e, a, gg, pi);
+        pl = kPpCtilde * (gg - 1.0) - pi;
+    }
+    double val = (gp1 * pl + pb) / (gb * rho);
+    if (val < kTiny) val = kTiny;
+    const float rhof = ar1f + ar2f;
+    const float irf = 1.0f / rhof;
+    const float u = ruf * irf, v = rvf * irf;
+    const float af = float(a), plf = float(pl);
+    p.lu[kw] = u;
+    p.lv[kw] = v;
+    p.lp[kw] = plf;
+    p.la[kw] = af;
+    p.lc[kw] = float(sqrt(val));
+    p.lE[kw] = prim_to_energy(e, rhof, u, v, plf, af);
+}
+
+// Smoothness indicators and Ducros sensor in binary32 (sensor_kernel's arithmetic).
+__global__ void __launch_bounds__(BX *BY) sensor32_kernel(Grid g, PrepT<float> p, Cells32 c, int sc)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.nxg || j >= g.nyg) return;
+    long long kw = kw_of(g, i, j);
+    const long long W = g.nyg;
+    const float *en = p.ent;
+    if (i >= 2 && i < g.nxg - 2)
+        p.cx[kw] = cator2_val(en[kw - 2 * W], en[kw - W], en[kw], en[kw + W], en[kw + 2 * W]);
+    if (j >= 2 && j < g.nyg - 2)
+        p.cy[kw] = cator2_val(en[kw - 2], en[kw - 1], en[kw], en[kw + 1], en[kw + 2]);
+    if (!sc) return;
+    if (i < 2 || i >= g.nxg - 2 || j < 2 || j >= g.nyg - 2) {
+        p.sx[kw] = 1.0f;
+        p.sy[kw] = 1.0f;
+        return;
+    }
+    const float *U = c.u, *V = c.v, *P = c.p;
+    float der_ux = 0.5f * (-U[kw - W] + U[kw + W]);
+    float der_vx = 0.5f * (-V[kw - W] + V[kw + W]);
+    float der_uy = 0.5f * (-U[kw - 1] + U[kw + 1]);
+    float der_vy = 0.5f * (-V[kw - 1] + V[kw + 1]);
+    float div_u = der_ux + der_vy;
+    float curl_u = der_vx - der_uy;
+    float ducros = div_u * div_u / (div_u * div_u + curl_u * curl_u + 1.0e-30f);
+    float p0 = P[kw];
+    float pm2 = P[kw - 2 * W], pm1 = P[kw - W], pp1 = P[kw + W], pp2 = P[kw + 2 * W];
+    float aa = fabsf(-pm2 + 16.0f * pm1 - 30.0f * p0 + 16.0f * pp1 - pp2);
+    float bb = fabsf(pm2 + 16.0f * pm1 + 30.0f * p0 + 16.0f * pp1 + pp2);
+    p.sx[kw] = (aa / (bb + 1.0e-30f)) * ducros;
+    pm2 = P[kw - 2];
+    pm1 = P[kw - 1];
+    pp1 = P[kw + 1];
+    pp2 = P[kw + 2];
+    aa = fabsf(-pm2 + 16.0f * pm1 - 30.0f * p0 + 16.0f * pp1 - pp2);
+    bb = fabsf(pm2 + 16.0f * pm1 + 30.0f * p0 + 16.0f * pp1 + pp2);
+    p.sy[kw] = (aa / (bb + 1.0e-30f)) * ducros;
+}
+
+__global__ void widen_kernel(const float *src, double *dst, long long n)
+{
+    long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (k < n) dst[k] = double(src[k]);
 }
 
 __global__ void copy_old_kernel(Grid g, Fields q, Fields old)
@@ -412,25 +537,55 @@ void launch_prep(const Grid &g, const Eos &e, const Fields &q, const Prep &p, in
     sensor_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, q, p, variant == kSC);
 }
 
-void launch_limiter(const Grid &g, const Eos &e, const Fields &q, const Face7 &fh, const Face7 &gh,
-                    const Face7 &fl, const Face7 &gl, double *const theta[3], double dt,
-                    const double *dt_dev, const Counters &cnt, cudaStream_t s)
+template <typename FT>
+void launch_limiter(const Grid &g, const Eos &e, const Fields &q, const Face<FT> &fh,
+                    const Face<FT> &gh, const Face<FT> &fl, const Face<FT> &gl,
+                    double *const theta[3], double dt, const double *dt_dev, const Counters &cnt,
+                    cudaStream_t s)
 {
     const dim3 gt = grid2(g.ny, g.nx), gb = grid2(g.ny + 1, g.nx + 1), bl(BX, BY);
-    theta_kernel<0><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, theta[0], dt, dt_dev, cnt.limited);
-    blend_kernel<<<gb, bl, 0, s>>>(g, fh, gh, fl, gl, theta[0]);
-    theta_kernel<1><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, theta[1], dt, dt_dev, cnt.limited);
-    blend_kernel<<<gb, bl, 0, s>>>(g, fh, gh, fl, gl, theta[1]);
-    theta_kernel<2><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, theta[2], dt, dt_dev, cnt.limited);
-    blend_kernel<<<gb, bl, 0, s>>>(g, fh, gh, fl, gl, theta[2]);
+    theta_kernel<0, FT><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, theta[0], dt, dt_dev, cnt.limited);
+    blend_kernel<FT><<<gb, bl, 0, s>>>(g, fh, gh, fl, gl, theta[0]);
+    theta_kernel<1, FT><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, theta[1], dt, dt_dev, cnt.limited);
+    blend_kernel<FT><<<gb, bl, 0, s>>>(g, fh, gh, fl, gl, theta[1]);
+    theta_kernel<2, FT><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, theta[2], dt, dt_dev, cnt.limited);
+    blend_kernel<FT><<<gb, bl, 0, s>>>(g, fh, gh, fl, gl, theta[2]);
 }
 
+template <typename FT>
 void launch_final(const Grid &g, const Eos &e, unsigned flags, const Fields &q, const Fields &old,
-                  const Face7 &fh, const Face7 &gh, double dt, const double *dt_dev, double alpha,
-                  double beta, const Counters &cnt, cudaStream_t s)
+                  const Face<FT> &fh, const Face<FT> &gh, double dt, const double *dt_dev,
+                  double alpha, double beta, const Counters &cnt, cudaStream_t s)
 {
-    final_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, e, flags, q, old, fh, gh, dt,
-                                                              dt_dev, alpha, beta, cnt);
+    final_kernel<FT><<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, e, flags, q, old, fh, gh, dt,
+                                                                  dt_dev, alpha, beta, cnt);
+}
+
+template void launch_limiter<double>(const Grid &, const Eos &, const Fields &, const Face<double> &,
+                                     const Face<double> &, const Face<double> &, const Face<double> &,
+                                     double *const[3], double, const double *, const Counters &,
+                                     cudaStream_t);
+template void launch_limiter<float>(const Grid &, const Eos &, const Fields &, const Face<float> &,
+                                    const Face<float> &, const Face<float> &, const Face<float> &,
+                                    double *const[3], double, const double *, const Counters &,
+                                    cudaStream_t);
+template void launch_final<double>(const Grid &, const Eos &, unsigned, const Fields &, const Fields &,
+                                   const Face<double> &, const Face<double> &, double, const double *,
+                                   double, double, const Counters &, cudaStream_t);
+template void launch_final<float>(const Grid &, const Eos &, unsigned, const Fields &, const Fields &,
+                                  const Face<float> &, const Face<float> &, double, const double *,
+                                  double, double, const Counters &, cudaStream_t);
+
+void launch_prep32(const Grid &g, const Eos &e, const Fields &q, const PrepT<float> &p,
+                   const Cells32 &c, int variant, cudaStream_t s)
+{
+    prep32_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, e, q, p, c);
+    sensor32_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, p, c, variant == kSC);
+}
+
+void launch_widen(const float *src, double *dst, long long n, cudaStream_t s)
+{
+    widen_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, dst, n);
 }
 
 void launch_copy_old(const Grid &g, const Fields &q, const Fields &old, cudaStream_t s)
