@@ -259,6 +259,14 @@ def run_ours(args):
         if world > 1:
             dist.barrier()
 
+    if args.form == "fp32":
+        ms32, prof32, finite32 = time_form("fp32", args.steps, args.warmup, dev)
+        v32 = NX * NY * 3 * args.steps / (ms32 * 1e-3) / 1e6
+        if rank == 0:
+            print(json.dumps({"metric": "Mcell-stage/s", "value": round(v32, 3), "unit": "Mcell-stage/s",
+                              "form": "precision_fp32", "workload": WORKLOAD, "finite": finite32,
+                              "kernels": {g: [round(t, 3), n] for g, (t, n) in prof32.items()}}), flush=True)
+        return 0
     fp64_peak = wavemp.probe_fp64_flops()
     s = wavemp.Solver(params(), NX, NY)
     q = wavemp.ic.triple_point(NX, NY, device=dev)
@@ -365,6 +373,10 @@ def run_ours(args):
     # ---- precision form (binary32 face sweep, binary64 recovery / bound solves / accumulation) ----
     del q, old, host, s
     torch.cuda.empty_cache()
+    if args.form == "plain":
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        return 0
     ms32, prof32, finite32 = time_form("fp32", args.steps, args.warmup, dev)
     if world > 1:
         t = torch.tensor([ms32], dtype=torch.float64, device=dev)
@@ -406,6 +418,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", default=None,
                     help="NXxNY: a smaller case of the same problem (profiling captures only)")
+    ap.add_argument("--form", choices=("both", "plain", "fp32"), default="both",
+                    help="profiling captures: time only the plain or only the precision form")
     args = ap.parse_args()
     if args.grid:
         global NX, NY, WORKLOAD
