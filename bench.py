@@ -44,7 +44,8 @@ SAMPLE_NX, SAMPLE_NY = 3584, 1536    # CPU sample: a quarter of the cells of the
 # Face-sweep binary64 work per face (x or y) and traffic per cell-stage, from the ncu captures
 # summarised in profiles/ (None until measured).
 FP64_FLOP_PER_FACE = 1020.0  # profiles/face_kernel_triple_point_2048x1024_fp64.md
-DRAM_BYTES_PER_CELL_STAGE = None
+DRAM_BYTES_PER_CELL_STAGE_FP32 = 1265.0
+DRAM_BYTES_PER_CELL_STAGE = 2140.0  # profiles/dram_traffic_triple_point_2048x1024.md
 
 
 def params(nx=None, ny=None, precision="fp64"):
@@ -392,6 +393,7 @@ def run_ours(args):
                           "fields": precision_errors(err_steps, dev)},
         "roofline": {"bound": "hbm", "achieved": round(ALG_BYTES_PER_CELL_STAGE * cells / (ms32 / args.steps / 3 * 1e-3) / 1e9, 2),
                      "peak": hbm, "unit": "GB/s",
+                     "traffic": round(DRAM_BYTES_PER_CELL_STAGE_FP32 * cells / 1e9, 3),
                      "frac": round(ALG_BYTES_PER_CELL_STAGE * cells / (ms32 / args.steps / 3 * 1e-3) / 1e9 / hbm, 5)},
     }}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
