@@ -135,6 +135,25 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+# --------------------------------------------------------------------------- replicas --------
+def max_over_ranks(x, world, device="cpu"):
+    """Largest value of x over the ranks (the slowest replica sets the whole job's time)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(cells_per_rank, steps, world, ms):
+    """Mcell-stage/s of all replicas together: every rank advances its own solve `steps` steps of
+    three stages each, and the job takes the slowest rank's `ms`."""
+    return cells_per_rank * 3 * steps * world / (ms * 1e-3) / 1e6
+
+
 # ------------------------------------------------------------------------------ clocks ------
 class ClockSampler:
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -298,12 +317,9 @@ def run_ours(args):
     clk = clocks.stop()
     dt_now = s.get_dt(q)
     finite = all(bool(torch.isfinite(q[k]).all()) for k in wavemp.FIELDS) and dt_now > 0
-    if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, dev)
     cells = NX * NY
-    value = cells * 3 * args.steps * world / (ms * 1e-3) / 1e6
+    value = whole_job_rate(cells, args.steps, world, ms)
     ms_step = ms / args.steps
     launches = sum(n for _, n in prof.values())
 
@@ -330,11 +346,8 @@ def run_ours(args):
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     ms_e2e = max(f0.elapsed_time(f1), wall * 1e3)
-    if world > 1:
-        t = torch.tensor([ms_e2e], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_e2e = float(t.item())
-    e2e_value = cells * 3 * ke * world / (ms_e2e * 1e-3) / 1e6
+    ms_e2e = max_over_ranks(ms_e2e, world, dev)
+    e2e_value = whole_job_rate(cells, ke, world, ms_e2e)
 
     # ---- roofline and FP64 rate ----
     hbm, hbm_kind = measured_peaks()
@@ -379,11 +392,8 @@ def run_ours(args):
             print(json.dumps(line), flush=True)
         return 0
     ms32, prof32, finite32 = time_form("fp32", args.steps, args.warmup, dev)
-    if world > 1:
-        t = torch.tensor([ms32], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms32 = float(t.item())
-    v32 = cells * 3 * args.steps * world / (ms32 * 1e-3) / 1e6
+    ms32 = max_over_ranks(ms32, world, dev)
+    v32 = whole_job_rate(cells, args.steps, world, ms32)
     err_steps = 10
     line["forms"] = {"precision_fp32": {
         "value": round(v32, 3), "unit": "Mcell-stage/s", "ms_per_step": round(ms32 / args.steps, 3),
