@@ -125,6 +125,151 @@ def precision_errors(steps, dev):
     return out
 
 
+def batched_form(dev, steps, warmup, n=64):
+    """Batched form on the batched workload (64 shock-droplet solves, grids log-uniform 128x64 to
+    1024x512, seed 0): `steps` SSP-RK3 steps of every solve in persistent launches, binary64 and
+    binary32 forms after the tile-shape autotuner, against the same solves stepped one after the
+    other through the plain binary64 per-solve path. Returns (summary, tuned shapes of the
+    binary32 batch)."""
+    import torch
+
+    import wavemp
+    from wavemp.batch import Batch, config3_solves
+
+    specs = config3_solves(n=n, seed=0, steps=0, device=dev)
+    cells = sum(sp.nx * sp.ny for sp in specs)
+    stream = torch.cuda.current_stream()
+    out, batches, shapes32 = {}, {}, {}
+    for prec in ("fp64", "fp32"):
+        b = Batch(n, precision=prec, device=dev)
+        for sp in specs:
+            b.add(sp)
+        t0 = time.perf_counter()
+        report = b.autotune(steps=1, repeats=2)
+        tune_s = time.perf_counter() - t0
+        b.run(warmup)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.run(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        st = b.status()
+        info = b.info()
+        ok = all(x["steps"] == warmup + steps for x in st[:n])
+        out[prec] = {"value": round(cells * 3 * steps / (ms * 1e-3) / 1e6, 3), "unit": "Mcell-stage/s",
+                     "ms_per_step": round(ms / steps, 3), "graph": info["graph"], "tiles": info["tiles"],
+                     "grid": info["grid"], "steps_ok": ok, "autotune_s": round(tune_s, 2),
+                     "shapes": {str(c): int(v[0]) for c, v in report.items()}}
+        batches[prec] = b
+        if prec == "fp32":
+            shapes32 = {c: int(v[0]) for c, v in report.items()}
+    # density L1 of the binary32 batch against the binary64 batch after the same number of steps
+    worst = 0.0
+    for k in range(n):
+        a, c = batches["fp32"].slots[k]["q"], batches["fp64"].slots[k]["q"]
+        ra, rc = (a["ar1"] + a["ar2"])[5:-5, 5:-5], (c["ar1"] + c["ar2"])[5:-5, 5:-5]
+        worst = max(worst, float((ra - rc).abs().sum() / rc.abs().sum()))
+    for b in batches.values():
+        b.close()
+    del batches
+    torch.cuda.empty_cache()
+    # serial plain binary64: each solve alone through the per-solve path, same step count
+    total_ms = 0.0
+    for sp in specs:
+        p = wavemp.SolverParams(dx=sp.dx, dy=sp.dy, gamma1=sp.gamma1, pinf1=sp.pinf1, bc=sp.bc,
+                                recon="mp5c6", variant="sc", cfl=0.4)
+        s = wavemp.Solver(p, sp.nx, sp.ny, device=dev)
+        q = sp.make_state()
+        old = wavemp.alloc_state(sp.nx, sp.ny, names=wavemp.FIELDS, device=dev)
+        s.initialize(q)
+        s.init_dt(q)
+        for _ in range(min(warmup, 2)):
+            s.step(q, old, None, sync=False)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            s.step(q, old, None, sync=False)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        total_ms += e0.elapsed_time(e1)
+        s.close()
+    serial = cells * 3 * steps / (total_ms * 1e-3) / 1e6
+    summary = {
+        "workload": f"{n} shock-droplet solves, grids log-uniform 128x64..1024x512 (seed 0), "
+                    f"{cells} cells in all; {steps} steps timed after {warmup} warm-up",
+        "batched_fp64": out["fp64"], "batched_fp32": out["fp32"],
+        "serial_plain_fp64": {"value": round(serial, 3), "unit": "Mcell-stage/s",
+                              "ms_per_step": round(total_ms / steps, 3)},
+        "speedup_fp32_vs_serial_plain": round(out["fp32"]["value"] / serial, 3),
+        "speedup_fp64_vs_serial_plain": round(out["fp64"]["value"] / serial, 3),
+        "density_l1_fp32_vs_fp64_max_over_solves": worst,
+    }
+    return summary, shapes32
+
+
+def served_form(dev, nreq, shapes=None, capacity=16, chunk_steps=10):
+    """Serving form on the serving workload (Poisson arrivals at 20/s, seed 0, grids log-uniform
+    64x32 to 2048x1024, step counts U[50, 2000], binary32 form, 150 GB admission budget): p50/p99
+    latency (arrival to result on the host) and cell-stage/s, beside the same requests served one
+    at a time in arrival order by the plain binary64 per-solve path, whose service time is the
+    measured step time at each request's grid times its step count."""
+    import torch
+
+    import wavemp
+    from wavemp.serve import Server, percentile, poisson_requests, serial_schedule
+
+    reqs = poisson_requests(nreq, rate=20.0, seed=0, device=dev)
+    srv = Server(capacity=capacity, budget_bytes=150e9, precision="fp32", chunk_steps=chunk_steps,
+                 shapes=shapes, keep_results=False, device=dev)
+    served = srv.run(reqs)
+    served.update({"slots": capacity, "chunk_steps": chunk_steps, "budget_gb": 150.0,
+                   "peak_admitted_gb": round(srv.admission.peak_bytes / 1e9, 3), "launches": srv.launches})
+    srv.close()
+    torch.cuda.empty_cache()
+    stream = torch.cuda.current_stream()
+    per_step = {}
+    for r in reqs:
+        key = (r.spec.nx, r.spec.ny)
+        if key in per_step:
+            continue
+        sp = r.spec
+        p = wavemp.SolverParams(dx=sp.dx, dy=sp.dy, gamma1=sp.gamma1, pinf1=sp.pinf1, bc=sp.bc,
+                                recon="mp5c6", variant="sc", cfl=0.4)
+        s = wavemp.Solver(p, sp.nx, sp.ny, device=dev)
+        q = sp.make_state()
+        old = wavemp.alloc_state(sp.nx, sp.ny, names=wavemp.FIELDS, device=dev)
+        s.initialize(q)
+        s.init_dt(q)
+        for _ in range(2):
+            s.step(q, old, None, sync=False)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(5):
+            s.step(q, old, None, sync=False)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        per_step[key] = e0.elapsed_time(e1) / 5 * 1e-3
+        s.close()
+    arrivals = [r.arrival for r in reqs]
+    finish = serial_schedule(arrivals, [per_step[(r.spec.nx, r.spec.ny)] * r.spec.max_steps for r in reqs])
+    lat = [f - a for f, a in zip(finish, arrivals)]
+    work = sum(r.cell_stages for r in reqs)
+    serial = {"p50_s": round(percentile(lat, 50), 4), "p99_s": round(percentile(lat, 99), 4),
+              "makespan_s": round(max(finish) - min(arrivals), 4),
+              "value": round(work / (max(finish) - min(arrivals)) / 1e6, 3), "unit": "Mcell-stage/s",
+              "service_time": "measured plain binary64 step time at the request's grid x its steps"}
+    return {"workload": f"{nreq} requests, Poisson 20/s (seed 0), grids 64x32..2048x1024, "
+                        f"steps U[50,2000], binary32 form",
+            "served_fp32": served, "serial_plain_fp64": serial,
+            "speedup_vs_serial_plain": round(served["value"] / serial["value"], 3),
+            "p50_ratio_serial_over_served": round(serial["p50_s"] / served["p50_s"], 3),
+            "p99_ratio_serial_over_served": round(serial["p99_s"] / served["p99_s"], 3)}
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -279,6 +424,17 @@ def run_ours(args):
         if world > 1:
             dist.barrier()
 
+    if args.form in ("batched", "serve"):
+        if args.form == "batched":
+            res, _ = batched_form(dev, args.batch_steps, args.warmup)
+            value = res["batched_fp32"]["value"]
+        else:
+            res = served_form(dev, args.serve_requests, capacity=args.serve_slots, chunk_steps=args.serve_chunk)
+            value = res["served_fp32"]["value"]
+        if rank == 0:
+            print(json.dumps({"metric": "Mcell-stage/s", "value": value, "unit": "Mcell-stage/s",
+                              "form": args.form, **res}), flush=True)
+        return 0
     if args.form == "fp32":
         ms32, prof32, finite32 = time_form("fp32", args.steps, args.warmup, dev)
         v32 = NX * NY * 3 * args.steps / (ms32 * 1e-3) / 1e6
@@ -406,6 +562,10 @@ def run_ours(args):
                      "traffic": round(DRAM_BYTES_PER_CELL_STAGE_FP32 * cells / 1e9, 3),
                      "frac": round(ALG_BYTES_PER_CELL_STAGE * cells / (ms32 / args.steps / 3 * 1e-3) / 1e9 / hbm, 5)},
     }}
+    batched, shapes32 = batched_form(dev, args.batch_steps, args.warmup)
+    line["forms"]["batched"] = batched
+    line["forms"]["served"] = served_form(dev, args.serve_requests, shapes=shapes32,
+                                          capacity=args.serve_slots, chunk_steps=args.serve_chunk)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         os.environ.setdefault("OMP_NUM_THREADS", str(cores))
@@ -430,8 +590,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", default=None,
                     help="NXxNY: a smaller case of the same problem (profiling captures only)")
-    ap.add_argument("--form", choices=("both", "plain", "fp32"), default="both",
-                    help="profiling captures: time only the plain or only the precision form")
+    ap.add_argument("--form", choices=("both", "plain", "fp32", "batched", "serve"), default="both",
+                    help="time one form alone (profiling captures, full-length batched/served runs)")
+    ap.add_argument("--batch-steps", type=int, default=20,
+                    help="steps of the 64-solve batched workload (300 is the full workload)")
+    ap.add_argument("--serve-requests", type=int, default=24, help="requests of the serving workload")
+    ap.add_argument("--serve-slots", type=int, default=16, help="slots of the serving batch")
+    ap.add_argument("--serve-chunk", type=int, default=10, help="steps per serving launch")
     args = ap.parse_args()
     if args.grid:
         global NX, NY, WORKLOAD

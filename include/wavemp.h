@@ -144,6 +144,57 @@ int wm_step(wm_handle *h, const wm_fields *q, const wm_fields *q_old, double dt,
  * with dt <= 0. */
 int wm_init_dt(wm_handle *h, const wm_fields *q, void *stream);
 
+/* ---- batched form: many independent solves, one persistent launch per call -------------------
+ * A batch holds up to `capacity` solves in slots. Each solve has its own grid size, cell sizes,
+ * equation of state, boundary rules, end time and step budget, and its own cell arrays and
+ * workspace (caller-owned device memory of wm_solve_workspace_bytes); all solves of a batch share
+ * the scheme (variant, reconstruction, precision, repair, ghost width, CFL). wm_batch_run advances
+ * every unfinished solve by up to nsteps SSP-RK3 steps in ONE persistent cooperative kernel launch
+ * (replayed from a CUDA graph captured on first use), each with its own device-resident dt
+ * (CFL 0.4 of its own state, clamped to its end time). Slots can be filled and cleared between
+ * runs (continuous batching). The batched counterpart of the reference's time loop, SC:2009-2059. */
+typedef struct wm_batch wm_batch;
+typedef struct wm_batch_params {
+    int variant, recon, precision, emergency_repair; /* as in wm_params */
+    int g;                                           /* ghost layers of every solve */
+    double cfl;
+    int tile_shape; /* -1: per grid-size class (wm_batch_tile_shape; 32-wide tiles by default),
+                       0..3: every grid in tiles of 1x128, 2x64, 4x32 or 8x16 cells */
+} wm_batch_params;
+typedef struct wm_solve_desc {
+    int nx, ny;
+    double dx, dy;
+    double gamma1, pinf1, gamma2, pinf2;
+    int bc[4];
+    double t_end;         /* > 0: stop at this time (the last dt is clamped to reach it) */
+    long long max_steps;  /* > 0: stop after this many steps */
+    wm_fields q, q_old;   /* the solve's ten cell arrays and six step-start arrays */
+} wm_solve_desc;
+typedef struct wm_solve_status {
+    int used, done;
+    double t, dt;         /* elapsed time, dt of the next step */
+    long long steps;
+} wm_solve_status;
+size_t wm_solve_workspace_bytes(const wm_batch_params *p, int nx, int ny);
+int wm_batch_create(const wm_batch_params *p, int capacity, wm_batch **out);
+void wm_batch_destroy(wm_batch *b);
+/* Occupy `slot` with a solve whose state is already initialised (the start-up sequence of the
+ * reference, SC:1998-2007, e.g. with wm_create + the closures). Time and step count start at 0. */
+int wm_batch_set(wm_batch *b, int slot, const wm_solve_desc *d, void *workspace, size_t bytes);
+int wm_batch_clear(wm_batch *b, int slot);
+/* dt of the slot's first step from its current state (get_dt), on the device. */
+int wm_batch_init_dt(wm_batch *b, int slot, void *stream);
+int wm_batch_run(wm_batch *b, int nsteps, void *stream);
+/* Waits for the stream and copies every slot's status (capacity entries); WM_ERR_STATE if a grid
+ * barrier of an earlier run timed out. */
+int wm_batch_query(wm_batch *b, wm_solve_status *out, void *stream);
+/* Tile shape (0..3) for the grids whose cell count has floor(log2(nx*ny)) == size_class. */
+int wm_batch_tile_shape(wm_batch *b, int size_class, int shape);
+/* Copy the per-slot scalars (dt accumulator, dt, t, steps, done; 40 bytes per slot) to (write=0)
+ * or from (write=1) host memory -- snapshot and restore for measuring runs. */
+int wm_batch_scalars(wm_batch *b, void *host, int write, void *stream);
+int wm_batch_info(wm_batch *b, int *ntiles, int *grid, int *graph);
+
 /* ---- diagnostics ---------------------------------------------------------------------------- */
 /* Copy workspace array `which` (WM_WS_*) of the padded grid into the caller's device buffer dst
  * (same padded shape, contiguous rows of ny + 2g). */

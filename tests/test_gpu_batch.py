@@ -1,0 +1,122 @@
+"""Batched form: uneven solves in one persistent launch give the same results as each solve run
+alone through the per-solve API (same kernels' arithmetic, same device dt), stop on their own step
+budget or end time, survive autotuning unchanged, and can join a running batch."""
+import numpy as np
+import pytest
+
+import parity_util as pu
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA device", allow_module_level=True)
+
+import wavemp  # noqa: E402
+from wavemp import Solver, SolverParams, alloc_state, ic  # noqa: E402
+from wavemp.batch import Batch, SolveSpec  # noqa: E402
+
+SIZES = [(40, 20), (64, 32), (33, 17), (96, 48), (128, 64), (8, 4)]
+
+
+def spec(nx, ny, mach=2.4, **kw):
+    return SolveSpec(nx=nx, ny=ny, dx=1.0 / nx, dy=0.5 / ny,
+                     state=ic.shock_droplet(nx, ny, 1.0, 0.5, mach=mach), **kw)
+
+
+def alone(sp: SolveSpec, steps, precision, recon="mp5c6", variant="sc"):
+    p = SolverParams(dx=sp.dx, dy=sp.dy, gamma1=sp.gamma1, pinf1=sp.pinf1, bc=sp.bc,
+                     precision=precision, recon=recon, variant=variant)
+    s = Solver(p, sp.nx, sp.ny)
+    q = {k: v.clone() for k, v in sp.state.items()}
+    old = alloc_state(sp.nx, sp.ny, names=wavemp.FIELDS)
+    s.initialize(q)
+    s.init_dt(q)
+    for _ in range(steps):
+        s.step(q, old, None, sync=False)
+    torch.cuda.synchronize()
+    return q
+
+
+def compare(q_batch, q_alone, what, precision="fp64"):
+    """FP64: the parity tolerance. FP32: per-field L1 <= 1e-6 and largest element error <= 1e-3
+    (the precision form's stage bound; measured 8e-9). The persistent kernel inlines the same
+    source in another context, where the compiler may fuse multiply-adds differently, and a
+    one-ulp binary32 difference can move a threshold decision of the scheme at an isolated face."""
+    got = {k: pu.host(v) for k, v in q_batch.items()}
+    ref = {k: pu.host(v) for k, v in q_alone.items()}
+    sc = pu.natural_scales(ref, 4.4, 6e8, 1.4, 0.0)
+    pu.assert_cells(got, ref, pu.ALL, sc, what, rtol=1e-10 if precision == "fp64" else 1e-3)
+    if precision == "fp32":
+        for k in ("ar1", "ar2", "ru", "rv", "E", "al"):
+            a, b = got[k][5:-5, 5:-5], ref[k][5:-5, 5:-5]
+            e = np.abs(a - b).sum() / max(np.abs(b).sum(), 1e-300)
+            assert e <= 1e-6, f"{what} {k}: L1 {e:.2e}"
+    return all(np.array_equal(got[k], ref[k], equal_nan=True) for k in pu.ALL)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_batch_matches_solves_run_alone(precision):
+    steps = 3
+    specs = [spec(nx, ny, max_steps=steps) for nx, ny in SIZES]
+    b = Batch(len(specs) + 2, precision=precision)
+    for sp in specs:
+        b.add(sp)
+    b.run(steps + 2)  # more steps than any budget: solves stop at their own count
+    st = b.status()
+    bitwise = True
+    for k, sp in enumerate(specs):
+        assert st[k]["done"] and st[k]["steps"] == steps
+        bitwise &= compare(b.slots[k]["q"], alone(sp, steps, precision), f"{precision} slot {k} {sp.nx}x{sp.ny}",
+                           precision)
+    assert not st[len(specs)]["used"]
+    info = b.info()
+    assert info["tiles"] > 0
+    print("bitwise equal to the per-solve path:", bitwise, "graph:", info["graph"])
+
+
+def test_end_time_and_step_budget_per_solve():
+    a = spec(48, 24, max_steps=2)
+    c = spec(64, 32)
+    b = Batch(2)
+    b.add(a)
+    b.add(c)
+    dt0 = b.status()[1]["dt"]
+    c.t_end = 0.0  # set below after reading dt
+    b.remove(1)
+    c2 = spec(64, 32, t_end=2.5 * dt0)
+    b.add(c2, slot=1)
+    b.run(10)
+    st = b.status()
+    assert st[0]["done"] and st[0]["steps"] == 2
+    assert st[1]["done"] and st[1]["steps"] == 3
+    assert abs(st[1]["t"] - 2.5 * dt0) <= 1e-9 * dt0
+
+
+def test_autotune_leaves_state_unchanged_and_picks_shapes():
+    specs = [spec(nx, ny, max_steps=4) for nx, ny in SIZES[:4]]
+    b1, b2 = Batch(4), Batch(4, tile_shape=2)
+    for sp in specs:
+        b1.add(sp)
+        b2.add(sp)
+    report = b1.autotune(steps=1, repeats=1)
+    assert report and all(0 <= shape < 4 for shape, _ in report.values())
+    b1.run(4)
+    b2.run(4)
+    for k in range(len(specs)):
+        compare(b1.slots[k]["q"], b2.slots[k]["q"], f"autotuned slot {k}")
+        assert b1.status()[k]["steps"] == 4
+
+
+def test_solve_joining_a_running_batch_matches_alone():
+    first = spec(64, 32, max_steps=4)
+    late = spec(96, 48, mach=4.0, max_steps=3)
+    b = Batch(3)
+    b.add(first)
+    b.run(2)
+    b.add(late)
+    b.run(5)
+    st = b.status()
+    assert st[0]["steps"] == 4 and st[1]["steps"] == 3
+    compare(b.slots[0]["q"], alone(first, 4, "fp64"), "early solve")
+    compare(b.slots[1]["q"], alone(late, 3, "fp64"), "late solve")

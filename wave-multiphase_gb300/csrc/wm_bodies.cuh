@@ -1,0 +1,559 @@
+// wm_bodies.cuh -- per-cell and per-face bodies of the stage kernels, shared by the per-solve
+// kernels (wm_stage.cu, wm_faces.cu) and the batched persistent kernel (wm_batch.cu). Each body
+// handles one cell (i, j) or the faces it owns; callers do the index mapping and range checks.
+#pragma once
+#include "wm_kernels.cuh"
+
+namespace wm {
+
+__device__ __forceinline__ long long kf_of(const Fields &q, int i, int j)
+{
+    return (long long)i * q.pitch + j;
+}
+__device__ __forceinline__ long long kw_of(const Grid &g, int i, int j)
+{
+    return (long long)i * g.nyg + j;
+}
+
+// Warp-aggregated counter increment (one atomic per warp).
+__device__ __forceinline__ void count_if(unsigned long long *ctr, bool pred)
+{
+    unsigned mask = __activemask();
+    unsigned b = __ballot_sync(mask, pred);
+    if (b && (threadIdx.x & 31) == (__ffs(mask) - 1)) atomicAdd(ctr, (unsigned long long)__popc(b));
+}
+
+// Entropy (SC:308-314) and the first-order HLLC cell state of fx_low_kernel (SC:1309-1327), both
+// pure functions of one cell, computed once per cell instead of once per face that reads them.
+__device__ __forceinline__ void prep_body(const Grid &g, const Eos &e, const Fields &q, const Prep &p, int i, int j)
+{
+    long long kf = kf_of(q, i, j), kw = kw_of(g, i, j);
+    double ar1 = q.f[F_AR1][kf], ar2 = q.f[F_AR2][kf], ru = q.f[F_RU][kf], rv = q.f[F_RV][kf];
+    double pp = q.f[F_P][kf], al = q.f[F_AL][kf];
+
+    double ge, pie;
+    mix_gamma_pinf(e, al, ge, pie);
+    double rho_e = ar1 + ar2;
+    if (rho_e < kTiny) rho_e = kTiny;
+    p.ent[kw] = pp / pow(rho_e, ge);
+
+    double rho = ar1 + ar2;
+    double ir = 1.0 / rho;
+    double a = clamp01_pp(al);
+    double gg = ge, pi = pie;
+    if (!(a == al)) mix_gamma_pinf(e, a, gg, pi);
+    double pl = pp;
+    if (isnan(pl) || (pl + pi) / (gg - 1.0) < kPpCtilde) pl = kPpCtilde * (gg - 1.0) - pi;
+    double u = ru * ir, v = rv * ir;
+    p.lu[kw] = u;
+    p.lv[kw] = v;
+    p.lp[kw] = pl;
+    p.la[kw] = a;
+    p.lc[kw] = sound_speed_r(e, ir, pl, a);
+    p.lE[kw] = prim_to_energy(e, rho, u, v, pl, a);
+}
+
+// Smoothness indicator per cell and direction (cator2_val, SC:318-325) and the Ducros x pressure
+// sensor (ducros_kernel, SC:875-916).
+__device__ __forceinline__ void sensor_body(const Grid &g, const Fields &q, const Prep &p, int sc, int i, int j)
+{
+    long long kw = kw_of(g, i, j);
+    const long long W = g.nyg;
+    const double *en = p.ent;
+    if (i >= 2 && i < g.nxg - 2)
+        p.cx[kw] = cator2_val(en[kw - 2 * W], en[kw - W], en[kw], en[kw + W], en[kw + 2 * W]);
+    if (j >= 2 && j < g.nyg - 2)
+        p.cy[kw] = cator2_val(en[kw - 2], en[kw - 1], en[kw], en[kw + 1], en[kw + 2]);
+    if (!sc) return;
+    if (i < 2 || i >= g.nxg - 2 || j < 2 || j >= g.nyg - 2) {
+        p.sx[kw] = 1.0;
+        p.sy[kw] = 1.0;
+        return;
+    }
+    const double *U = q.f[F_U], *V = q.f[F_V], *P = q.f[F_P];
+    long long kf = kf_of(q, i, j), Q = q.pitch;
+    double der_ux = 0.5 * (-U[kf - Q] + U[kf + Q]);
+    double der_vx = 0.5 * (-V[kf - Q] + V[kf + Q]);
+    double der_uy = 0.5 * (-U[kf - 1] + U[kf + 1]);
+    double der_vy = 0.5 * (-V[kf - 1] + V[kf + 1]);
+    double div_u = der_ux + der_vy;
+    double curl_u = der_vx - der_uy;
+    double ducros = div_u * div_u / (div_u * div_u + curl_u * curl_u + 1.0e-30);
+    double p0 = P[kf];
+    double pm2 = P[kf - 2 * Q], pm1 = P[kf - Q], pp1 = P[kf + Q], pp2 = P[kf + 2 * Q];
+    double aa = fabs(-pm2 + 16.0 * pm1 - 30.0 * p0 + 16.0 * pp1 - pp2);
+    double bb = fabs(pm2 + 16.0 * pm1 + 30.0 * p0 + 16.0 * pp1 + pp2);
+    p.sx[kw] = (aa / (bb + 1.0e-30)) * ducros;
+    pm2 = P[kf - 2];
+    pm1 = P[kf - 1];
+    pp1 = P[kf + 1];
+    pp2 = P[kf + 2];
+    aa = fabs(-pm2 + 16.0 * pm1 - 30.0 * p0 + 16.0 * pp1 - pp2);
+    bb = fabs(pm2 + 16.0 * pm1 + 30.0 * p0 + 16.0 * pp1 + pp2);
+    p.sy[kw] = (aa / (bb + 1.0e-30)) * ducros;
+}
+
+// pp_cell_theta_kernel (SC:1397-1476): residuals of the current (partly blended) high-order and of
+// the first-order fluxes, bound solve of this pass. Pass 0 bounds the partial densities, pass 1
+// alpha and 1 - alpha, pass 2 rho c~^2 (theta_cons_stage, SC:268-292); each pass forms only the
+// residual components its bound uses.
+template <int STAGE, typename FT>
+__device__ __forceinline__ double theta_body(const Grid &g, const Eos &e, const Fields &q,
+                                             const Face<FT> &fh, const Face<FT> &gh,
+                                             const Face<FT> &fl, const Face<FT> &gl, double dt,
+                                             int i, int j)
+{
+    long long kf = kf_of(q, i, j), kw = kw_of(g, i, j), kx = kw - g.nyg, ky = kw - 1;
+    const FT idx = FT(g.inv_dx), idy = FT(g.inv_dy);
+    double l[6], h[6];
+    constexpr int C0 = STAGE == 1 ? 5 : 0, C1 = STAGE == 0 ? 2 : 6;
+#pragma unroll
+    for (int c = C0; c < C1; ++c) {
+        FT rh = (fh.f[c][kw] - fh.f[c][kx]) * idx + (gh.f[c][kw] - gh.f[c][ky]) * idy;
+        FT rl = (fl.f[c][kw] - fl.f[c][kx]) * idx + (gl.f[c][kw] - gl.f[c][ky]) * idy;
+        if (c == 5) {
+            FT a = FT(q.f[F_ALP][kf]);
+            rh = rh - a * (fh.f[6][kw] - fh.f[6][kx]) * idx - a * (gh.f[6][kw] - gh.f[6][ky]) * idy;
+            rl = rl - a * (fl.f[6][kw] - fl.f[6][kx]) * idx - a * (gl.f[6][kw] - gl.f[6][ky]) * idy;
+        }
+        double qc = q.f[c][kf];
+        l[c] = qc - dt * double(rl);
+        h[c] = qc - dt * double(rh);
+    }
+    double th;
+    if (STAGE == 2) {
+        th = theta_ctilde(e, l, h);
+    } else {
+        th = theta_cons_stage(e, l, h, STAGE);
+    }
+    return th;
+}
+
+// pp_blend_x_flux_kernel + pp_blend_y_flux_kernel (SC:1479-1548) in one launch: the thread at
+// (i, j) blends x-face (i, j) and y-face (i, j) when they exist. Face theta is the min over its
+// interior neighbours.
+template <typename FT>
+__device__ __forceinline__ void blend_body(const Grid &g, const Face<FT> &fh, const Face<FT> &gh,
+                                           const Face<FT> &fl, const Face<FT> &gl,
+                                           const double *theta, int i, int j)
+{
+    long long kw = kw_of(g, i, j);
+    bool ii = i >= g.g, ji = j >= g.g;  // cell (i, j) interior along x / y
+    if (ji) {                           // x face between (i, j) and (i+1, j)
+        double th = 1.0;
+        if (ii) th = wmin(th, theta[kw]);
+        if (i + 1 < g.g + g.nx) th = wmin(th, theta[kw + g.nyg]);
+        const FT t = FT(th);
+#pragma unroll
+        for (int c = 0; c < 7; ++c) fh.f[c][kw] = face_blend(fl.f[c][kw], fh.f[c][kw], t);
+    }
+    if (ii) {  // y face between (i, j) and (i, j+1)
+        double th = 1.0;
+        if (ji) th = wmin(th, theta[kw]);
+        if (j + 1 < g.g + g.ny) th = wmin(th, theta[kw + 1]);
+        const FT t = FT(th);
+#pragma unroll
+        for (int c = 0; c < 7; ++c) gh.f[c][kw] = face_blend(gl.f[c][kw], gh.f[c][kw], t);
+    }
+}
+
+// rk3_kernel (SC:1553-1611) on interior cells, then enforce_admissible_kernel (SC:918-958) and
+// cons_to_prim_kernel (SC:840-864) + al_prim copy on every cell, then the dt candidate of
+// timestep_kernel (SC:1686-1705) -- each step selected by `flags`.
+// Returns the bit pattern of the cell's time-step candidate (all ones when it has none).
+template <typename FT>
+__device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eos &e, unsigned flags,
+                                                         const Fields &q, const Fields &old,
+                                                         const Face<FT> &fh, const Face<FT> &gh,
+                                                         double dt, const double *dt_dev,
+                                                         double alpha, double beta,
+                                                         const Counters &cnt, int i, int j)
+{
+    bool inb = i < g.nxg && j < g.nyg;
+    bool interior = inb && i >= g.g && i < g.g + g.nx && j >= g.g && j < g.g + g.ny;
+    unsigned long long dt_bits = ~0ull;
+    if (inb && (interior || (flags & (FIN_ADMISSIBLE | FIN_PRIM)))) {
+        long long kf = kf_of(q, i, j);
+        double Q[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) Q[c] = q.f[c][kf];
+        bool wrote_q = false;
+        if (interior && (flags & FIN_SAVE_OLD)) {
+            long long ko = (long long)i * old.pitch + j;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) old.f[c][ko] = Q[c];
+        }
+        if (interior && (flags & FIN_RK3)) {
+            if (dt_dev) dt = *dt_dev;
+            long long kw = kw_of(g, i, j), kx = kw - g.nyg, ky = kw - 1;
+            const FT idx = FT(g.inv_dx), idy = FT(g.inv_dy);
+            FT ap = FT(q.f[F_ALP][kf]);
+            FT res[6];
+#pragma unroll
+            for (int c = 0; c < 5; ++c)
+                res[c] = (fh.f[c][kw] - fh.f[c][kx]) * idx + (gh.f[c][kw] - gh.f[c][ky]) * idy;
+            FT src6x = ap * (fh.f[6][kw] - fh.f[6][kx]) * idx;
+            FT src6y = ap * (gh.f[6][kw] - gh.f[6][ky]) * idy;
+            res[5] = (fh.f[5][kw] - fh.f[5][kx]) * idx + (gh.f[5][kw] - gh.f[5][ky]) * idy -
+                     src6x - src6y;
+            long long ko = (long long)i * old.pitch + j;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                double base = beta * (Q[c] - dt * double(res[c]));
+                Q[c] = (flags & FIN_OLD_READ) ? alpha * old.f[c][ko] + base : base;
+            }
+            wrote_q = true;
+        }
+        // 1/(rho Gamma) of the admissibility check, reused by the primitive recovery when alpha
+        // is unchanged by the second clamp
+        double rg_a1 = -1.0, rg_rho = 0.0, rg_inv = 0.0, rg_gb = 0.0, rg_pb = 0.0;
+        if (flags & FIN_ADMISSIBLE) {
+            double a1 = clamp01_pp(Q[F_AL]);
+            double m1 = Q[0], m2 = Q[1], mx = Q[2], my = Q[3], E = Q[4];
+            bool nonfinite = isnan(m1) || isnan(m2) || isnan(mx) || isnan(my) || isnan(E);
+            if (isnan(m1) || m1 < kPpRho) m1 = kPpRho;
+            if (isnan(m2) || m2 < kPpRho) m2 = kPpRho;
+            if (isnan(mx)) mx = 0.0;
+            if (isnan(my)) my = 0.0;
+            double rho = m1 + m2;
+            double gb, pb;
+            mix_gamma_pibig(e, a1, gb, pb);
+            const double inv = 1.0 / (rho * gb);
+            const double ir = gb * inv;
+            double uu = mx * ir, vv = my * ir;
+            double kin = 0.5 * rho * (uu * uu + vv * vv);
+            double p = (E - pb - kin) * (rho * inv);
+            // E - kin - p_inf < floor with p_inf = Pi / (1 + Gamma), multiplied by 1 + Gamma > 0
+            const double gp1 = 1.0 + gb;
+            bool repair = isnan(E) || isnan(p) || ((E - kin) * gp1 - pb < kPpCtilde * gp1);
+            if (repair) {
+                double gg, pi;
+                mix_gamma_pinf(e, a1, gg, pi);
+                double p_min = kPpCtilde * (gg - 1.0) - pi;
+                E = gb * p_min + pb + kin;
+            }
+            rg_a1 = a1; rg_rho = rho; rg_inv = inv; rg_gb = gb; rg_pb = pb;
+            Q[0] = m1;
+            Q[1] = m2;
+            Q[2] = mx;
+            Q[3] = my;
+            Q[4] = E;
+            Q[5] = a1;
+            wrote_q = true;
+            if (cnt.repaired) {
+                count_if(cnt.repaired, repair);
+                count_if(cnt.nonfinite, nonfinite);
+            }
+        }
+        if (flags & FIN_PRIM) {
+            double a1 = Q[F_AL];
+            if (a1 < kPrimAlphaFloor) a1 = kPrimAlphaFloor;
+            if (a1 > 1.0 - kPrimAlphaFloor) a1 = 1.0 - kPrimAlphaFloor;
+            Q[F_AL] = a1;
+            double rho = Q[0] + Q[1];
+            double gb, pb, inv;
+            if (a1 == rg_a1 && rho == rg_rho) {
+                gb = rg_gb; pb = rg_pb; inv = rg_inv;
+            } else {
+                mix_gamma_pibig(e, a1, gb, pb);
+                inv = 1.0 / (rho * gb);
+            }
+            double ir = gb * inv;
+            double uu = Q[2] * ir, vv = Q[3] * ir;
+            double pp = (Q[4] - pb - 0.5 * rho * (uu * uu + vv * vv)) * (rho * inv);
+            q.f[F_U][kf] = uu;
+            q.f[F_V][kf] = vv;
+            q.f[F_P][kf] = pp;
+            q.f[F_ALP][kf] = a1;
+            q.f[F_AL][kf] = a1;
+            if (interior && (flags & FIN_DT)) {
+                double c = sound_speed_r(e, ir, pp, a1);
+                double sx = g.dx / (fabs(uu) + c);
+                double sy = g.dy / (fabs(vv) + c);
+                double d = sx * sy / (sx + sy);
+                dt_bits = (unsigned long long)__double_as_longlong(d);
+            }
+        }
+        if (wrote_q) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) q.f[c][kf] = Q[c];
+        }
+    }
+    return dt_bits;
+}
+
+// Binary32 copies of the cell state for the face sweep, the entropy in binary32, and the
+// first-order HLLC cell state whose pressure floor and sound speed are recovered in binary64
+// (the stiffened-gas p + p_inf cancels to round-off of p_inf ~ 6e8 in binary32).
+__device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const Fields &q, const PrepT<float> &p, const Cells32 &c, int i, int j)
+{
+    long long kf = kf_of(q, i, j), kw = kw_of(g, i, j);
+    const double ar1 = q.f[F_AR1][kf], ar2 = q.f[F_AR2][kf], ru = q.f[F_RU][kf], rv = q.f[F_RV][kf];
+    const double pp = q.f[F_P][kf], al = q.f[F_AL][kf];
+    const float ar1f = float(ar1), ar2f = float(ar2), ruf = float(ru), rvf = float(rv);
+    const float pf = float(pp), alf = float(al);
+    c.ar1[kw] = ar1f;
+    c.ar2[kw] = ar2f;
+    c.ru[kw] = ruf;
+    c.rv[kw] = rvf;
+    c.p[kw] = pf;
+    c.al[kw] = alf;
+    c.u[kw] = float(q.f[F_U][kf]);
+    c.v[kw] = float(q.f[F_V][kf]);
+
+    float ge, pie;
+    mix_gamma_pinf(e, alf, ge, pie);
+    float rho_e = ar1f + ar2f;
+    if (rho_e < float(kTiny)) rho_e = float(kTiny);
+    p.ent[kw] = pf / powf(rho_e, ge);
+
+    // With g = 1 + 1/Gamma and p_inf = Pi / (1 + Gamma): (p + p_inf) / (g - 1) < floor  <=>
+    // ((1 + Gamma) p + Pi) Gamma < floor (1 + Gamma), and c^2 = ((1 + Gamma) p + Pi) / (Gamma rho).
+    const double rho = ar1 + ar2;
+    const double a = clamp01_pp(al);
+    double gb, pb;
+    mix_gamma_pibig(e, a, gb, pb);
+    const double gp1 = 1.0 + gb;
+    double pl = pp;
+    if (isnan(pl) || (gp1 * pl + pb) * gb < kPpCtilde * gp1) {
+        double gg, pi;
+        mix_gamma_pinf(e, a, gg, pi);
+        pl = kPpCtilde * (gg - 1.0) - pi;
+    }
+    double val = (gp1 * pl + pb) / (gb * rho);
+    if (val < kTiny) val = kTiny;
+    const float rhof = ar1f + ar2f;
+    const float irf = 1.0f / rhof;
+    const float u = ruf * irf, v = rvf * irf;
+    const float af = float(a), plf = float(pl);
+    p.lu[kw] = u;
+    p.lv[kw] = v;
+    p.lp[kw] = plf;
+    p.la[kw] = af;
+    p.lc[kw] = float(sqrt(val));
+    p.lE[kw] = prim_to_energy(e, rhof, u, v, plf, af);
+}
+
+// Smoothness indicators and Ducros sensor in binary32 (sensor_kernel's arithmetic).
+__device__ __forceinline__ void sensor32_body(const Grid &g, const PrepT<float> &p, const Cells32 &c, int sc, int i, int j)
+{
+    long long kw = kw_of(g, i, j);
+    const long long W = g.nyg;
+    const float *en = p.ent;
+    if (i >= 2 && i < g.nxg - 2)
+        p.cx[kw] = cator2_val(en[kw - 2 * W], en[kw - W], en[kw], en[kw + W], en[kw + 2 * W]);
+    if (j >= 2 && j < g.nyg - 2)
+        p.cy[kw] = cator2_val(en[kw - 2], en[kw - 1], en[kw], en[kw + 1], en[kw + 2]);
+    if (!sc) return;
+    if (i < 2 || i >= g.nxg - 2 || j < 2 || j >= g.nyg - 2) {
+        p.sx[kw] = 1.0f;
+        p.sy[kw] = 1.0f;
+        return;
+    }
+    const float *U = c.u, *V = c.v, *P = c.p;
+    float der_ux = 0.5f * (-U[kw - W] + U[kw + W]);
+    float der_vx = 0.5f * (-V[kw - W] + V[kw + W]);
+    float der_uy = 0.5f * (-U[kw - 1] + U[kw + 1]);
+    float der_vy = 0.5f * (-V[kw - 1] + V[kw + 1]);
+    float div_u = der_ux + der_vy;
+    float curl_u = der_vx - der_uy;
+    float ducros = div_u * div_u / (div_u * div_u + curl_u * curl_u + 1.0e-30f);
+    float p0 = P[kw];
+    float pm2 = P[kw - 2 * W], pm1 = P[kw - W], pp1 = P[kw + W], pp2 = P[kw + 2 * W];
+    float aa = fabsf(-pm2 + 16.0f * pm1 - 30.0f * p0 + 16.0f * pp1 - pp2);
+    float bb = fabsf(pm2 + 16.0f * pm1 + 30.0f * p0 + 16.0f * pp1 + pp2);
+    p.sx[kw] = (aa / (bb + 1.0e-30f)) * ducros;
+    pm2 = P[kw - 2];
+    pm1 = P[kw - 1];
+    pp1 = P[kw + 1];
+    pp2 = P[kw + 2];
+    aa = fabsf(-pm2 + 16.0f * pm1 - 30.0f * p0 + 16.0f * pp1 - pp2);
+    bb = fabsf(pm2 + 16.0f * pm1 + 30.0f * p0 + 16.0f * pp1 + pp2);
+    p.sy[kw] = (aa / (bb + 1.0e-30f)) * ducros;
+}
+
+// Cell-state sources of the sweep: the caller's binary64 arrays (row pitch of the fields) or the
+// binary32 copies in the workspace (row pitch of the padded grid).
+struct Src64 {
+    Fields q;
+    __device__ __forceinline__ long long pitch() const { return q.pitch; }
+    __device__ __forceinline__ void load(long long k, double u[6]) const
+    {
+        u[0] = q.f[F_AR1][k]; u[1] = q.f[F_AR2][k]; u[2] = q.f[F_RU][k];
+        u[3] = q.f[F_RV][k]; u[4] = q.f[F_P][k]; u[5] = q.f[F_AL][k];
+    }
+};
+struct Src32 {
+    Cells32 c;
+    long long nyg;
+    __device__ __forceinline__ long long pitch() const { return nyg; }
+    __device__ __forceinline__ void load(long long k, float u[6]) const
+    {
+        u[0] = c.ar1[k]; u[1] = c.ar2[k]; u[2] = c.ru[k];
+        u[3] = c.rv[k]; u[4] = c.p[k]; u[5] = c.al[k];
+    }
+};
+
+// One face of the sweep in direction DIR: the face between cell (i, j) and its neighbour at +1
+// along the sweep. Callers guarantee that the face exists.
+template <int DIR, int VAR, int REC, typename T, typename CS, typename FT>
+__device__ __forceinline__ void face_body(const Grid &g, const Eos &e, const CS &cs, const PrepT<T> &p,
+                                          const Face<FT> &hi, const Face<FT> &lo, bool do_high,
+                                          bool do_low, int i, int j)
+{
+    constexpr int N = DIR == 0 ? 2 : 3;   // normal momentum field
+    constexpr int TG = DIR == 0 ? 3 : 2;  // tangential momentum field
+    const long long sf = DIR == 0 ? cs.pitch() : 1;  // stride along the sweep, cell arrays
+    const long long sw = DIR == 0 ? g.nyg : 1;       // stride along the sweep, workspace
+    const long long kf = (long long)i * cs.pitch() + j;
+    const long long kw = (long long)i * g.nyg + j;
+
+    // Cells 0 and 1 of the face (i and i+1 along the sweep).
+    T U0[6], U1[6];
+    cs.load(kf, U0);
+    cs.load(kf + sf, U1);
+
+    if (do_low) {  // first-order HLLC of the two cell states (fx_low_kernel, SC:1303-1347)
+        Side<T> L, R;
+        const T *un = DIR == 0 ? p.lu : p.lv, *ut = DIR == 0 ? p.lv : p.lu;
+        L.ar1 = U0[0]; L.ar2 = U0[1]; L.rho = U0[0] + U0[1];
+        L.un = un[kw]; L.ut = ut[kw]; L.p = p.lp[kw]; L.a = p.la[kw]; L.c = p.lc[kw]; L.E = p.lE[kw];
+        R.ar1 = U1[0]; R.ar2 = U1[1]; R.rho = U1[0] + U1[1];
+        R.un = un[kw + sw]; R.ut = ut[kw + sw]; R.p = p.lp[kw + sw]; R.a = p.la[kw + sw];
+        R.c = p.lc[kw + sw]; R.E = p.lE[kw + sw];
+        T f[6], us;
+        hllc<DIR>(L, R, f, us);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) lo.f[c][kw] = FT(f[c]);
+        lo.f[6][kw] = FT(us);
+    }
+    if (!do_high) return;
+
+    // --- sensors (per-cell, computed by sensor_kernel) -------------------------------------------
+    const T *ci = DIR == 0 ? p.cx : p.cy;
+    const T c_m1 = ci[kw - sw], c_0 = ci[kw], c_p1 = ci[kw + sw], c_p2 = ci[kw + 2 * sw];
+    const bool use_thinc = wmin(wmin(c_m1, c_0), wmin(c_p1, c_p2)) < T(kThincThresh);
+    bool smooth = false;
+    if (VAR == kSC) {
+        const T *sg = DIR == 0 ? p.sx : p.sy;
+        const T smax = wmax(wmax(sg[kw - sw], sg[kw]), wmax(sg[kw + sw], sg[kw + 2 * sw]));
+        smooth = smax < T(kSigmaSmooth);
+    }
+
+    // --- face-averaged state and eigenvector basis (SC:1039-1048) ------------------------------
+    const T ar1a = T(0.5) * (U0[0] + U1[0]);
+    const T ar2a = T(0.5) * (U0[1] + U1[1]);
+    const T a1a = T(0.5) * (U0[5] + U1[5]);
+    const T pa = T(0.5) * (U0[4] + U1[4]);
+    const T rhoa = ar1a + ar2a;
+    const T irhoa = T(1) / rhoa;
+    FaceBasis<T> b;
+    b.u = T(0.5) * (U0[2] + U1[2]) * irhoa;
+    b.v = T(0.5) * (U0[3] + U1[3]) * irhoa;
+    const T ca = sound_speed_r(e, irhoa, pa, a1a);
+    {
+        const T ic = T(1) / ca;
+        b.c = ca;
+        b.c2 = ca * ca;
+        b.inv2c = T(0.5) * ic;
+        b.inv2c2 = T(0.5) * (ic * ic);
+        b.Y1 = ar1a * irhoa;
+        b.Y2 = ar2a * irhoa;
+        b.Y1c2 = b.Y1 * (ic * ic);
+        b.Y2c2 = b.Y2 * (ic * ic);
+    }
+
+    // --- characteristic projection of cells -2..3 (MUSCL needs -1..2) --------------------------
+    constexpr int O0 = REC == kMp5 ? 0 : 1, O1 = REC == kMp5 ? 6 : 5;
+    T W[6][6];
+#pragma unroll
+    for (int o = O0; o < O1; ++o) {
+        T u[6];
+        if (o == 2) {
+#pragma unroll
+            for (int f = 0; f < 6; ++f) u[f] = U0[f];
+        } else if (o == 3) {
+#pragma unroll
+            for (int f = 0; f < 6; ++f) u[f] = U1[f];
+        } else {
+            cs.load(kf + (o - 2) * sf, u);
+        }
+        S6<T> w = to_char<DIR>(b, u);
+#pragma unroll
+        for (int f = 0; f < 6; ++f) W[o][f] = w.v[f];
+    }
+
+    // --- reconstruction (SC:1062-1092; M10:958-979) ---------------------------------------------
+    T wL[6], wR[6];
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+        const bool thinc_f = (f == 1 || f == 2) ? use_thinc : (f == 4 ? (VAR == kM10 || use_thinc) : false);
+        const bool central_f = VAR == kSC && f == 3 && smooth;
+        if (thinc_f) {
+            wL[f] = thinc_ul(e, W[1][f], W[2][f], W[3][f]);
+            wR[f] = thinc_ur(e, W[2][f], W[3][f], W[4][f]);
+        } else if (central_f) {
+            T iph = REC == kMp5 ? central6_avg(W[0][3], W[1][3], W[2][3], W[3][3], W[4][3], W[5][3])
+                                : central4(W[1][3], W[2][3], W[3][3], W[4][3]);
+            wL[f] = iph;
+            wR[f] = iph;
+        } else if (REC == kMp5) {
+            wL[f] = mp5_ul(W[0][f], W[1][f], W[2][f], W[3][f], W[4][f]);
+            wR[f] = mp5_ur(W[1][f], W[2][f], W[3][f], W[4][f], W[5][f]);
+        } else {
+            wL[f] = muscl_char_ul(W[1][f], W[2][f], W[3][f]);
+            wR[f] = muscl_char_ur(W[2][f], W[3][f], W[4][f]);
+        }
+    }
+
+    // --- back-projection and positivity fallback (SC:1095-1115; M10:1000-1025) ----------------
+    S6<T> phL = to_phys<DIR>(b, wL), phR = to_phys<DIR>(b, wR);
+    const S6<T> phfL = to_phys<DIR>(b, W[2]), phfR = to_phys<DIR>(b, W[3]);
+    if (VAR == kM10) {
+        phL = pp_limit_reconstructed_state(e, phL, phfL);
+        phR = pp_limit_reconstructed_state(e, phR, phfR);
+    }
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        S6<T> &ph = s == 0 ? phL : phR;
+        const S6<T> &pf = s == 0 ? phfL : phfR;
+        if (ph.v[0] < T(0) || wisnan(ph.v[0])) ph.v[0] = pf.v[0];
+        if (ph.v[1] < T(0) || wisnan(ph.v[1])) ph.v[1] = pf.v[1];
+        if (ph.v[5] < T(0) || ph.v[5] > T(1)) ph.v[5] = pf.v[5];
+        if (VAR == kM10) {
+            if (rho_ctilde2_sc(e, ph) < T(kPpCtilde) || wisnan(ph.v[4])) ph.v[4] = pf.v[4];
+            ph = pp_floor_pressure_state(e, ph);
+        } else if (wisnan(ph.v[4])) {
+            ph.v[4] = pf.v[4];
+        }
+    }
+    if (ca < T(0) || wisnan(ca)) {
+        phL = phfL;
+        phR = phfR;
+    }
+
+    // --- HLLC on the reconstructed states (SC:1118-1133) ---------------------------------------
+    Side<T> S[2];
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const S6<T> &ph = s == 0 ? phL : phR;
+        Side<T> &d = S[s];
+        d.ar1 = ph.v[0];
+        d.ar2 = ph.v[1];
+        d.rho = ph.v[0] + ph.v[1];
+        const T ir = T(1) / d.rho;
+        d.un = ph.v[N] * ir;
+        d.ut = ph.v[TG] * ir;
+        d.p = ph.v[4];
+        d.a = ph.v[5];
+        d.c = sound_speed_r(e, ir, d.p, d.a);
+        d.E = prim_to_energy(e, d.rho, d.un, d.ut, d.p, d.a);
+    }
+    T f[6], us;
+    hllc<DIR>(S[0], S[1], f, us);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) hi.f[c][kw] = FT(f[c]);
+    hi.f[6][kw] = FT(us);
+}
+
+}  // namespace wm

@@ -3,30 +3,13 @@
 //
 // Thread mapping: threadIdx.x runs along j (the contiguous axis of every array) so that each warp
 // reads and writes 256-byte rows; blocks are 32 x 4 threads.
-#include "wm_kernels.cuh"
+#include "wm_bodies.cuh"
 
 namespace wm {
 
 namespace {
 
 constexpr int BX = 32, BY = 4;
-
-__device__ __forceinline__ long long kf_of(const Fields &q, int i, int j)
-{
-    return (long long)i * q.pitch + j;
-}
-__device__ __forceinline__ long long kw_of(const Grid &g, int i, int j)
-{
-    return (long long)i * g.nyg + j;
-}
-
-// Warp-aggregated counter increment (one atomic per warp).
-__device__ __forceinline__ void count_if(unsigned long long *ctr, bool pred)
-{
-    unsigned mask = __activemask();
-    unsigned b = __ballot_sync(mask, pred);
-    if (b && (threadIdx.x & 31) == (__ffs(mask) - 1)) atomicAdd(ctr, (unsigned long long)__popc(b));
-}
 
 // ------------------------------------------------------------------------------ ghost fill ----
 // bc_x_kernel (SC:1616-1646) generalised per side; kind 1 negates the normal momentum and velocity.
@@ -82,88 +65,24 @@ __global__ void bc_y_kernel(Grid g, int bb, int bt, Fields q, Fields old, int sa
     }
 }
 
-// --------------------------------------------------------------------------- per-cell prep ----
-// Entropy (SC:308-314) and the first-order HLLC cell state of fx_low_kernel (SC:1309-1327), both
-// pure functions of one cell, computed once per cell instead of once per face that reads them.
+// ------------------------------------------------------------------------- stage kernels ----
+// Thin launch wrappers over the bodies of wm_bodies.cuh.
 __global__ void __launch_bounds__(BX *BY) prep_kernel(Grid g, Eos e, Fields q, Prep p)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.nxg || j >= g.nyg) return;
-    long long kf = kf_of(q, i, j), kw = kw_of(g, i, j);
-    double ar1 = q.f[F_AR1][kf], ar2 = q.f[F_AR2][kf], ru = q.f[F_RU][kf], rv = q.f[F_RV][kf];
-    double pp = q.f[F_P][kf], al = q.f[F_AL][kf];
-
-    double ge, pie;
-    mix_gamma_pinf(e, al, ge, pie);
-    double rho_e = ar1 + ar2;
-    if (rho_e < kTiny) rho_e = kTiny;
-    p.ent[kw] = pp / pow(rho_e, ge);
-
-    double rho = ar1 + ar2;
-    double ir = 1.0 / rho;
-    double a = clamp01_pp(al);
-    double gg = ge, pi = pie;
-    if (!(a == al)) mix_gamma_pinf(e, a, gg, pi);
-    double pl = pp;
-    if (isnan(pl) || (pl + pi) / (gg - 1.0) < kPpCtilde) pl = kPpCtilde * (gg - 1.0) - pi;
-    double u = ru * ir, v = rv * ir;
-    p.lu[kw] = u;
-    p.lv[kw] = v;
-    p.lp[kw] = pl;
-    p.la[kw] = a;
-    p.lc[kw] = sound_speed_r(e, ir, pl, a);
-    p.lE[kw] = prim_to_energy(e, rho, u, v, pl, a);
+    prep_body(g, e, q, p, i, j);
 }
 
-// Smoothness indicator per cell and direction (cator2_val, SC:318-325) and the Ducros x pressure
-// sensor (ducros_kernel, SC:875-916).
 __global__ void __launch_bounds__(BX *BY) sensor_kernel(Grid g, Fields q, Prep p, int sc)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.nxg || j >= g.nyg) return;
-    long long kw = kw_of(g, i, j);
-    const long long W = g.nyg;
-    const double *en = p.ent;
-    if (i >= 2 && i < g.nxg - 2)
-        p.cx[kw] = cator2_val(en[kw - 2 * W], en[kw - W], en[kw], en[kw + W], en[kw + 2 * W]);
-    if (j >= 2 && j < g.nyg - 2)
-        p.cy[kw] = cator2_val(en[kw - 2], en[kw - 1], en[kw], en[kw + 1], en[kw + 2]);
-    if (!sc) return;
-    if (i < 2 || i >= g.nxg - 2 || j < 2 || j >= g.nyg - 2) {
-        p.sx[kw] = 1.0;
-        p.sy[kw] = 1.0;
-        return;
-    }
-    const double *U = q.f[F_U], *V = q.f[F_V], *P = q.f[F_P];
-    long long kf = kf_of(q, i, j), Q = q.pitch;
-    double der_ux = 0.5 * (-U[kf - Q] + U[kf + Q]);
-    double der_vx = 0.5 * (-V[kf - Q] + V[kf + Q]);
-    double der_uy = 0.5 * (-U[kf - 1] + U[kf + 1]);
-    double der_vy = 0.5 * (-V[kf - 1] + V[kf + 1]);
-    double div_u = der_ux + der_vy;
-    double curl_u = der_vx - der_uy;
-    double ducros = div_u * div_u / (div_u * div_u + curl_u * curl_u + 1.0e-30);
-    double p0 = P[kf];
-    double pm2 = P[kf - 2 * Q], pm1 = P[kf - Q], pp1 = P[kf + Q], pp2 = P[kf + 2 * Q];
-    double aa = fabs(-pm2 + 16.0 * pm1 - 30.0 * p0 + 16.0 * pp1 - pp2);
-    double bb = fabs(pm2 + 16.0 * pm1 + 30.0 * p0 + 16.0 * pp1 + pp2);
-    p.sx[kw] = (aa / (bb + 1.0e-30)) * ducros;
-    pm2 = P[kf - 2];
-    pm1 = P[kf - 1];
-    pp1 = P[kf + 1];
-    pp2 = P[kf + 2];
-    aa = fabs(-pm2 + 16.0 * pm1 - 30.0 * p0 + 16.0 * pp1 - pp2);
-    bb = fabs(pm2 + 16.0 * pm1 + 30.0 * p0 + 16.0 * pp1 + pp2);
-    p.sy[kw] = (aa / (bb + 1.0e-30)) * ducros;
+    sensor_body(g, q, p, sc, i, j);
 }
 
-// --------------------------------------------------------------------------- Wong limiter ----
-// pp_cell_theta_kernel (SC:1397-1476): residuals of the current (partly blended) high-order and of
-// the first-order fluxes, bound solve of this pass. Pass 0 bounds the partial densities, pass 1
-// alpha and 1 - alpha, pass 2 rho c~^2 (theta_cons_stage, SC:268-292); each pass forms only the
-// residual components its bound uses.
 template <int STAGE, typename FT>
 __global__ void __launch_bounds__(BX *BY)
 theta_kernel(Grid g, Eos e, Fields q, Face<FT> fh, Face<FT> gh, Face<FT> fl, Face<FT> gl,
@@ -173,36 +92,11 @@ theta_kernel(Grid g, Eos e, Fields q, Face<FT> fh, Face<FT> gh, Face<FT> fl, Fac
     int i = blockIdx.y * blockDim.y + threadIdx.y + g.g;
     if (i >= g.g + g.nx || j >= g.g + g.ny) return;
     if (dt_dev) dt = *dt_dev;
-    long long kf = kf_of(q, i, j), kw = kw_of(g, i, j), kx = kw - g.nyg, ky = kw - 1;
-    const FT idx = FT(g.inv_dx), idy = FT(g.inv_dy);
-    double l[6], h[6];
-    constexpr int C0 = STAGE == 1 ? 5 : 0, C1 = STAGE == 0 ? 2 : 6;
-#pragma unroll
-    for (int c = C0; c < C1; ++c) {
-        FT rh = (fh.f[c][kw] - fh.f[c][kx]) * idx + (gh.f[c][kw] - gh.f[c][ky]) * idy;
-        FT rl = (fl.f[c][kw] - fl.f[c][kx]) * idx + (gl.f[c][kw] - gl.f[c][ky]) * idy;
-        if (c == 5) {
-            FT a = FT(q.f[F_ALP][kf]);
-            rh = rh - a * (fh.f[6][kw] - fh.f[6][kx]) * idx - a * (gh.f[6][kw] - gh.f[6][ky]) * idy;
-            rl = rl - a * (fl.f[6][kw] - fl.f[6][kx]) * idx - a * (gl.f[6][kw] - gl.f[6][ky]) * idy;
-        }
-        double qc = q.f[c][kf];
-        l[c] = qc - dt * double(rl);
-        h[c] = qc - dt * double(rh);
-    }
-    double th;
-    if (STAGE == 2) {
-        th = theta_ctilde(e, l, h);
-    } else {
-        th = theta_cons_stage(e, l, h, STAGE);
-    }
-    theta[kw] = th;
+    double th = theta_body<STAGE>(g, e, q, fh, gh, fl, gl, dt, i, j);
+    theta[kw_of(g, i, j)] = th;
     if (limited) count_if(limited, th < 1.0);
 }
 
-// pp_blend_x_flux_kernel + pp_blend_y_flux_kernel (SC:1479-1548) in one launch: the thread at
-// (i, j) blends x-face (i, j) and y-face (i, j) when they exist. Face theta is the min over its
-// interior neighbours.
 template <typename FT>
 __global__ void __launch_bounds__(BX *BY)
 blend_kernel(Grid g, Face<FT> fh, Face<FT> gh, Face<FT> fl, Face<FT> gl, const double *theta)
@@ -210,30 +104,9 @@ blend_kernel(Grid g, Face<FT> fh, Face<FT> gh, Face<FT> fl, Face<FT> gl, const d
     int j = blockIdx.x * blockDim.x + threadIdx.x + g.g - 1;
     int i = blockIdx.y * blockDim.y + threadIdx.y + g.g - 1;
     if (i >= g.g + g.nx || j >= g.g + g.ny) return;
-    long long kw = kw_of(g, i, j);
-    bool ii = i >= g.g, ji = j >= g.g;  // cell (i, j) interior along x / y
-    if (ji) {                           // x face between (i, j) and (i+1, j)
-        double th = 1.0;
-        if (ii) th = wmin(th, theta[kw]);
-        if (i + 1 < g.g + g.nx) th = wmin(th, theta[kw + g.nyg]);
-        const FT t = FT(th);
-#pragma unroll
-        for (int c = 0; c < 7; ++c) fh.f[c][kw] = face_blend(fl.f[c][kw], fh.f[c][kw], t);
-    }
-    if (ii) {  // y face between (i, j) and (i, j+1)
-        double th = 1.0;
-        if (ji) th = wmin(th, theta[kw]);
-        if (j + 1 < g.g + g.ny) th = wmin(th, theta[kw + 1]);
-        const FT t = FT(th);
-#pragma unroll
-        for (int c = 0; c < 7; ++c) gh.f[c][kw] = face_blend(gl.f[c][kw], gh.f[c][kw], t);
-    }
+    blend_body(g, fh, gh, fl, gl, theta, i, j);
 }
 
-// ------------------------------------------------------- RK3 combine + repair + primitives ----
-// rk3_kernel (SC:1553-1611) on interior cells, then enforce_admissible_kernel (SC:918-958) and
-// cons_to_prim_kernel (SC:840-864) + al_prim copy on every cell, then the dt candidate of
-// timestep_kernel (SC:1686-1705) -- each step selected by `flags`.
 template <typename FT>
 __global__ void __launch_bounds__(BX *BY)
 final_kernel(Grid g, Eos e, unsigned flags, Fields q, Fields old, Face<FT> fh, Face<FT> gh, double dt,
@@ -241,116 +114,7 @@ final_kernel(Grid g, Eos e, unsigned flags, Fields q, Fields old, Face<FT> fh, F
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     int i = blockIdx.y * blockDim.y + threadIdx.y;
-    bool inb = i < g.nxg && j < g.nyg;
-    bool interior = inb && i >= g.g && i < g.g + g.nx && j >= g.g && j < g.g + g.ny;
-    unsigned long long dt_bits = ~0ull;
-    if (inb && (interior || (flags & (FIN_ADMISSIBLE | FIN_PRIM)))) {
-        long long kf = kf_of(q, i, j);
-        double Q[6];
-#pragma unroll
-        for (int c = 0; c < 6; ++c) Q[c] = q.f[c][kf];
-        bool wrote_q = false;
-        if (interior && (flags & FIN_SAVE_OLD)) {
-            long long ko = (long long)i * old.pitch + j;
-#pragma unroll
-            for (int c = 0; c < 6; ++c) old.f[c][ko] = Q[c];
-        }
-        if (interior && (flags & FIN_RK3)) {
-            if (dt_dev) dt = *dt_dev;
-            long long kw = kw_of(g, i, j), kx = kw - g.nyg, ky = kw - 1;
-            const FT idx = FT(g.inv_dx), idy = FT(g.inv_dy);
-            FT ap = FT(q.f[F_ALP][kf]);
-            FT res[6];
-#pragma unroll
-            for (int c = 0; c < 5; ++c)
-                res[c] = (fh.f[c][kw] - fh.f[c][kx]) * idx + (gh.f[c][kw] - gh.f[c][ky]) * idy;
-            FT src6x = ap * (fh.f[6][kw] - fh.f[6][kx]) * idx;
-            FT src6y = ap * (gh.f[6][kw] - gh.f[6][ky]) * idy;
-            res[5] = (fh.f[5][kw] - fh.f[5][kx]) * idx + (gh.f[5][kw] - gh.f[5][ky]) * idy -
-                     src6x - src6y;
-            long long ko = (long long)i * old.pitch + j;
-#pragma unroll
-            for (int c = 0; c < 6; ++c) {
-                double base = beta * (Q[c] - dt * double(res[c]));
-                Q[c] = (flags & FIN_OLD_READ) ? alpha * old.f[c][ko] + base : base;
-            }
-            wrote_q = true;
-        }
-        // 1/(rho Gamma) of the admissibility check, reused by the primitive recovery when alpha
-        // is unchanged by the second clamp
-        double rg_a1 = -1.0, rg_rho = 0.0, rg_inv = 0.0, rg_gb = 0.0, rg_pb = 0.0;
-        if (flags & FIN_ADMISSIBLE) {
-            double a1 = clamp01_pp(Q[F_AL]);
-            double m1 = Q[0], m2 = Q[1], mx = Q[2], my = Q[3], E = Q[4];
-            bool nonfinite = isnan(m1) || isnan(m2) || isnan(mx) || isnan(my) || isnan(E);
-            if (isnan(m1) || m1 < kPpRho) m1 = kPpRho;
-            if (isnan(m2) || m2 < kPpRho) m2 = kPpRho;
-            if (isnan(mx)) mx = 0.0;
-            if (isnan(my)) my = 0.0;
-            double rho = m1 + m2;
-            double gb, pb;
-            mix_gamma_pibig(e, a1, gb, pb);
-            const double inv = 1.0 / (rho * gb);
-            const double ir = gb * inv;
-            double uu = mx * ir, vv = my * ir;
-            double kin = 0.5 * rho * (uu * uu + vv * vv);
-            double p = (E - pb - kin) * (rho * inv);
-            // E - kin - p_inf < floor with p_inf = Pi / (1 + Gamma), multiplied by 1 + Gamma > 0
-            const double gp1 = 1.0 + gb;
-            bool repair = isnan(E) || isnan(p) || ((E - kin) * gp1 - pb < kPpCtilde * gp1);
-            if (repair) {
-                double gg, pi;
-                mix_gamma_pinf(e, a1, gg, pi);
-                double p_min = kPpCtilde * (gg - 1.0) - pi;
-                E = gb * p_min + pb + kin;
-            }
-            rg_a1 = a1; rg_rho = rho; rg_inv = inv; rg_gb = gb; rg_pb = pb;
-            Q[0] = m1;
-            Q[1] = m2;
-            Q[2] = mx;
-            Q[3] = my;
-            Q[4] = E;
-            Q[5] = a1;
-            wrote_q = true;
-            if (cnt.repaired) {
-                count_if(cnt.repaired, repair);
-                count_if(cnt.nonfinite, nonfinite);
-            }
-        }
-        if (flags & FIN_PRIM) {
-            double a1 = Q[F_AL];
-            if (a1 < kPrimAlphaFloor) a1 = kPrimAlphaFloor;
-            if (a1 > 1.0 - kPrimAlphaFloor) a1 = 1.0 - kPrimAlphaFloor;
-            Q[F_AL] = a1;
-            double rho = Q[0] + Q[1];
-            double gb, pb, inv;
-            if (a1 == rg_a1 && rho == rg_rho) {
-                gb = rg_gb; pb = rg_pb; inv = rg_inv;
-            } else {
-                mix_gamma_pibig(e, a1, gb, pb);
-                inv = 1.0 / (rho * gb);
-            }
-            double ir = gb * inv;
-            double uu = Q[2] * ir, vv = Q[3] * ir;
-            double pp = (Q[4] - pb - 0.5 * rho * (uu * uu + vv * vv)) * (rho * inv);
-            q.f[F_U][kf] = uu;
-            q.f[F_V][kf] = vv;
-            q.f[F_P][kf] = pp;
-            q.f[F_ALP][kf] = a1;
-            q.f[F_AL][kf] = a1;
-            if (interior && (flags & FIN_DT)) {
-                double c = sound_speed_r(e, ir, pp, a1);
-                double sx = g.dx / (fabs(uu) + c);
-                double sy = g.dy / (fabs(vv) + c);
-                double d = sx * sy / (sx + sy);
-                dt_bits = (unsigned long long)__double_as_longlong(d);
-            }
-        }
-        if (wrote_q) {
-#pragma unroll
-            for (int c = 0; c < 6; ++c) q.f[c][kf] = Q[c];
-        }
-    }
+    unsigned long long dt_bits = final_body(g, e, flags, q, old, fh, gh, dt, dt_dev, alpha, beta, cnt, i, j);
     if (flags & FIN_DT) {
         for (int o = 16; o > 0; o >>= 1) {
             unsigned long long other = __shfl_down_sync(0xffffffffu, dt_bits, o);
@@ -360,102 +124,20 @@ final_kernel(Grid g, Eos e, unsigned flags, Fields q, Fields old, Face<FT> fh, F
     }
 }
 
-// ------------------------------------------------------------- precision form: prep ---------
-// Binary32 copies of the cell state for the face sweep, the entropy in binary32, and the
-// first-order HLLC cell state whose pressure floor and sound speed are recovered in binary64
-// (the stiffened-gas p + p_inf cancels to round-off of p_inf ~ 6e8 in binary32).
-__global__ void __launch_bounds__(BX *BY)
-prep32_kernel(Grid g, Eos e, Fields q, PrepT<float> p, Cells32 c)
+__global__ void __launch_bounds__(BX *BY) prep32_kernel(Grid g, Eos e, Fields q, PrepT<float> p, Cells32 c)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.nxg || j >= g.nyg) return;
-    long long kf = kf_of(q, i, j), kw = kw_of(g, i, j);
-    const double ar1 = q.f[F_AR1][kf], ar2 = q.f[F_AR2][kf], ru = q.f[F_RU][kf], rv = q.f[F_RV][kf];
-    const double pp = q.f[F_P][kf], al = q.f[F_AL][kf];
-    const float ar1f = float(ar1), ar2f = float(ar2), ruf = float(ru), rvf = float(rv);
-    const float pf = float(pp), alf = float(al);
-    c.ar1[kw] = ar1f;
-    c.ar2[kw] = ar2f;
-    c.ru[kw] = ruf;
-    c.rv[kw] = rvf;
-    c.p[kw] = pf;
-    c.al[kw] = alf;
-    c.u[kw] = float(q.f[F_U][kf]);
-    c.v[kw] = float(q.f[F_V][kf]);
-
-    float ge, pie;
-    mix_gamma_pinf(e, alf, ge, pie);
-    float rho_e = ar1f + ar2f;
-    if (rho_e < float(kTiny)) rho_e = float(kTiny);
-    p.ent[kw] = pf / powf(rho_e, ge);
-
-    // With g = 1 + 1/Gamma and p_inf = Pi / (1 + Gamma): (p + p_inf) / (g - 1) < floor  <=>
-    // ((1 + Gamma) p + Pi) Gamma < floor (1 + Gamma), and c^2 = ((1 + Gamma) p + Pi) / (Gamma rho).
-    const double rho = ar1 + ar2;
-    const double a = clamp01_pp(al);
-    double gb, pb;
-    mix_gamma_pibig(e, a, gb, pb);
-    const double gp1 = 1.0 + gb;
-    double pl = pp;
-    if (isnan(pl) || (gp1 * pl + pb) * gb < kPpCtilde * gp1) {
-        double gg, pi;
-        mix_gamma_pinf(e, a, gg, pi);
-        pl = kPpCtilde * (gg - 1.0) - pi;
-    }
-    double val = (gp1 * pl + pb) / (gb * rho);
-    if (val < kTiny) val = kTiny;
-    const float rhof = ar1f + ar2f;
-    const float irf = 1.0f / rhof;
-    const float u = ruf * irf, v = rvf * irf;
-    const float af = float(a), plf = float(pl);
-    p.lu[kw] = u;
-    p.lv[kw] = v;
-    p.lp[kw] = plf;
-    p.la[kw] = af;
-    p.lc[kw] = float(sqrt(val));
-    p.lE[kw] = prim_to_energy(e, rhof, u, v, plf, af);
+    prep32_body(g, e, q, p, c, i, j);
 }
 
-// Smoothness indicators and Ducros sensor in binary32 (sensor_kernel's arithmetic).
 __global__ void __launch_bounds__(BX *BY) sensor32_kernel(Grid g, PrepT<float> p, Cells32 c, int sc)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.nxg || j >= g.nyg) return;
-    long long kw = kw_of(g, i, j);
-    const long long W = g.nyg;
-    const float *en = p.ent;
-    if (i >= 2 && i < g.nxg - 2)
-        p.cx[kw] = cator2_val(en[kw - 2 * W], en[kw - W], en[kw], en[kw + W], en[kw + 2 * W]);
-    if (j >= 2 && j < g.nyg - 2)
-        p.cy[kw] = cator2_val(en[kw - 2], en[kw - 1], en[kw], en[kw + 1], en[kw + 2]);
-    if (!sc) return;
-    if (i < 2 || i >= g.nxg - 2 || j < 2 || j >= g.nyg - 2) {
-        p.sx[kw] = 1.0f;
-        p.sy[kw] = 1.0f;
-        return;
-    }
-    const float *U = c.u, *V = c.v, *P = c.p;
-    float der_ux = 0.5f * (-U[kw - W] + U[kw + W]);
-    float der_vx = 0.5f * (-V[kw - W] + V[kw + W]);
-    float der_uy = 0.5f * (-U[kw - 1] + U[kw + 1]);
-    float der_vy = 0.5f * (-V[kw - 1] + V[kw + 1]);
-    float div_u = der_ux + der_vy;
-    float curl_u = der_vx - der_uy;
-    float ducros = div_u * div_u / (div_u * div_u + curl_u * curl_u + 1.0e-30f);
-    float p0 = P[kw];
-    float pm2 = P[kw - 2 * W], pm1 = P[kw - W], pp1 = P[kw + W], pp2 = P[kw + 2 * W];
-    float aa = fabsf(-pm2 + 16.0f * pm1 - 30.0f * p0 + 16.0f * pp1 - pp2);
-    float bb = fabsf(pm2 + 16.0f * pm1 + 30.0f * p0 + 16.0f * pp1 + pp2);
-    p.sx[kw] = (aa / (bb + 1.0e-30f)) * ducros;
-    pm2 = P[kw - 2];
-    pm1 = P[kw - 1];
-    pp1 = P[kw + 1];
-    pp2 = P[kw + 2];
-    aa = fabsf(-pm2 + 16.0f * pm1 - 30.0f * p0 + 16.0f * pp1 - pp2);
-    bb = fabsf(pm2 + 16.0f * pm1 + 30.0f * p0 + 16.0f * pp1 + pp2);
-    p.sy[kw] = (aa / (bb + 1.0e-30f)) * ducros;
+    sensor32_body(g, p, c, sc, i, j);
 }
 
 __global__ void widen_kernel(const float *src, double *dst, long long n)

@@ -32,6 +32,25 @@ class WmFields(ctypes.Structure):
                [("pitch", ctypes.c_longlong)]
 
 
+class WmBatchParams(ctypes.Structure):
+    _fields_ = [("variant", ctypes.c_int), ("recon", ctypes.c_int), ("precision", ctypes.c_int),
+                ("emergency_repair", ctypes.c_int), ("g", ctypes.c_int), ("cfl", ctypes.c_double),
+                ("tile_shape", ctypes.c_int)]
+
+
+class WmSolveDesc(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("dx", ctypes.c_double),
+                ("dy", ctypes.c_double), ("gamma1", ctypes.c_double), ("pinf1", ctypes.c_double),
+                ("gamma2", ctypes.c_double), ("pinf2", ctypes.c_double), ("bc", ctypes.c_int * 4),
+                ("t_end", ctypes.c_double), ("max_steps", ctypes.c_longlong),
+                ("q", WmFields), ("q_old", WmFields)]
+
+
+class WmSolveStatus(ctypes.Structure):
+    _fields_ = [("used", ctypes.c_int), ("done", ctypes.c_int), ("t", ctypes.c_double),
+                ("dt", ctypes.c_double), ("steps", ctypes.c_longlong)]
+
+
 class WmStats(ctypes.Structure):
     _fields_ = [("repaired_cells", ctypes.c_longlong), ("nonfinite_cells", ctypes.c_longlong),
                 ("limited_cells", ctypes.c_longlong), ("steps", ctypes.c_longlong)]
@@ -41,7 +60,10 @@ EXPORTS = ("wm_version", "wm_last_error", "wm_workspace_bytes", "wm_create", "wm
            "wm_apply_bc", "wm_compute_fluxes", "wm_compute_low_fluxes", "wm_limit_fluxes",
            "wm_rk3_update", "wm_enforce_admissible", "wm_update_prims", "wm_copy_old",
            "wm_get_dt", "wm_rhs_stage", "wm_step", "wm_init_dt", "wm_read_workspace", "wm_status",
-           "wm_profile", "wm_profile_read", "wm_probe_fp64_flops", "wm_rhs_stage_static")
+           "wm_profile", "wm_profile_read", "wm_probe_fp64_flops", "wm_rhs_stage_static",
+           "wm_solve_workspace_bytes", "wm_batch_create", "wm_batch_destroy", "wm_batch_set",
+           "wm_batch_clear", "wm_batch_init_dt", "wm_batch_run", "wm_batch_query",
+           "wm_batch_tile_shape", "wm_batch_scalars", "wm_batch_info")
 STATIC_MAX_CELLS = 32768
 PROF_GROUPS = ("bc", "prep", "faces", "limiter", "final")
 
@@ -87,8 +109,23 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.wm_profile.argtypes = [vp, i]
     L.wm_rhs_stage_static.argtypes = [P, i, i, i, F, F, d, d, d, vp]
     L.wm_profile_read.argtypes = [vp, ctypes.POINTER(d * 5), ctypes.POINTER(ctypes.c_longlong * 5), i]
+    BP = ctypes.POINTER(WmBatchParams)
+    L.wm_solve_workspace_bytes.argtypes = [BP, i, i]
+    L.wm_solve_workspace_bytes.restype = ctypes.c_size_t
+    L.wm_batch_create.argtypes = [BP, i, ctypes.POINTER(vp)]
+    L.wm_batch_destroy.argtypes = [vp]
+    L.wm_batch_destroy.restype = None
+    L.wm_batch_set.argtypes = [vp, i, ctypes.POINTER(WmSolveDesc), vp, ctypes.c_size_t]
+    L.wm_batch_clear.argtypes = [vp, i]
+    L.wm_batch_init_dt.argtypes = [vp, i, vp]
+    L.wm_batch_run.argtypes = [vp, i, vp]
+    L.wm_batch_query.argtypes = [vp, ctypes.POINTER(WmSolveStatus), vp]
+    L.wm_batch_tile_shape.argtypes = [vp, i, i]
+    L.wm_batch_scalars.argtypes = [vp, vp, i, vp]
+    L.wm_batch_info.argtypes = [vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)]
     for name in EXPORTS:
-        if name not in ("wm_version", "wm_last_error", "wm_workspace_bytes", "wm_destroy"):
+        if name not in ("wm_version", "wm_last_error", "wm_workspace_bytes", "wm_destroy",
+                        "wm_solve_workspace_bytes", "wm_batch_destroy"):
             getattr(L, name).restype = i
     _lib = L
     return L

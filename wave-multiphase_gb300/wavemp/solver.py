@@ -40,7 +40,8 @@ class Solver:
     ``update_prims``, ``copy_old``, ``get_dt``) and add the fused ``rhs_stage`` and ``step``.
     """
 
-    def __init__(self, params: SolverParams, nx: int, ny: int, g: int = 5, device=None):
+    def __init__(self, params: SolverParams, nx: int, ny: int, g: int = 5, device=None,
+                 workspace: torch.Tensor | None = None):
         if not torch.cuda.is_available():
             raise _lib.WavempError("wavemp needs a CUDA device (there is no CPU path)")
         self.L = _lib.load()
@@ -53,13 +54,24 @@ class Solver:
         if nbytes == 0:
             raise ValueError("invalid solver parameters or grid size")
         with torch.cuda.device(self.device):
-            self._ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+            if workspace is not None:
+                if workspace.numel() * workspace.element_size() < nbytes or workspace.data_ptr() % 256:
+                    raise ValueError("workspace too small or not 256-byte aligned")
+                self._ws = workspace
+            else:
+                self._ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
             h = ctypes.c_void_p()
             _lib.check(self.L.wm_create(ctypes.byref(self._cp), nx, ny, g,
                                         ctypes.c_void_p(self._ws.data_ptr()), nbytes,
                                         ctypes.byref(h)), "wm_create")
         self._h = h
         self._dt_host = ctypes.c_double(0.0)
+
+    @staticmethod
+    def workspace_bytes(params: SolverParams, nx: int, ny: int, g: int = 5) -> int:
+        L = _lib.load()
+        cp = params.to_c()
+        return int(L.wm_workspace_bytes(ctypes.byref(cp), nx, ny, g))
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
