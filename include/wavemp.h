@@ -144,6 +144,42 @@ int wm_step(wm_handle *h, const wm_fields *q, const wm_fields *q_old, double dt,
  * with dt <= 0. */
 int wm_init_dt(wm_handle *h, const wm_fields *q, void *stream);
 
+/* Limiter form of the fused stage (wm_rhs_stage, wm_step, wm_run). Default (in_place = 1): the
+ * reference's in-place blend sweeps (pp_blend_x/y_flux_kernel, SC:1479-1548) between the passes.
+ * in_place = 0: no blend sweeps -- each limiter pass and the combine rebuild the blended face fluxes
+ * in registers from the high- and first-order fluxes and the passes' cell factors, bit-identical
+ * (it moves less memory but costs binary64 operations, so it pays where the kernels' occupancy is
+ * fixed anyway, as in the batched form, which always uses it). After a fused stage the workspace's
+ * high-order arrays hold the limited fluxes in place form, the unlimited ones otherwise; the
+ * closures always blend in place. */
+int wm_set_limiter_sweeps(wm_handle *h, int in_place);
+
+/* ---- the time loop on the device -------------------------------------------------------------
+ * wm_run runs the reference's time loop (SC:2009-2073) for one solve: per step, clamp dt to every
+ * save time not yet written and to t_end (SC:2021-2026), one SSP-RK3 step, t += dt, step += 1,
+ * dt = the CFL dt of the new state, and a save time ts counts as reached when |t - ts| < dt/2
+ * (SC:2066-2073). The steps run inside one CUDA graph (a conditional while node: the step kernels
+ * plus two single-thread kernels for the clamps and the loop test) until a save time is reached
+ * (sched->hit = its index; the caller writes its output and calls again), t >= t_end - 1e-14
+ * (sched->finished), or max_steps steps; one host wait per call. Before the first call set t,
+ * t_end, step, the save times and saved[k] = (t >= save_times[k] - 1e-14) (SC:2013). The first
+ * call allocates a small device block for the loop state. Not for a stream in capture. */
+#define WM_MAX_SAVES 32
+typedef struct wm_schedule {
+    double t, t_end;
+    long long step;
+    int nsaves;
+    int hit;       /* out: first save index reached by the call's last step, or -1 */
+    int finished;  /* out: the loop condition t < t_end - 1e-14 failed */
+    double dt;     /* out: the CFL dt of the current state */
+    double save_times[WM_MAX_SAVES];
+    int saved[WM_MAX_SAVES];
+} wm_schedule;
+int wm_run(wm_handle *h, const wm_fields *q, const wm_fields *q_old, wm_schedule *sched, long long max_steps,
+           void *stream);
+/* 1 when wm_run's last call ran as a graph (0: the same kernels, one host wait per step). */
+int wm_run_uses_graph(wm_handle *h);
+
 /* ---- batched form: many independent solves, one persistent launch per call -------------------
  * A batch holds up to `capacity` solves in slots. Each solve has its own grid size, cell sizes,
  * equation of state, boundary rules, end time and step budget, and its own cell arrays and
@@ -194,6 +230,24 @@ int wm_batch_tile_shape(wm_batch *b, int size_class, int shape);
  * or from (write=1) host memory -- snapshot and restore for measuring runs. */
 int wm_batch_scalars(wm_batch *b, void *host, int write, void *stream);
 int wm_batch_info(wm_batch *b, int *ntiles, int *grid, int *graph);
+/* Phase timing of later runs (enable=1) or none (0). WM_BATCH_PHASES device-time sums in ms (the
+ * phases of a stage: ghost fill x, ghost fill y, preparation, sensors, face sweeps, the three
+ * limiter passes, combine; then the end-of-step dt phase), summed over stages and steps. */
+#define WM_BATCH_PHASES 10
+int wm_batch_profile(wm_batch *b, int enable);
+int wm_batch_profile_read(wm_batch *b, double *ms, int reset, void *stream);
+
+/* ---- post-processing ------------------------------------------------------------------------ */
+/* Schlieren field of the reference's figure (save_png SC:1728-1771, without a plotting library):
+ * grad[i*ny + j] = |grad(ar1 + ar2)| over the interior by numpy.gradient's rule on the cell
+ * centres (bit-identical to it). xh / yh: the nx-1 / ny-1 device spacings of the interior
+ * coordinates, or NULL when every spacing equals x_h0 / y_h0 (numpy's uniform branch).
+ * rho_scratch: nx*ny doubles. rgb (optional, ny x 2nx x 3 bytes): the schlieren panel (blue ramp
+ * over [1, 2400], alpha1 = 0.5 level in red) beside alpha1 in inverted grey. Needs 2 <= nx <= 65535,
+ * ny >= 2. */
+int wm_schlieren(const wm_fields *q, int nx, int ny, int g, const double *xh, const double *yh,
+                 double x_h0, double y_h0, double *rho_scratch, double *grad, unsigned char *rgb,
+                 void *stream);
 
 /* ---- diagnostics ---------------------------------------------------------------------------- */
 /* Copy workspace array `which` (WM_WS_*) of the padded grid into the caller's device buffer dst

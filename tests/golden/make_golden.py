@@ -615,6 +615,62 @@ def run_units(ref_dir, out_dir):
     print(f"units -> {path} ({os.path.getsize(path) // 1024} KB)")
 
 
+class _Arrays:
+    def __init__(self, nx, ny):
+        self.a = {k: np.zeros((nx + 2 * G, ny + 2 * G)) for k in FIELDS + PRIMS}
+
+
+def run_checkpoint(ref_dir, out_dir):
+    """The reference's output and restart functions -- ``save_npz`` (SC:1714-1726),
+    ``load_restart_host`` (SC:1779-1821) and ``infer_restart_step`` (SC:1773-1776) -- on a small
+    perturbed droplet state with the script's own water EOS (6.12, 3.43e8), plus a restart file
+    whose alpha1 leaves [0, 1] (the loader clips it to [1e-8, 1 - 1e-8])."""
+    import tempfile
+
+    mod = load_reference(os.path.join(ref_dir, "sainath_SC_it_works.py"))
+    nx, ny = 24, 12
+    mod.NX, mod.NY, mod.NXG, mod.NYG = nx, ny, nx + 2 * G, ny + 2 * G
+    x, y, dx, dy = centres(nx, ny, 0.0, 1.0, 0.0, 0.5)
+    st = _Arrays(nx, ny)
+    g1, p1, g2, p2 = 6.12, 3.43e8, 1.4, 0.0
+    droplet_ic(st, x, y, dx, g1, p1, g2, p2, 2.4)
+    perturb(st, np.random.default_rng(5), g1, p1, g2, p2)
+    a = st.a
+    out = {f"in_{k}": a[k] for k in FIELDS + PRIMS}
+    out.update(in_x=x, in_y=y, in_step=np.int64(137), in_time=np.float64(1.25e-5))
+    rng = np.random.default_rng(6)
+    cwd = os.getcwd()
+    with tempfile.TemporaryDirectory() as d:
+        os.chdir(d)
+        try:
+            mod.save_npz(a["ar1"], a["ar2"], a["u_p"], a["v_p"], a["p_p"], a["al"], x, y, 137, 1.25e-5)
+            name = "mp5_000137.npz"
+            with np.load(name) as f:
+                for k in f.files:
+                    out["saved_" + k] = f[k]
+            res = mod.load_restart_host(os.path.join(d, name), x, y)
+            out["restart_step"] = np.int64(mod.infer_restart_step(os.path.join(d, name)))
+            edge = {k: out["saved_" + k].copy() for k in ("ar1", "ar2", "u", "v", "p", "alpha1")}
+            edge["alpha1"] = rng.uniform(-0.2, 1.2, size=(nx, ny))
+            edge["alpha1"][0, :4] = [0.0, 1.0, 1e-9, 1.0 - 1e-9]
+            np.savez(os.path.join(d, "edge.npz"), **edge)  # no time key: restart time 0
+            res_edge = mod.load_restart_host(os.path.join(d, "edge.npz"), x, y)
+        finally:
+            os.chdir(cwd)
+    names = ("ar1", "ar2", "ru", "rv", "E", "al", "u_p", "v_p", "p_p")
+    for k, v in zip(names, res[:9]):
+        out["restart_" + k] = v
+    out["restart_time"] = np.float64(res[9])
+    for k, v in edge.items():
+        out["edge_in_" + k] = v
+    for k, v in zip(names, res_edge[:9]):
+        out["edge_restart_" + k] = v
+    out["edge_restart_time"] = np.float64(res_edge[9])
+    path = os.path.join(out_dir, "checkpoint.npz")
+    np.savez_compressed(path, **out)
+    print(f"checkpoint -> {path} ({os.path.getsize(path) // 1024} KB)")
+
+
 ALL_CASES = ("sc_ref_ic", "m10_ref_ic", "sc_cfg0", "sc_mp5c6_cfg0", "sc_mp5c6_rand",
              "m10_cfg2", "m10_mp5c6_rand", "sc_mp5c6_triple", "sc_mp5c6_stress")
 
@@ -625,10 +681,12 @@ def main():
     ap.add_argument("--out-dir", default=HERE)
     ap.add_argument("--only", nargs="*", default=None)
     args = ap.parse_args()
-    todo = args.only if args.only else list(ALL_CASES) + ["units"]
+    todo = args.only if args.only else list(ALL_CASES) + ["units", "checkpoint"]
     for name in todo:
         if name == "units":
             run_units(args.ref_dir, args.out_dir)
+        elif name == "checkpoint":
+            run_checkpoint(args.ref_dir, args.out_dir)
         else:
             run_case(name, args.ref_dir, args.out_dir)
 

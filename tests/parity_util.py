@@ -9,7 +9,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 CASES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-               if not p.endswith("units.npz"))
+               if not p.endswith(("units.npz", "checkpoint.npz")))
 FIELDS = ("ar1", "ar2", "ru", "rv", "E", "al")
 PRIMS = ("u_p", "v_p", "p_p")
 ALL = FIELDS + PRIMS + ("al_prim",)

@@ -6,7 +6,7 @@
 // rules, time limit and step budget, its caller-owned cell arrays and workspace) or is empty.
 // wm_batch_run launches batch_kernel once: every block walks the batch's tile list through the
 // phases of a stage (ghost fill x, ghost fill y, preparation, sensors, face sweeps, three limiter
-// bound/blend pairs, combine), separated by grid-wide barriers, three stages per step, then a
+// passes whose blends are rebuilt in registers, combine), separated by grid-wide barriers, three stages per step, then a
 // per-solve time-step phase (dt from the solve's own CFL reduction, clamped to its end time), for
 // up to `nsteps` steps. Solves that reach their end time or step budget drop out of later steps.
 //
@@ -37,6 +37,7 @@ constexpr int kShapes = 4;
 constexpr int kShapeTI[kShapes] = {1, 2, 4, 8};  // tile rows (x) x columns (y) = 128 cells
 constexpr int kShapeTJ[kShapes] = {128, 64, 32, 16};
 constexpr unsigned long long kSpinLimit = 1ull << 26;
+constexpr int kPhaseSlots = 10;  // the 9 phases of a stage, then the end-of-step phase
 
 struct SolveDev {
     Grid g;
@@ -71,7 +72,15 @@ struct BatchDev {
     unsigned *bar_count, *bar_gen;
     int *err;
     int repair;
+    unsigned long long *prof;  // per-phase nanoseconds (block 0's view), or null
 };
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 __device__ bool grid_barrier(const BatchDev &B)
 {
@@ -155,10 +164,9 @@ __device__ __forceinline__ void bcy_cell(const SolveDev &S, bool save, int i, in
     }
 }
 
-enum Phase {
-    PH_BCX, PH_BCY, PH_PREP, PH_SENSOR, PH_FACES, PH_THETA0, PH_BLEND0, PH_THETA1, PH_BLEND1,
-    PH_THETA2, PH_BLEND2, PH_FINAL
-};
+// The limiter's blends are rebuilt in registers by the next pass and by the combine (CellFaces),
+// so a stage has no blend phases.
+enum Phase { PH_BCX, PH_BCY, PH_PREP, PH_SENSOR, PH_FACES, PH_THETA0, PH_THETA1, PH_THETA2, PH_FINAL };
 
 template <int VAR, int REC, int FP32>
 __device__ __forceinline__ void run_phase(const BatchDev &B, int phase, int stage)
@@ -217,28 +225,17 @@ __device__ __forceinline__ void run_phase(const BatchDev &B, int phase, int stag
         case PH_THETA2:
             if (interior) {
                 double th;
-                const int p = phase == PH_THETA0 ? 0 : (phase == PH_THETA1 ? 1 : 2);
+                const int p = phase - PH_THETA0;
                 if (FP32) {
-                    th = p == 0 ? theta_body<0>(g, S.e, S.q, S.fh32, S.gh32, S.fl32, S.gl32, dt, i, j)
-                       : p == 1 ? theta_body<1>(g, S.e, S.q, S.fh32, S.gh32, S.fl32, S.gl32, dt, i, j)
-                                : theta_body<2>(g, S.e, S.q, S.fh32, S.gh32, S.fl32, S.gl32, dt, i, j);
+                    th = p == 0 ? theta_body<0, float, 0>(g, S.e, S.q, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta, i, j)
+                       : p == 1 ? theta_body<1, float, 1>(g, S.e, S.q, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta, i, j)
+                                : theta_body<2, float, 2>(g, S.e, S.q, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta, i, j);
                 } else {
-                    th = p == 0 ? theta_body<0>(g, S.e, S.q, S.fh, S.gh, S.fl, S.gl, dt, i, j)
-                       : p == 1 ? theta_body<1>(g, S.e, S.q, S.fh, S.gh, S.fl, S.gl, dt, i, j)
-                                : theta_body<2>(g, S.e, S.q, S.fh, S.gh, S.fl, S.gl, dt, i, j);
+                    th = p == 0 ? theta_body<0, double, 0>(g, S.e, S.q, S.fh, S.gh, S.fl, S.gl, dt, S.theta, i, j)
+                       : p == 1 ? theta_body<1, double, 1>(g, S.e, S.q, S.fh, S.gh, S.fl, S.gl, dt, S.theta, i, j)
+                                : theta_body<2, double, 2>(g, S.e, S.q, S.fh, S.gh, S.fl, S.gl, dt, S.theta, i, j);
                 }
                 S.theta[p][kw_of(g, i, j)] = th;
-            }
-            break;
-        case PH_BLEND0:
-        case PH_BLEND1:
-        case PH_BLEND2:
-            if (i >= g.g - 1 && i < g.g + g.nx && j >= g.g - 1 && j < g.g + g.ny) {
-                const int p = phase == PH_BLEND0 ? 0 : (phase == PH_BLEND1 ? 1 : 2);
-                if (FP32)
-                    blend_body(g, S.fh32, S.gh32, S.fl32, S.gl32, S.theta[p], i, j);
-                else
-                    blend_body(g, S.fh, S.gh, S.fl, S.gl, S.theta[p], i, j);
             }
             break;
         case PH_FINAL: {
@@ -250,9 +247,11 @@ __device__ __forceinline__ void run_phase(const BatchDev &B, int phase, int stag
             const Counters none = {nullptr, nullptr, nullptr, nullptr};
             unsigned long long bits;
             if (FP32)
-                bits = final_body(g, S.e, flags, S.q, S.old, S.fh32, S.gh32, dt, nullptr, alpha, beta, none, i, j);
+                bits = final_body<float, 3>(g, S.e, flags, S.q, S.old, S.fh32, S.gh32, S.fl32, S.gl32, S.theta,
+                                            dt, nullptr, alpha, beta, none, i, j);
             else
-                bits = final_body(g, S.e, flags, S.q, S.old, S.fh, S.gh, dt, nullptr, alpha, beta, none, i, j);
+                bits = final_body<double, 3>(g, S.e, flags, S.q, S.old, S.fh, S.gh, S.fl, S.gl, S.theta, dt,
+                                             nullptr, alpha, beta, none, i, j);
             if (stage == 2) {  // every lane of the warp takes part (tiles are warp multiples)
                 for (int o = 16; o > 0; o >>= 1) {
                     unsigned long long other = __shfl_down_sync(0xffffffffu, bits, o);
@@ -269,11 +268,20 @@ __device__ __forceinline__ void run_phase(const BatchDev &B, int phase, int stag
 template <int VAR, int REC, int FP32>
 __global__ void __launch_bounds__(kThreads) batch_kernel(BatchDev B, int nsteps)
 {
+    // Phase timing: a phase ends when the grid barrier after it opens, so block 0's clock between
+    // successive barrier exits is the phase's duration across the whole grid.
+    const bool timing = B.prof != nullptr && blockIdx.x == 0 && threadIdx.x == 0;
+    unsigned long long last = timing ? global_ns() : 0;
     for (int step = 0; step < nsteps; ++step) {
         for (int stage = 0; stage < 3; ++stage) {
             for (int ph = PH_BCX; ph <= PH_FINAL; ++ph) {
                 run_phase<VAR, REC, FP32>(B, ph, stage);
                 if (!grid_barrier(B)) return;
+                if (timing) {
+                    const unsigned long long now = global_ns();
+                    B.prof[ph] += now - last;
+                    last = now;
+                }
             }
         }
         // End of the step: the next dt of every unfinished solve from its own CFL reduction
@@ -301,6 +309,11 @@ __global__ void __launch_bounds__(kThreads) batch_kernel(BatchDev B, int nsteps)
             }
         }
         if (!grid_barrier(B)) return;
+        if (timing) {
+            const unsigned long long now = global_ns();
+            B.prof[kPhaseSlots - 1] += now - last;
+            last = now;
+        }
     }
 }
 
@@ -369,6 +382,8 @@ struct wm_batch {
     bool graph_ok = true;
     unsigned *bar_count = nullptr, *bar_gen = nullptr;
     int *err = nullptr;
+    unsigned long long *prof = nullptr;  // kPhaseSlots counters in d_small's tail
+    bool prof_on = false;
 };
 
 namespace {
@@ -449,6 +464,7 @@ int launch(wm_batch *b, int nsteps, cudaStream_t s)
     B.bar_gen = b->bar_gen;
     B.err = b->err;
     B.repair = b->P.emergency_repair;
+    B.prof = b->prof_on ? b->prof : nullptr;
     void *args[] = {&B, &nsteps};
     int grid = std::max(1, std::min(b->grid, b->ntiles));
     cudaError_t e = cudaLaunchCooperativeKernel((const void *)b->fn, dim3(grid), dim3(kThreads), args, 0, s);
@@ -503,6 +519,7 @@ int wm_batch_create(const wm_batch_params *p, int capacity, wm_batch **out)
     b->bar_count = reinterpret_cast<unsigned *>(tail);
     b->bar_gen = reinterpret_cast<unsigned *>(tail + 4);
     b->err = reinterpret_cast<int *>(tail + 8);
+    b->prof = reinterpret_cast<unsigned long long *>(tail + 64);  // kPhaseSlots x 8 bytes, within the 256
     for (int s = 0; s < capacity; ++s) {
         slot_scalars(b, s, b->host[s]);
         b->host[s].done = nullptr;  // empty slot: no done flag, skipped by the kernel's step end
@@ -749,6 +766,35 @@ int wm_batch_scalars(wm_batch *b, void *host, int write, void *stream)
         set_err("wm_batch_scalars", e);
         return WM_ERR_CUDA;
     }
+    return WM_OK;
+}
+
+int wm_batch_profile(wm_batch *b, int enable)
+{
+    if (!b) return WM_ERR_INVALID;
+    if (b->prof_on != (enable != 0)) {  // the counters' address is a kernel argument: re-capture
+        b->prof_on = enable != 0;
+        if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
+        if (b->graph) cudaGraphDestroy(b->graph);
+        b->graph_exec = nullptr;
+        b->graph = nullptr;
+    }
+    return WM_OK;
+}
+
+int wm_batch_profile_read(wm_batch *b, double *ms, int reset, void *stream)
+{
+    if (!b || !ms) return WM_ERR_INVALID;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    unsigned long long raw[kPhaseSlots];
+    cudaError_t e = cudaMemcpyAsync(raw, b->prof, sizeof raw, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && reset) e = cudaMemsetAsync(b->prof, 0, sizeof raw, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        set_err("wm_batch_profile_read", e);
+        return WM_ERR_CUDA;
+    }
+    for (int k = 0; k < kPhaseSlots; ++k) ms[k] = 1e-6 * (double)raw[k];
     return WM_OK;
 }
 

@@ -93,27 +93,84 @@ __device__ __forceinline__ void sensor_body(const Grid &g, const Fields &q, cons
     p.sy[kw] = (aa / (bb + 1.0e-30)) * ducros;
 }
 
+// Face limiter factors of pass p (pp_blend_x/y_flux_kernel, SC:1479-1548): the x face between
+// cells (i, j) and (i+1, j) takes min(1, theta(i, j), theta(i+1, j)) over its interior neighbours,
+// in that order; the y face between (i, j) and (i, j+1) likewise. Shared by blend_body, which
+// writes the blended fluxes, and CellFaces, which rebuilds them in registers.
+__device__ __forceinline__ double face_theta_x(const Grid &g, const double *theta, long long kw, int i)
+{
+    double th = 1.0;
+    if (i >= g.g) th = wmin(th, theta[kw]);
+    if (i + 1 < g.g + g.nx) th = wmin(th, theta[kw + g.nyg]);
+    return th;
+}
+__device__ __forceinline__ double face_theta_y(const Grid &g, const double *theta, long long kw, int j)
+{
+    double th = 1.0;
+    if (j >= g.g) th = wmin(th, theta[kw]);
+    if (j + 1 < g.g + g.ny) th = wmin(th, theta[kw + 1]);
+    return th;
+}
+
+// The four faces of interior cell (i, j) with NP limiter passes deferred: the flux a face holds
+// after passes 0..NP-1 is rebuilt from its high- and first-order values and the passes' cell
+// factors by the same face_blend chain blend_body applies in place, so the values are identical
+// bit for bit -- and the three blend sweeps over 28 face arrays are not needed. NP = 0 reads the
+// (already blended, or not yet limited) high-order arrays as they are.
+template <typename FT, int NP>
+struct CellFaces {
+    long long kw, kx, ky;
+    FT txp[NP > 0 ? NP : 1], txm[NP > 0 ? NP : 1], typ[NP > 0 ? NP : 1], tym[NP > 0 ? NP : 1];
+
+    __device__ __forceinline__ CellFaces(const Grid &g, double *const theta[3], int i, int j)
+    {
+        kw = kw_of(g, i, j);
+        kx = kw - g.nyg;
+        ky = kw - 1;
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            txp[p] = FT(face_theta_x(g, theta[p], kw, i));
+            txm[p] = FT(face_theta_x(g, theta[p], kx, i - 1));
+            typ[p] = FT(face_theta_y(g, theta[p], kw, j));
+            tym[p] = FT(face_theta_y(g, theta[p], ky, j - 1));
+        }
+    }
+    __device__ __forceinline__ FT chain(const FT *hi, const FT *lo, long long k, const FT *t) const
+    {
+        FT v = hi[k];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) v = face_blend(lo[k], v, t[p]);
+        return v;
+    }
+    __device__ __forceinline__ FT xp(const Face<FT> &h, const Face<FT> &l, int c) const { return chain(h.f[c], l.f[c], kw, txp); }
+    __device__ __forceinline__ FT xm(const Face<FT> &h, const Face<FT> &l, int c) const { return chain(h.f[c], l.f[c], kx, txm); }
+    __device__ __forceinline__ FT yp(const Face<FT> &h, const Face<FT> &l, int c) const { return chain(h.f[c], l.f[c], kw, typ); }
+    __device__ __forceinline__ FT ym(const Face<FT> &h, const Face<FT> &l, int c) const { return chain(h.f[c], l.f[c], ky, tym); }
+};
+
 // pp_cell_theta_kernel (SC:1397-1476): residuals of the current (partly blended) high-order and of
 // the first-order fluxes, bound solve of this pass. Pass 0 bounds the partial densities, pass 1
 // alpha and 1 - alpha, pass 2 rho c~^2 (theta_cons_stage, SC:268-292); each pass forms only the
-// residual components its bound uses.
-template <int STAGE, typename FT>
+// residual components its bound uses. NP: limiter passes whose blends are deferred (0 when the
+// high-order arrays already hold the blended fluxes, STAGE when they are rebuilt in registers).
+template <int STAGE, typename FT, int NP = 0>
 __device__ __forceinline__ double theta_body(const Grid &g, const Eos &e, const Fields &q,
                                              const Face<FT> &fh, const Face<FT> &gh,
                                              const Face<FT> &fl, const Face<FT> &gl, double dt,
-                                             int i, int j)
+                                             double *const theta[3], int i, int j)
 {
-    long long kf = kf_of(q, i, j), kw = kw_of(g, i, j), kx = kw - g.nyg, ky = kw - 1;
+    const CellFaces<FT, NP> cf(g, theta, i, j);
+    const long long kf = kf_of(q, i, j), kw = cf.kw, kx = cf.kx, ky = cf.ky;
     const FT idx = FT(g.inv_dx), idy = FT(g.inv_dy);
     double l[6], h[6];
     constexpr int C0 = STAGE == 1 ? 5 : 0, C1 = STAGE == 0 ? 2 : 6;
 #pragma unroll
     for (int c = C0; c < C1; ++c) {
-        FT rh = (fh.f[c][kw] - fh.f[c][kx]) * idx + (gh.f[c][kw] - gh.f[c][ky]) * idy;
+        FT rh = (cf.xp(fh, fl, c) - cf.xm(fh, fl, c)) * idx + (cf.yp(gh, gl, c) - cf.ym(gh, gl, c)) * idy;
         FT rl = (fl.f[c][kw] - fl.f[c][kx]) * idx + (gl.f[c][kw] - gl.f[c][ky]) * idy;
         if (c == 5) {
             FT a = FT(q.f[F_ALP][kf]);
-            rh = rh - a * (fh.f[6][kw] - fh.f[6][kx]) * idx - a * (gh.f[6][kw] - gh.f[6][ky]) * idy;
+            rh = rh - a * (cf.xp(fh, fl, 6) - cf.xm(fh, fl, 6)) * idx - a * (cf.yp(gh, gl, 6) - cf.ym(gh, gl, 6)) * idy;
             rl = rl - a * (fl.f[6][kw] - fl.f[6][kx]) * idx - a * (gl.f[6][kw] - gl.f[6][ky]) * idy;
         }
         double qc = q.f[c][kf];
@@ -130,28 +187,20 @@ __device__ __forceinline__ double theta_body(const Grid &g, const Eos &e, const 
 }
 
 // pp_blend_x_flux_kernel + pp_blend_y_flux_kernel (SC:1479-1548) in one launch: the thread at
-// (i, j) blends x-face (i, j) and y-face (i, j) when they exist. Face theta is the min over its
-// interior neighbours.
+// (i, j) blends x-face (i, j) and y-face (i, j) when they exist.
 template <typename FT>
 __device__ __forceinline__ void blend_body(const Grid &g, const Face<FT> &fh, const Face<FT> &gh,
                                            const Face<FT> &fl, const Face<FT> &gl,
                                            const double *theta, int i, int j)
 {
     long long kw = kw_of(g, i, j);
-    bool ii = i >= g.g, ji = j >= g.g;  // cell (i, j) interior along x / y
-    if (ji) {                           // x face between (i, j) and (i+1, j)
-        double th = 1.0;
-        if (ii) th = wmin(th, theta[kw]);
-        if (i + 1 < g.g + g.nx) th = wmin(th, theta[kw + g.nyg]);
-        const FT t = FT(th);
+    if (j >= g.g) {  // x face between (i, j) and (i+1, j)
+        const FT t = FT(face_theta_x(g, theta, kw, i));
 #pragma unroll
         for (int c = 0; c < 7; ++c) fh.f[c][kw] = face_blend(fl.f[c][kw], fh.f[c][kw], t);
     }
-    if (ii) {  // y face between (i, j) and (i, j+1)
-        double th = 1.0;
-        if (ji) th = wmin(th, theta[kw]);
-        if (j + 1 < g.g + g.ny) th = wmin(th, theta[kw + 1]);
-        const FT t = FT(th);
+    if (i >= g.g) {  // y face between (i, j) and (i, j+1)
+        const FT t = FT(face_theta_y(g, theta, kw, j));
 #pragma unroll
         for (int c = 0; c < 7; ++c) gh.f[c][kw] = face_blend(gl.f[c][kw], gh.f[c][kw], t);
     }
@@ -161,10 +210,14 @@ __device__ __forceinline__ void blend_body(const Grid &g, const Face<FT> &fh, co
 // cons_to_prim_kernel (SC:840-864) + al_prim copy on every cell, then the dt candidate of
 // timestep_kernel (SC:1686-1705) -- each step selected by `flags`.
 // Returns the bit pattern of the cell's time-step candidate (all ones when it has none).
-template <typename FT>
+// NP: limiter passes whose blends are deferred (3 in the fused stage: the limited fluxes are rebuilt
+// from fh/gh, fl/gl and the three theta arrays; 0 when fh/gh already hold them).
+template <typename FT, int NP = 0>
 __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eos &e, unsigned flags,
                                                          const Fields &q, const Fields &old,
                                                          const Face<FT> &fh, const Face<FT> &gh,
+                                                         const Face<FT> &fl, const Face<FT> &gl,
+                                                         double *const theta[3],
                                                          double dt, const double *dt_dev,
                                                          double alpha, double beta,
                                                          const Counters &cnt, int i, int j)
@@ -185,16 +238,16 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
         }
         if (interior && (flags & FIN_RK3)) {
             if (dt_dev) dt = *dt_dev;
-            long long kw = kw_of(g, i, j), kx = kw - g.nyg, ky = kw - 1;
+            const CellFaces<FT, NP> cf(g, theta, i, j);
             const FT idx = FT(g.inv_dx), idy = FT(g.inv_dy);
             FT ap = FT(q.f[F_ALP][kf]);
             FT res[6];
 #pragma unroll
             for (int c = 0; c < 5; ++c)
-                res[c] = (fh.f[c][kw] - fh.f[c][kx]) * idx + (gh.f[c][kw] - gh.f[c][ky]) * idy;
-            FT src6x = ap * (fh.f[6][kw] - fh.f[6][kx]) * idx;
-            FT src6y = ap * (gh.f[6][kw] - gh.f[6][ky]) * idy;
-            res[5] = (fh.f[5][kw] - fh.f[5][kx]) * idx + (gh.f[5][kw] - gh.f[5][ky]) * idy -
+                res[c] = (cf.xp(fh, fl, c) - cf.xm(fh, fl, c)) * idx + (cf.yp(gh, gl, c) - cf.ym(gh, gl, c)) * idy;
+            FT src6x = ap * (cf.xp(fh, fl, 6) - cf.xm(fh, fl, 6)) * idx;
+            FT src6y = ap * (cf.yp(gh, gl, 6) - cf.ym(gh, gl, 6)) * idy;
+            res[5] = (cf.xp(fh, fl, 5) - cf.xm(fh, fl, 5)) * idx + (cf.yp(gh, gl, 5) - cf.ym(gh, gl, 5)) * idy -
                      src6x - src6y;
             long long ko = (long long)i * old.pitch + j;
 #pragma unroll

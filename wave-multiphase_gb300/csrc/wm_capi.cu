@@ -1,6 +1,7 @@
 // wm_capi.cu -- the C ABI of include/wavemp.h: handle, workspace layout and the launch sequences
 // of the reference's closures (SC:1894-1995) and of the fused stage / step.
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -73,6 +74,13 @@ namespace wm {
 void set_error_text(const char *msg) { snprintf(g_last_error, sizeof g_last_error, "%s", msg); }
 }  // namespace wm
 
+// Device-resident state of wm_run's loop: the caller's schedule plus the loop's own counters.
+struct RunClock {
+    wm_schedule s;
+    long long iter, max_iter;
+    double dt_use;  // the dt of the step in flight (after the save-time and end-time clamps)
+};
+
 struct wm_handle {
     wm_params P;
     Grid g;
@@ -95,6 +103,13 @@ struct wm_handle {
     bool dt_valid = false;
     long long steps = 0;
     bool fluxes_ready = false, low_ready = false;
+    bool defer_limiter = false;  // fused stage: limiter blends rebuilt in registers (wm_set_limiter_sweeps)
+    // device-side time loop (wm_run): clock block, graph with a conditional while node
+    struct RunClock *clock = nullptr;
+    cudaGraph_t run_graph = nullptr;
+    cudaGraphExec_t run_exec = nullptr;
+    bool run_graph_ok = true;
+    Fields run_F{}, run_O{};
     // kernel-group profiler (wm_profile)
     bool prof = false;
     struct Rec {
@@ -304,6 +319,9 @@ void wm_destroy(wm_handle *h)
         cudaEventDestroy(r.b);
     }
     for (auto e : h->pool) cudaEventDestroy(e);
+    if (h->run_exec) cudaGraphExecDestroy(h->run_exec);
+    if (h->run_graph) cudaGraphDestroy(h->run_graph);
+    if (h->clock) cudaFree(h->clock);
     if (h->own_ws && h->ws) cudaFree(h->ws);
     delete h;
 }
@@ -394,10 +412,10 @@ int wm_limit_fluxes(wm_handle *h, const wm_fields *q, double dt, void *stream)
     if (!h->fluxes_ready || !h->low_ready) return WM_ERR_STATE;
     if (h->fp32)
         launch_limiter(h->g, h->e, to_fields(q), h->fh32, h->gh32, h->fl32, h->gl32, h->theta, dt,
-                       nullptr, h->cnt, as_stream(stream));
+                       nullptr, h->cnt, false, as_stream(stream));
     else
         launch_limiter(h->g, h->e, to_fields(q), h->fh, h->gh, h->fl, h->gl, h->theta, dt, nullptr,
-                       h->cnt, as_stream(stream));
+                       h->cnt, false, as_stream(stream));
     return check_launch("wm_limit_fluxes");
 }
 
@@ -410,11 +428,11 @@ int wm_rk3_update(wm_handle *h, const wm_fields *q, const wm_fields *q_old, doub
     Fields F = to_fields(q), O = q_old ? to_fields(q_old) : F;
     const unsigned fl = FIN_RK3 | (alpha != 0.0 ? FIN_OLD_READ : 0u);
     if (h->fp32)
-        launch_final(h->g, h->e, fl, F, O, h->fh32, h->gh32, dt, nullptr, alpha, beta, h->cnt,
-                     as_stream(stream));
+        launch_final(h->g, h->e, fl, F, O, h->fh32, h->gh32, h->fl32, h->gl32, h->theta, false, dt,
+                     nullptr, alpha, beta, h->cnt, as_stream(stream));
     else
-        launch_final(h->g, h->e, fl, F, O, h->fh, h->gh, dt, nullptr, alpha, beta, h->cnt,
-                     as_stream(stream));
+        launch_final(h->g, h->e, fl, F, O, h->fh, h->gh, h->fl, h->gl, h->theta, false, dt, nullptr,
+                     alpha, beta, h->cnt, as_stream(stream));
     return check_launch("wm_rk3_update");
 }
 
@@ -423,8 +441,8 @@ int wm_enforce_admissible(wm_handle *h, const wm_fields *q, void *stream)
     if (!h || !fields_ok(h, q)) return WM_ERR_INVALID;
     if (!h->P.emergency_repair) return WM_OK;
     Fields F = to_fields(q);
-    launch_final(h->g, h->e, FIN_ADMISSIBLE, F, F, h->fh, h->gh, 0.0, nullptr, 0.0, 1.0, h->cnt,
-                 as_stream(stream));
+    launch_final(h->g, h->e, FIN_ADMISSIBLE, F, F, h->fh, h->gh, h->fl, h->gl, h->theta, false, 0.0,
+                 nullptr, 0.0, 1.0, h->cnt, as_stream(stream));
     return check_launch("wm_enforce_admissible");
 }
 
@@ -432,8 +450,8 @@ int wm_update_prims(wm_handle *h, const wm_fields *q, void *stream)
 {
     if (!h || !fields_ok(h, q)) return WM_ERR_INVALID;
     Fields F = to_fields(q);
-    launch_final(h->g, h->e, FIN_PRIM, F, F, h->fh, h->gh, 0.0, nullptr, 0.0, 1.0, h->cnt,
-                 as_stream(stream));
+    launch_final(h->g, h->e, FIN_PRIM, F, F, h->fh, h->gh, h->fl, h->gl, h->theta, false, 0.0, nullptr,
+                 0.0, 1.0, h->cnt, as_stream(stream));
     return check_launch("wm_update_prims");
 }
 
@@ -499,9 +517,10 @@ static int run_stage(wm_handle *h, const Fields &F, const Fields &O, double dt, 
         ProfScope ps(h, WM_PROF_LIMITER, 6, s);
         if (h->fp32)
             launch_limiter(h->g, h->e, F, h->fh32, h->gh32, h->fl32, h->gl32, h->theta, dt, dt_dev,
-                           h->cnt, s);
+                           h->cnt, h->defer_limiter, s);
         else
-            launch_limiter(h->g, h->e, F, h->fh, h->gh, h->fl, h->gl, h->theta, dt, dt_dev, h->cnt, s);
+            launch_limiter(h->g, h->e, F, h->fh, h->gh, h->fl, h->gl, h->theta, dt, dt_dev, h->cnt,
+                           h->defer_limiter, s);
     }
     unsigned flags = final_flags(h, alpha);
     if (save_old) flags |= FIN_SAVE_OLD;
@@ -512,9 +531,11 @@ static int run_stage(wm_handle *h, const Fields &F, const Fields &O, double dt, 
             launch_dt_reset(h->cnt, s);
         }
         if (h->fp32)
-            launch_final(h->g, h->e, flags, F, O, h->fh32, h->gh32, dt, dt_dev, alpha, beta, h->cnt, s);
+            launch_final(h->g, h->e, flags, F, O, h->fh32, h->gh32, h->fl32, h->gl32, h->theta,
+                         h->defer_limiter, dt, dt_dev, alpha, beta, h->cnt, s);
         else
-            launch_final(h->g, h->e, flags, F, O, h->fh, h->gh, dt, dt_dev, alpha, beta, h->cnt, s);
+            launch_final(h->g, h->e, flags, F, O, h->fh, h->gh, h->fl, h->gl, h->theta, h->defer_limiter,
+                         dt, dt_dev, alpha, beta, h->cnt, s);
     }
     h->fluxes_ready = h->low_ready = true;
     return check_launch("stage");
@@ -561,6 +582,207 @@ int wm_step(wm_handle *h, const wm_fields *q, const wm_fields *q_old, double dt,
             return WM_ERR_CUDA;
         }
     }
+    return WM_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// The dt clamps at the top of the reference's loop (SC:2021-2026): to each save time not yet
+// written, then to the end time.
+__global__ void run_clamp_kernel(RunClock *c, const double *dt_cfl)
+{
+    double dt = *dt_cfl;
+    const double t = c->s.t;
+    for (int k = 0; k < c->s.nsaves; ++k)
+        if (!c->s.saved[k] && t + dt > c->s.save_times[k]) dt = c->s.save_times[k] - t;
+    if (t + dt > c->s.t_end) dt = c->s.t_end - t;
+    c->dt_use = dt;
+}
+
+// The bottom of the loop (SC:2057-2073): time and step advance, the next dt is the CFL dt just
+// reduced, a save time is reached when |t - ts| < dt/2 with that dt, the loop runs while
+// t < t_end - 1e-14. The graph's while node repeats the step until a save time is reached, the end
+// time, or the call's step limit.
+__global__ void run_advance_kernel(RunClock *c, const double *dt_cfl, cudaGraphConditionalHandle cond,
+                                   int in_graph)
+{
+    const double t = c->s.t + c->dt_use;
+    c->s.t = t;
+    c->s.step += 1;
+    c->iter += 1;
+    const double dt = *dt_cfl;
+    c->s.dt = dt;
+    int hit = -1;
+    for (int k = 0; k < c->s.nsaves; ++k) {
+        if (!c->s.saved[k] && fabs(t - c->s.save_times[k]) < 0.5 * dt) {
+            c->s.saved[k] = 1;
+            if (hit < 0) hit = k;
+        }
+    }
+    c->s.hit = hit;
+    c->s.finished = !(t < c->s.t_end - 1.0e-14);
+    const bool go = hit < 0 && !c->s.finished && c->iter < c->max_iter;
+    if (in_graph) cudaGraphSetConditional(cond, go ? 1u : 0u);
+}
+
+double *clock_dt_use(wm_handle *h)
+{
+    return reinterpret_cast<double *>(reinterpret_cast<char *>(h->clock) + offsetof(RunClock, dt_use));
+}
+
+// One loop iteration: clamp, three stages on the clamped dt, CFL reduction into dt slot 0, advance.
+int run_iteration(wm_handle *h, const Fields &F, const Fields &O, cudaGraphConditionalHandle cond,
+                  int in_graph, cudaStream_t s)
+{
+    run_clamp_kernel<<<1, 1, 0, s>>>(h->clock, h->dt_dev[0]);
+    const double *dd = clock_dt_use(h);
+    int rc = run_stage(h, F, O, 0.0, dd, 0.0, 1.0, true, false, s);
+    if (!rc) rc = run_stage(h, F, O, 0.0, dd, 0.75, 0.25, false, false, s);
+    if (!rc) rc = run_stage(h, F, O, 0.0, dd, 1.0 / 3.0, 2.0 / 3.0, false, true, s);
+    if (rc) return rc;
+    launch_dt_finalize(h->g, h->cnt, h->dt_dev[0], s);
+    run_advance_kernel<<<1, 1, 0, s>>>(h->clock, h->dt_dev[0], cond, in_graph);
+    return check_launch("wm_run step");
+}
+
+void drop_run_graph(wm_handle *h)
+{
+    if (h->run_exec) cudaGraphExecDestroy(h->run_exec);
+    if (h->run_graph) cudaGraphDestroy(h->run_graph);
+    h->run_exec = nullptr;
+    h->run_graph = nullptr;
+}
+
+// Graph: one conditional while node whose body is one loop iteration (captured into the body).
+bool build_run_graph(wm_handle *h, const Fields &F, const Fields &O)
+{
+    drop_run_graph(h);
+    cudaGraph_t g = nullptr;
+    cudaStream_t cs = nullptr;
+    bool ok = cudaGraphCreate(&g, 0) == cudaSuccess;
+    cudaGraphConditionalHandle cond = 0;
+    if (ok) ok = cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = cond;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (ok) ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) == cudaSuccess;
+    if (ok) ok = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess;
+    if (ok) {
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        ok = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+             cudaSuccess;
+        if (ok) {
+            const bool prof = h->prof;
+            h->prof = false;  // no event records inside the body
+            int rc = run_iteration(h, F, O, cond, 1, cs);
+            h->prof = prof;
+            cudaGraph_t out = nullptr;
+            ok = cudaStreamEndCapture(cs, &out) == cudaSuccess && rc == WM_OK;
+        }
+    }
+    if (ok) ok = cudaGraphInstantiate(&h->run_exec, g, 0) == cudaSuccess;
+    if (cs) cudaStreamDestroy(cs);
+    if (ok) {
+        h->run_graph = g;
+        h->run_F = F;
+        h->run_O = O;
+    } else {
+        if (h->run_exec) cudaGraphExecDestroy(h->run_exec);
+        h->run_exec = nullptr;
+        if (g) cudaGraphDestroy(g);
+    }
+    cudaGetLastError();
+    return ok;
+}
+
+bool same_fields(const Fields &a, const Fields &b) { return memcmp(&a, &b, sizeof(Fields)) == 0; }
+
+}  // namespace
+
+extern "C" {
+
+int wm_run(wm_handle *h, const wm_fields *q, const wm_fields *q_old, wm_schedule *sched, long long max_steps,
+           void *stream)
+{
+    if (!h || !fields_ok(h, q) || !fields_ok(h, q_old, false) || !sched || max_steps < 1 ||
+        sched->nsaves < 0 || sched->nsaves > WM_MAX_SAVES || std::isnan(sched->t) || std::isnan(sched->t_end))
+        return WM_ERR_INVALID;
+    sched->hit = -1;
+    if (!(sched->t < sched->t_end - 1.0e-14)) {
+        sched->finished = 1;
+        return WM_OK;
+    }
+    cudaStream_t s = as_stream(stream);
+    Fields F = to_fields(q), O = to_fields(q_old);
+    cudaError_t err = cudaSuccess;
+    if (!h->clock) {
+        err = cudaMalloc(&h->clock, sizeof(RunClock));
+        if (err != cudaSuccess) {
+            h->clock = nullptr;
+            set_error("wm_run", err);
+            return WM_ERR_NOMEM;
+        }
+    }
+    // the loop's dt lives in slot 0: get_dt before the loop (SC:2015), or the dt of the last step
+    if (!h->dt_valid) {
+        h->dt_cur = 0;
+        launch_dt_reset(h->cnt, s);
+        launch_dt_cell(h->g, h->e, F, h->cnt, s);
+        launch_dt_finalize(h->g, h->cnt, h->dt_dev[0], s);
+        h->dt_valid = true;
+    } else if (h->dt_cur != 0) {
+        err = cudaMemcpyAsync(h->dt_dev[0], h->dt_dev[1], sizeof(double), cudaMemcpyDeviceToDevice, s);
+        h->dt_cur = 0;
+    }
+    RunClock c;
+    c.s = *sched;
+    c.s.hit = -1;
+    c.s.finished = 0;
+    c.iter = 0;
+    c.max_iter = max_steps;
+    c.dt_use = 0.0;
+    if (err == cudaSuccess) err = cudaMemcpyAsync(h->clock, &c, sizeof c, cudaMemcpyHostToDevice, s);
+    if (err != cudaSuccess) {
+        set_error("wm_run", err);
+        return WM_ERR_CUDA;
+    }
+    if (h->run_graph_ok && (!h->run_exec || !same_fields(F, h->run_F) || !same_fields(O, h->run_O)))
+        h->run_graph_ok = build_run_graph(h, F, O);
+    if (h->run_exec) {
+        err = cudaGraphLaunch(h->run_exec, s);
+        if (err == cudaSuccess) err = cudaMemcpyAsync(&c, h->clock, sizeof c, cudaMemcpyDeviceToHost, s);
+        if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    } else {  // no conditional graphs: the same kernels, one host wait per step
+        for (long long n = 0; n < max_steps && err == cudaSuccess; ++n) {
+            int rc = run_iteration(h, F, O, 0, 0, s);
+            if (rc) return rc;
+            err = cudaMemcpyAsync(&c, h->clock, sizeof c, cudaMemcpyDeviceToHost, s);
+            if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+            if (c.s.hit >= 0 || c.s.finished) break;
+        }
+    }
+    if (err != cudaSuccess) {
+        set_error("wm_run", err);
+        return WM_ERR_CUDA;
+    }
+    *sched = c.s;
+    h->steps += c.iter;
+    return WM_OK;
+}
+
+int wm_run_uses_graph(wm_handle *h) { return h && h->run_exec ? 1 : 0; }
+
+int wm_set_limiter_sweeps(wm_handle *h, int in_place)
+{
+    if (!h) return WM_ERR_INVALID;
+    const bool defer = in_place == 0;
+    if (defer != h->defer_limiter) drop_run_graph(h);  // the captured loop used the other form
+    h->defer_limiter = defer;
     return WM_OK;
 }
 

@@ -41,6 +41,10 @@ struct Counters {
     unsigned long long *dt_bits;  // atomic min of the positive dt candidates (bit pattern)
 };
 
+struct Theta3 {
+    double *t[3];  // cell limiter factors of the three passes
+};
+
 // Flags of final_kernel.
 enum : unsigned {
     FIN_RK3 = 1u,         // rk3_update on interior cells
@@ -58,14 +62,17 @@ void launch_prep(const Grid &g, const Eos &e, const Fields &q, const Prep &p, in
 void launch_faces(const Grid &g, const Eos &e, int variant, int recon, const Fields &q,
                   const Prep &p, const Face7 &fh, const Face7 &gh, const Face7 &fl, const Face7 &gl,
                   bool high, bool low, cudaStream_t s);
+// The three limiter passes. deferred: no in-place blend sweeps -- each pass and the combine rebuild
+// the blended fluxes in registers (bit-identical); fh/gh keep the unlimited high-order fluxes.
 template <typename FT>
 void launch_limiter(const Grid &g, const Eos &e, const Fields &q, const Face<FT> &fh,
                     const Face<FT> &gh, const Face<FT> &fl, const Face<FT> &gl,
                     double *const theta[3], double dt, const double *dt_dev, const Counters &cnt,
-                    cudaStream_t s);
+                    bool deferred, cudaStream_t s);
 template <typename FT>
 void launch_final(const Grid &g, const Eos &e, unsigned flags, const Fields &q, const Fields &old,
-                  const Face<FT> &fh, const Face<FT> &gh, double dt, const double *dt_dev,
+                  const Face<FT> &fh, const Face<FT> &gh, const Face<FT> &fl, const Face<FT> &gl,
+                  double *const theta[3], bool deferred, double dt, const double *dt_dev,
                   double alpha, double beta, const Counters &cnt, cudaStream_t s);
 void launch_copy_old(const Grid &g, const Fields &q, const Fields &old, cudaStream_t s);
 void launch_dt_reset(const Counters &cnt, cudaStream_t s);

@@ -1,0 +1,123 @@
+// wm_post.cu -- schlieren post-processing on the device, the computation behind the reference's
+// figure (save_png, SC:1728-1771) without a plotting library.
+//
+// grad[i*ny + j] = sqrt(drho/dx^2 + drho/dy^2) over the interior, rho = ar1 + ar2, with the
+// derivatives taken by numpy.gradient's rule on the cell-centre coordinates (SC:1737-1739):
+//   * inside, for unequal spacings h1 = x[i]-x[i-1], h2 = x[i+1]-x[i]:
+//       a f[i-1] + b f[i] + c f[i+1],  a = -h2/(h1 (h1+h2)),  b = (h2-h1)/(h1 h2),  c = h1/(h2 (h1+h2));
+//     when every spacing of the axis is the same number h: (f[i+1] - f[i-1]) / (2 h);
+//   * at the two ends, first order: (f[1] - f[0]) / h and (f[n-1] - f[n-2]) / h.
+// Every product and sum is rounded separately (no fused multiply-add) and the square root is the
+// correctly rounded one, so the result equals numpy's bit for bit.
+//
+// The optional RGB image (ny rows, 2*nx columns, row r = y index j as the reference's imshow of
+// the transposed array with origin 'upper' shows it) holds two panels: |grad rho| normalised to
+// [1, 2400] through a nine-step blue ramp (ColorBrewer "Blues", the anchors of matplotlib's Blues),
+// with the alpha1 = 0.5 level marked red where alpha1 - 0.5 changes sign towards the next cell in
+// x or y; and alpha1 in inverted grey (0 white, 1 black).
+#include <cstdint>
+#include <cstdio>
+
+#include "../../include/wavemp.h"
+
+namespace wm {
+void set_error_text(const char *msg);
+}
+
+namespace {
+
+struct Axis {
+    const double *h;  // n-1 spacings of the interior coordinates
+    double h0;        // the common spacing when uniform
+    int uniform;
+    int n;
+};
+
+__device__ __forceinline__ double deriv(const double *f, long long stride, int i, const Axis &A)
+{
+    const int n = A.n;
+    if (n < 2) return 0.0;
+    if (i == 0) return __ddiv_rn(__dsub_rn(f[stride], f[0]), A.uniform ? A.h0 : A.h[0]);
+    if (i == n - 1)
+        return __ddiv_rn(__dsub_rn(f[0], f[-stride]), A.uniform ? A.h0 : A.h[n - 2]);
+    if (A.uniform) return __ddiv_rn(__dsub_rn(f[stride], f[-stride]), __dmul_rn(2.0, A.h0));
+    const double h1 = A.h[i - 1], h2 = A.h[i];
+    const double s = __dadd_rn(h1, h2);
+    const double a = __ddiv_rn(-h2, __dmul_rn(h1, s));
+    const double b = __ddiv_rn(__dsub_rn(h2, h1), __dmul_rn(h1, h2));
+    const double c = __ddiv_rn(h1, __dmul_rn(h2, s));
+    return __dadd_rn(__dadd_rn(__dmul_rn(a, f[-stride]), __dmul_rn(b, f[0])), __dmul_rn(c, f[stride]));
+}
+
+// rho of the interior into a dense (nx, ny) scratch array (the derivative stencils read it)
+__global__ void rho_kernel(const double *ar1, const double *ar2, long long pitch, int nx, int ny, int g,
+                           double *rho)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+    if (i >= nx || j >= ny) return;
+    const long long k = (long long)(i + g) * pitch + (j + g);
+    rho[(long long)i * ny + j] = __dadd_rn(ar1[k], ar2[k]);
+}
+
+__constant__ unsigned char kBlues[9][3] = {
+    {0xf7, 0xfb, 0xff}, {0xde, 0xeb, 0xf7}, {0xc6, 0xdb, 0xef}, {0x9e, 0xca, 0xe1}, {0x6b, 0xae, 0xd6},
+    {0x42, 0x92, 0xc6}, {0x21, 0x71, 0xb5}, {0x08, 0x51, 0x9c}, {0x08, 0x30, 0x6b}};
+
+__global__ void grad_kernel(const double *rho, int nx, int ny, Axis X, Axis Y, const double *al,
+                            long long pitch, int g, double *grad, unsigned char *rgb)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+    if (i >= nx || j >= ny) return;
+    const double *f = rho + (long long)i * ny + j;
+    const double dx = deriv(f, ny, i, X), dy = deriv(f, 1, j, Y);
+    const double m = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+    grad[(long long)i * ny + j] = m;
+    if (!rgb) return;
+    const long long ka = (long long)(i + g) * pitch + (j + g);
+    const double a = al[ka];
+    unsigned char *px = rgb + ((long long)j * (2 * nx) + i) * 3;
+    bool edge = false;
+    if (i + 1 < nx) edge |= (a - 0.5) * (al[ka + pitch] - 0.5) < 0.0;
+    if (j + 1 < ny) edge |= (a - 0.5) * (al[ka + 1] - 0.5) < 0.0;
+    if (edge) {
+        px[0] = 255;
+        px[1] = 0;
+        px[2] = 0;
+    } else {
+        double s = (m - 1.0) / (2400.0 - 1.0);
+        s = s != s ? 0.0 : fmin(fmax(s, 0.0), 1.0);
+        const double pos = s * 8.0;
+        const int k0 = min((int)pos, 7);
+        const double w = pos - k0;
+        for (int c = 0; c < 3; ++c)
+            px[c] = (unsigned char)lrint((1.0 - w) * kBlues[k0][c] + w * kBlues[k0 + 1][c]);
+    }
+    double v = a != a ? 0.0 : fmin(fmax(a, 0.0), 1.0);
+    const unsigned char grey = (unsigned char)lrint(255.0 * (1.0 - v));
+    unsigned char *pa = rgb + ((long long)j * (2 * nx) + nx + i) * 3;
+    pa[0] = pa[1] = pa[2] = grey;
+}
+
+}  // namespace
+
+extern "C" int wm_schlieren(const wm_fields *q, int nx, int ny, int g, const double *xh, const double *yh,
+                            double x_h0, double y_h0, double *rho_scratch, double *grad,
+                            unsigned char *rgb, void *stream)
+{
+    if (!q || !q->ar1 || !q->ar2 || !q->al || !rho_scratch || !grad || nx < 2 || ny < 2 || nx > 65535 || g < 0 ||
+        q->pitch < ny + 2 * g || (!xh && !(x_h0 != 0.0)) || (!yh && !(y_h0 != 0.0)))
+        return WM_ERR_INVALID;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const dim3 block(128), grid((ny + 127) / 128, nx);
+    rho_kernel<<<grid, block, 0, s>>>(q->ar1, q->ar2, q->pitch, nx, ny, g, rho_scratch);
+    const Axis X{xh, x_h0, xh == nullptr, nx}, Y{yh, y_h0, yh == nullptr, ny};
+    grad_kernel<<<grid, block, 0, s>>>(rho_scratch, nx, ny, X, Y, q->al, q->pitch, g, grad, rgb);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        char msg[200];
+        snprintf(msg, sizeof msg, "wm_schlieren: %s", cudaGetErrorString(e));
+        wm::set_error_text(msg);
+        return WM_ERR_CUDA;
+    }
+    return WM_OK;
+}

@@ -83,17 +83,19 @@ __global__ void __launch_bounds__(BX *BY) sensor_kernel(Grid g, Fields q, Prep p
     sensor_body(g, q, p, sc, i, j);
 }
 
-template <int STAGE, typename FT>
+// Pass STAGE of the limiter; NP = STAGE rebuilds the blends of the earlier passes in registers
+// (fused stage), NP = 0 reads fh/gh as the in-place blend sweeps left them (closures).
+template <int STAGE, typename FT, int NP>
 __global__ void __launch_bounds__(BX *BY)
 theta_kernel(Grid g, Eos e, Fields q, Face<FT> fh, Face<FT> gh, Face<FT> fl, Face<FT> gl,
-             double *theta, double dt, const double *dt_dev, unsigned long long *limited)
+             Theta3 th3, double dt, const double *dt_dev, unsigned long long *limited)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x + g.g;
     int i = blockIdx.y * blockDim.y + threadIdx.y + g.g;
     if (i >= g.g + g.nx || j >= g.g + g.ny) return;
     if (dt_dev) dt = *dt_dev;
-    double th = theta_body<STAGE>(g, e, q, fh, gh, fl, gl, dt, i, j);
-    theta[kw_of(g, i, j)] = th;
+    double th = theta_body<STAGE, FT, NP>(g, e, q, fh, gh, fl, gl, dt, th3.t, i, j);
+    th3.t[STAGE][kw_of(g, i, j)] = th;
     if (limited) count_if(limited, th < 1.0);
 }
 
@@ -107,14 +109,15 @@ blend_kernel(Grid g, Face<FT> fh, Face<FT> gh, Face<FT> fl, Face<FT> gl, const d
     blend_body(g, fh, gh, fl, gl, theta, i, j);
 }
 
-template <typename FT>
+template <typename FT, int NP>
 __global__ void __launch_bounds__(BX *BY)
-final_kernel(Grid g, Eos e, unsigned flags, Fields q, Fields old, Face<FT> fh, Face<FT> gh, double dt,
-             const double *dt_dev, double alpha, double beta, Counters cnt)
+final_kernel(Grid g, Eos e, unsigned flags, Fields q, Fields old, Face<FT> fh, Face<FT> gh, Face<FT> fl,
+             Face<FT> gl, Theta3 th3, double dt, const double *dt_dev, double alpha, double beta, Counters cnt)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     int i = blockIdx.y * blockDim.y + threadIdx.y;
-    unsigned long long dt_bits = final_body(g, e, flags, q, old, fh, gh, dt, dt_dev, alpha, beta, cnt, i, j);
+    unsigned long long dt_bits =
+        final_body<FT, NP>(g, e, flags, q, old, fh, gh, fl, gl, th3.t, dt, dt_dev, alpha, beta, cnt, i, j);
     if (flags & FIN_DT) {
         for (int o = 16; o > 0; o >>= 1) {
             unsigned long long other = __shfl_down_sync(0xffffffffu, dt_bits, o);
@@ -223,39 +226,54 @@ template <typename FT>
 void launch_limiter(const Grid &g, const Eos &e, const Fields &q, const Face<FT> &fh,
                     const Face<FT> &gh, const Face<FT> &fl, const Face<FT> &gl,
                     double *const theta[3], double dt, const double *dt_dev, const Counters &cnt,
-                    cudaStream_t s)
+                    bool deferred, cudaStream_t s)
 {
     const dim3 gt = grid2(g.ny, g.nx), gb = grid2(g.ny + 1, g.nx + 1), bl(BX, BY);
-    theta_kernel<0, FT><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, theta[0], dt, dt_dev, cnt.limited);
+    const Theta3 t3{{theta[0], theta[1], theta[2]}};
+    if (deferred) {  // blends rebuilt by the next pass and by the combine
+        theta_kernel<0, FT, 0><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited);
+        theta_kernel<1, FT, 1><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited);
+        theta_kernel<2, FT, 2><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited);
+        return;
+    }
+    theta_kernel<0, FT, 0><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited);
     blend_kernel<FT><<<gb, bl, 0, s>>>(g, fh, gh, fl, gl, theta[0]);
-    theta_kernel<1, FT><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, theta[1], dt, dt_dev, cnt.limited);
+    theta_kernel<1, FT, 0><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited);
     blend_kernel<FT><<<gb, bl, 0, s>>>(g, fh, gh, fl, gl, theta[1]);
-    theta_kernel<2, FT><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, theta[2], dt, dt_dev, cnt.limited);
+    theta_kernel<2, FT, 0><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited);
     blend_kernel<FT><<<gb, bl, 0, s>>>(g, fh, gh, fl, gl, theta[2]);
 }
 
 template <typename FT>
 void launch_final(const Grid &g, const Eos &e, unsigned flags, const Fields &q, const Fields &old,
-                  const Face<FT> &fh, const Face<FT> &gh, double dt, const double *dt_dev,
+                  const Face<FT> &fh, const Face<FT> &gh, const Face<FT> &fl, const Face<FT> &gl,
+                  double *const theta[3], bool deferred, double dt, const double *dt_dev,
                   double alpha, double beta, const Counters &cnt, cudaStream_t s)
 {
-    final_kernel<FT><<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, e, flags, q, old, fh, gh, dt,
-                                                                  dt_dev, alpha, beta, cnt);
+    const Theta3 t3{{theta[0], theta[1], theta[2]}};
+    if (deferred && (flags & FIN_RK3))
+        final_kernel<FT, 3><<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, e, flags, q, old, fh, gh, fl, gl,
+                                                                          t3, dt, dt_dev, alpha, beta, cnt);
+    else
+        final_kernel<FT, 0><<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, e, flags, q, old, fh, gh, fl, gl,
+                                                                          t3, dt, dt_dev, alpha, beta, cnt);
 }
 
 template void launch_limiter<double>(const Grid &, const Eos &, const Fields &, const Face<double> &,
                                      const Face<double> &, const Face<double> &, const Face<double> &,
-                                     double *const[3], double, const double *, const Counters &,
+                                     double *const[3], double, const double *, const Counters &, bool,
                                      cudaStream_t);
 template void launch_limiter<float>(const Grid &, const Eos &, const Fields &, const Face<float> &,
                                     const Face<float> &, const Face<float> &, const Face<float> &,
-                                    double *const[3], double, const double *, const Counters &,
+                                    double *const[3], double, const double *, const Counters &, bool,
                                     cudaStream_t);
 template void launch_final<double>(const Grid &, const Eos &, unsigned, const Fields &, const Fields &,
-                                   const Face<double> &, const Face<double> &, double, const double *,
+                                   const Face<double> &, const Face<double> &, const Face<double> &,
+                                   const Face<double> &, double *const[3], bool, double, const double *,
                                    double, double, const Counters &, cudaStream_t);
 template void launch_final<float>(const Grid &, const Eos &, unsigned, const Fields &, const Fields &,
-                                  const Face<float> &, const Face<float> &, double, const double *,
+                                  const Face<float> &, const Face<float> &, const Face<float> &,
+                                  const Face<float> &, double *const[3], bool, double, const double *,
                                   double, double, const Counters &, cudaStream_t);
 
 void launch_prep32(const Grid &g, const Eos &e, const Fields &q, const PrepT<float> &p,

@@ -154,11 +154,11 @@ extern "C" int wm_rhs_stage_static(const wm_params *p, int nx, int ny, int g, co
     launch_bc(G, p->bc, F, nullptr, s);
     launch_prep(G, E, F, P, p->variant, s);
     launch_faces(G, E, p->variant, p->recon, F, P, fh, gh, fl, gl, true, true, s);
-    launch_limiter(G, E, F, fh, gh, fl, gl, theta, dt, nullptr, none, s);
+    launch_limiter(G, E, F, fh, gh, fl, gl, theta, dt, nullptr, none, false, s);
     unsigned flags = FIN_RK3 | FIN_PRIM;
     if (p->emergency_repair) flags |= FIN_ADMISSIBLE;
     if (alpha != 0.0) flags |= FIN_OLD_READ;
-    launch_final(G, E, flags, F, O, fh, gh, dt, nullptr, alpha, beta, none, s);
+    launch_final(G, E, flags, F, O, fh, gh, fl, gl, theta, false, dt, nullptr, alpha, beta, none, s);
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) {
         char msg[256];

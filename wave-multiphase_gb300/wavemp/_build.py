@@ -11,7 +11,7 @@ ROOT_DIR = os.path.dirname(PKG_DIR)           # .../wave-multiphase_gb300
 CSRC = os.path.join(ROOT_DIR, "csrc")
 BUILD = os.path.join(ROOT_DIR, "_build")
 LIB = os.path.join(PKG_DIR, "libwavemp.so")
-SOURCES = ("wm_capi.cu", "wm_stage.cu", "wm_faces.cu", "wm_static.cu", "wm_batch.cu")
+SOURCES = ("wm_capi.cu", "wm_stage.cu", "wm_faces.cu", "wm_static.cu", "wm_batch.cu", "wm_post.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

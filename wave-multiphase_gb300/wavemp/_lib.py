@@ -32,6 +32,16 @@ class WmFields(ctypes.Structure):
                [("pitch", ctypes.c_longlong)]
 
 
+MAX_SAVES = 32
+
+
+class WmSchedule(ctypes.Structure):
+    _fields_ = [("t", ctypes.c_double), ("t_end", ctypes.c_double), ("step", ctypes.c_longlong),
+                ("nsaves", ctypes.c_int), ("hit", ctypes.c_int), ("finished", ctypes.c_int),
+                ("dt", ctypes.c_double), ("save_times", ctypes.c_double * MAX_SAVES),
+                ("saved", ctypes.c_int * MAX_SAVES)]
+
+
 class WmBatchParams(ctypes.Structure):
     _fields_ = [("variant", ctypes.c_int), ("recon", ctypes.c_int), ("precision", ctypes.c_int),
                 ("emergency_repair", ctypes.c_int), ("g", ctypes.c_int), ("cfl", ctypes.c_double),
@@ -63,9 +73,13 @@ EXPORTS = ("wm_version", "wm_last_error", "wm_workspace_bytes", "wm_create", "wm
            "wm_profile", "wm_profile_read", "wm_probe_fp64_flops", "wm_rhs_stage_static",
            "wm_solve_workspace_bytes", "wm_batch_create", "wm_batch_destroy", "wm_batch_set",
            "wm_batch_clear", "wm_batch_init_dt", "wm_batch_run", "wm_batch_query",
-           "wm_batch_tile_shape", "wm_batch_scalars", "wm_batch_info")
+           "wm_batch_tile_shape", "wm_batch_scalars", "wm_batch_info", "wm_batch_profile",
+           "wm_batch_profile_read", "wm_schlieren", "wm_run", "wm_run_uses_graph",
+           "wm_set_limiter_sweeps")
 STATIC_MAX_CELLS = 32768
 PROF_GROUPS = ("bc", "prep", "faces", "limiter", "final")
+BATCH_PHASES = ("bc_x", "bc_y", "prep", "sensor", "faces", "theta0", "theta1", "theta2", "final",
+                "step_end")
 
 _lib = None
 
@@ -123,6 +137,12 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.wm_batch_tile_shape.argtypes = [vp, i, i]
     L.wm_batch_scalars.argtypes = [vp, vp, i, vp]
     L.wm_batch_info.argtypes = [vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)]
+    L.wm_batch_profile.argtypes = [vp, i]
+    L.wm_schlieren.argtypes = [F, i, i, i, vp, vp, d, d, vp, vp, vp, vp]
+    L.wm_run.argtypes = [vp, F, F, ctypes.POINTER(WmSchedule), ctypes.c_longlong, vp]
+    L.wm_run_uses_graph.argtypes = [vp]
+    L.wm_set_limiter_sweeps.argtypes = [vp, i]
+    L.wm_batch_profile_read.argtypes = [vp, ctypes.POINTER(d * len(BATCH_PHASES)), i, vp]
     for name in EXPORTS:
         if name not in ("wm_version", "wm_last_error", "wm_workspace_bytes", "wm_destroy",
                         "wm_solve_workspace_bytes", "wm_batch_destroy"):

@@ -157,6 +157,16 @@ class Batch:
         _lib.check(self.L.wm_batch_info(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)), "wm_batch_info")
         return {"tiles": a.value, "grid": b.value, "graph": bool(c.value)}
 
+    def profile(self, enable: bool = True):
+        """Per-phase device timing of later runs (block 0's clock between grid barriers)."""
+        _lib.check(self.L.wm_batch_profile(self._h, int(bool(enable))), "wm_batch_profile")
+
+    def profile_read(self, reset: bool = True) -> dict:
+        ms = (ctypes.c_double * len(_lib.BATCH_PHASES))()
+        _lib.check(self.L.wm_batch_profile_read(self._h, ctypes.byref(ms), int(reset), _stream()),
+                   "wm_batch_profile_read")
+        return dict(zip(_lib.BATCH_PHASES, list(ms)))
+
     def set_shape(self, cls: int, shape: int):
         _lib.check(self.L.wm_batch_tile_shape(self._h, int(cls), int(shape)), "wm_batch_tile_shape")
 

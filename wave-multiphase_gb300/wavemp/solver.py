@@ -177,6 +177,43 @@ class Solver:
                                   float(dt) if dt is not None else 0.0, out, _stream()), "step")
         return self._dt_host.value if sync else None
 
+    def run(self, q, q_old, t_end: float, save_times=(), t: float = 0.0, step: int = 0,
+            on_save=None, max_steps: int | None = None):
+        """The reference's time loop (SC:2009-2073) with its steps on the device (wm_run): dt
+        clamped to the save times and to t_end, one host wait per save time. on_save(q, step, t, k)
+        is called when save time k is reached (the reference writes its npz there). Returns
+        (t, step); the schedule of the last call is kept in ``self.schedule``."""
+        times = [float(v) for v in save_times]
+        if len(times) > _lib.MAX_SAVES:
+            raise ValueError(f"at most {_lib.MAX_SAVES} save times")
+        sch = _lib.WmSchedule()
+        sch.t, sch.t_end, sch.step, sch.nsaves = float(t), float(t_end), int(step), len(times)
+        for k, ts in enumerate(times):
+            sch.save_times[k] = ts
+            sch.saved[k] = int(t >= ts - 1.0e-14)
+        limit = (1 << 62) if max_steps is None else int(max_steps)
+        fq, fo = self._fields(q), self._fields(q_old, need_prims=False)
+        done = 0
+        while done < limit:
+            before = sch.step
+            _lib.check(self.L.wm_run(self._h, ctypes.byref(fq), ctypes.byref(fo), ctypes.byref(sch),
+                                     min(limit - done, 1 << 40), _stream()), "run")
+            done += sch.step - before
+            if sch.hit >= 0 and on_save is not None:
+                on_save(q, sch.step, sch.t, sch.hit)
+            if sch.finished or sch.step == before:
+                break
+        self.schedule = sch
+        return sch.t, sch.step
+
+    def set_limiter_sweeps(self, in_place: bool):
+        """Fused stage: blend sweeps in place (default, the reference's form) or rebuilt in
+        registers by the next pass and the combine (bit-identical)."""
+        _lib.check(self.L.wm_set_limiter_sweeps(self._h, int(bool(in_place))), "set_limiter_sweeps")
+
+    def run_uses_graph(self) -> bool:
+        return bool(self.L.wm_run_uses_graph(self._h))
+
     # -- diagnostics ----------------------------------------------------------------------------
     def workspace(self, which: int) -> torch.Tensor:
         out = torch.empty((self.nxg, self.nyg), dtype=torch.float64, device=self.device)
