@@ -144,14 +144,14 @@ int wm_step(wm_handle *h, const wm_fields *q, const wm_fields *q_old, double dt,
  * with dt <= 0. */
 int wm_init_dt(wm_handle *h, const wm_fields *q, void *stream);
 
-/* Limiter form of the fused stage (wm_rhs_stage, wm_step, wm_run). Default (in_place = 1): the
- * reference's in-place blend sweeps (pp_blend_x/y_flux_kernel, SC:1479-1548) between the passes.
- * in_place = 0: no blend sweeps -- each limiter pass and the combine rebuild the blended face fluxes
- * in registers from the high- and first-order fluxes and the passes' cell factors, bit-identical
- * (it moves less memory but costs binary64 operations, so it pays where the kernels' occupancy is
- * fixed anyway, as in the batched form, which always uses it). After a fused stage the workspace's
- * high-order arrays hold the limited fluxes in place form, the unlimited ones otherwise; the
- * closures always blend in place. */
+/* Limiter form of the fused stage (wm_rhs_stage, wm_step, wm_run). in_place = 1: the reference's
+ * in-place blend sweeps (pp_blend_x/y_flux_kernel, SC:1479-1548) between the passes. in_place = 0:
+ * no blend sweeps -- each limiter pass and the combine rebuild the blended face fluxes in registers
+ * from the high- and first-order fluxes and the passes' cell factors, bit-identical. The second
+ * moves less memory but adds blend arithmetic: the default is in place for WM_PREC_FP64 (whose
+ * binary64 pipe is the bound) and rebuilt for WM_PREC_FP32 (blends in binary32); the batched form
+ * always rebuilds. After a fused stage the workspace's high-order arrays hold the limited fluxes in
+ * place form, the unlimited ones otherwise; the closures always blend in place. */
 int wm_set_limiter_sweeps(wm_handle *h, int in_place);
 
 /* ---- the time loop on the device -------------------------------------------------------------
@@ -230,6 +230,12 @@ int wm_batch_tile_shape(wm_batch *b, int size_class, int shape);
  * or from (write=1) host memory -- snapshot and restore for measuring runs. */
 int wm_batch_scalars(wm_batch *b, void *host, int write, void *stream);
 int wm_batch_info(wm_batch *b, int *ntiles, int *grid, int *graph);
+/* Per-step dt record (mode 1: log[k] = the dt of the slot's step k) or replay (mode 2: step k
+ * uses log[k] instead of its own CFL dt, the end-time clamp still applies; the slot's first dt is
+ * log[0] when wm_batch_init_dt runs after this call), for len steps; mode 0 turns it off. `log` is
+ * caller-owned device memory of len doubles. Lets two forms of the same solves run on one dt
+ * sequence, so that their difference is the arithmetic's alone. */
+int wm_batch_dt_log(wm_batch *b, int slot, double *log, long long len, int mode);
 /* Phase timing of later runs (enable=1) or none (0). WM_BATCH_PHASES device-time sums in ms (the
  * phases of a stage: ghost fill x, ghost fill y, preparation, sensors, face sweeps, the three
  * limiter passes, combine; then the end-of-step dt phase), summed over stages and steps. */

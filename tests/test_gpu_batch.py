@@ -39,8 +39,8 @@ def alone(sp: SolveSpec, steps, precision, recon="mp5c6", variant="sc"):
 
 
 def compare(q_batch, q_alone, what, precision="fp64"):
-    """FP64: the parity tolerance. FP32: per-field L1 <= 1e-6 and largest element error <= 1e-3
-    (the precision form's stage bound; measured 8e-9). The persistent kernel inlines the same
+    """FP64: the parity tolerance. FP32: per-field L1 <= 1e-6 (momenta against the momentum
+    magnitude) and largest element error <= 1e-3 (the precision form's stage bound; measured 8e-9). The persistent kernel inlines the same
     source in another context, where the compiler may fuse multiply-adds differently, and a
     one-ulp binary32 difference can move a threshold decision of the scheme at an isolated face."""
     got = {k: pu.host(v) for k, v in q_batch.items()}
@@ -48,9 +48,11 @@ def compare(q_batch, q_alone, what, precision="fp64"):
     sc = pu.natural_scales(ref, 4.4, 6e8, 1.4, 0.0)
     pu.assert_cells(got, ref, pu.ALL, sc, what, rtol=1e-10 if precision == "fp64" else 1e-3)
     if precision == "fp32":
+        mom = np.abs(ref["ru"][5:-5, 5:-5]).sum() + np.abs(ref["rv"][5:-5, 5:-5]).sum()
         for k in ("ar1", "ar2", "ru", "rv", "E", "al"):
             a, b = got[k][5:-5, 5:-5], ref[k][5:-5, 5:-5]
-            e = np.abs(a - b).sum() / max(np.abs(b).sum(), 1e-300)
+            norm = mom if k in ("ru", "rv") else np.abs(b).sum()  # rv alone can be ~0 by symmetry
+            e = np.abs(a - b).sum() / max(norm, 1e-300)
             assert e <= 1e-6, f"{what} {k}: L1 {e:.2e}"
     return all(np.array_equal(got[k], ref[k], equal_nan=True) for k in pu.ALL)
 
@@ -120,3 +122,32 @@ def test_solve_joining_a_running_batch_matches_alone():
     assert st[0]["steps"] == 4 and st[1]["steps"] == 3
     compare(b.slots[0]["q"], alone(first, 4, "fp64"), "early solve")
     compare(b.slots[1]["q"], alone(late, 3, "fp64"), "late solve")
+
+
+def test_dt_record_and_replay():
+    """A batch replaying another batch's recorded dt sequence takes the same time steps: the same
+    scheme gives the same bits, the binary32 form differs from binary64 by round-off only."""
+    specs = [spec(nx, ny, mach=m, max_steps=6) for (nx, ny), m in zip(SIZES[:4], (1.5, 3.0, 6.0, 2.4))]
+    logs = [torch.zeros(16, dtype=torch.float64, device="cuda") for _ in specs]
+    rec = Batch(len(specs))
+    for sp, log in zip(specs, logs):
+        rec.add(sp, dt_log=log, dt_mode="record")
+    rec.run(8)
+    st = rec.status()
+    for k, log in enumerate(logs):
+        assert st[k]["steps"] == 6 and bool((log[:6] > 0).all()) and not bool(log[6:].any())
+        assert abs(float(log[:6].sum()) - st[k]["t"]) <= 1e-12 * st[k]["t"]
+    for precision in ("fp64", "fp32"):
+        rep = Batch(len(specs), precision=precision)
+        for sp, log in zip(specs, logs):
+            rep.add(sp, dt_log=log, dt_mode="replay")
+        rep.run(8)
+        sr = rep.status()
+        for k in range(len(specs)):
+            assert sr[k]["t"] == st[k]["t"]
+            if precision == "fp64":
+                for f in pu.ALL:
+                    assert np.array_equal(pu.host(rep.slots[k]["q"][f]), pu.host(rec.slots[k]["q"][f]),
+                                          equal_nan=True)
+            else:
+                compare(rep.slots[k]["q"], rec.slots[k]["q"], f"replayed fp32 slot {k}", "fp32")

@@ -50,12 +50,16 @@ struct SolveDev {
     PrepT<float> prep32;
     Cells32 cells32;
     double *theta[3];
+    float *theta32[3];
     unsigned long long *dt_bits;  // CFL reduction of the current step
     double *dt, *t;               // this step's dt, elapsed time
     long long *steps;
     int *done;
     double t_end;
     long long max_steps;
+    double *dt_log;        // per-step dt record / replay buffer (caller-owned), or null
+    long long dt_log_len;
+    int dt_mode;           // 0 none, 1 record the dt of every step, 2 replay it
 };
 
 struct Tile {
@@ -227,15 +231,16 @@ __device__ __forceinline__ void run_phase(const BatchDev &B, int phase, int stag
                 double th;
                 const int p = phase - PH_THETA0;
                 if (FP32) {
-                    th = p == 0 ? theta_body<0, float, 0>(g, S.e, S.q, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta, i, j)
-                       : p == 1 ? theta_body<1, float, 1>(g, S.e, S.q, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta, i, j)
-                                : theta_body<2, float, 2>(g, S.e, S.q, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta, i, j);
+                    th = p == 0 ? theta_body<0, float, 0>(g, S.e, S.q, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta32, i, j)
+                       : p == 1 ? theta_body<1, float, 1>(g, S.e, S.q, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta32, i, j)
+                                : theta_body<2, float, 2>(g, S.e, S.q, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta32, i, j);
+                    S.theta32[p][kw_of(g, i, j)] = float(th);
                 } else {
                     th = p == 0 ? theta_body<0, double, 0>(g, S.e, S.q, S.fh, S.gh, S.fl, S.gl, dt, S.theta, i, j)
                        : p == 1 ? theta_body<1, double, 1>(g, S.e, S.q, S.fh, S.gh, S.fl, S.gl, dt, S.theta, i, j)
                                 : theta_body<2, double, 2>(g, S.e, S.q, S.fh, S.gh, S.fl, S.gl, dt, S.theta, i, j);
+                    S.theta[p][kw_of(g, i, j)] = th;
                 }
-                S.theta[p][kw_of(g, i, j)] = th;
             }
             break;
         case PH_FINAL: {
@@ -247,7 +252,7 @@ __device__ __forceinline__ void run_phase(const BatchDev &B, int phase, int stag
             const Counters none = {nullptr, nullptr, nullptr, nullptr};
             unsigned long long bits;
             if (FP32)
-                bits = final_body<float, 3>(g, S.e, flags, S.q, S.old, S.fh32, S.gh32, S.fl32, S.gl32, S.theta,
+                bits = final_body<float, 3>(g, S.e, flags, S.q, S.old, S.fh32, S.gh32, S.fl32, S.gl32, S.theta32,
                                             dt, nullptr, alpha, beta, none, i, j);
             else
                 bits = final_body<double, 3>(g, S.e, flags, S.q, S.old, S.fh, S.gh, S.fl, S.gl, S.theta, dt,
@@ -297,6 +302,8 @@ __global__ void __launch_bounds__(kThreads) batch_kernel(BatchDev B, int nsteps)
                 *S.t = t;
                 long long n = *S.steps + 1;
                 *S.steps = n;
+                if (S.dt_mode == 1 && n - 1 < S.dt_log_len) S.dt_log[n - 1] = *S.dt;
+                if (S.dt_mode == 2 && n < S.dt_log_len) dt_next = S.dt_log[n];
                 bool stop = (S.max_steps > 0 && n >= S.max_steps) || !(dt_next > 0.0);
                 if (S.t_end > 0.0) {
                     if (t >= S.t_end - 1.0e-14 * S.t_end)
@@ -323,6 +330,7 @@ __global__ void batch_init_dt_kernel(SolveDev *solves, int slot)
     SolveDev &S = solves[slot];
     double dt = S.g.cfl * __longlong_as_double((long long)*S.dt_bits);
     *S.dt_bits = (unsigned long long)__double_as_longlong(1.0e30);
+    if (S.dt_mode == 2 && S.dt_log_len > 0) dt = S.dt_log[0];
     if (S.t_end > 0.0 && *S.t + dt > S.t_end) dt = S.t_end - *S.t;
     *S.dt = dt;
 }
@@ -484,7 +492,7 @@ size_t wm_solve_workspace_bytes(const wm_batch_params *p, int nx, int ny)
     if (!p || nx < 1 || ny < 1) return 0;
     const int g = p->g;
     if (p->precision == WM_PREC_FP32)
-        return (size_t)(28 + 11 + 8) * arr_bytes(nx, ny, g, 4) + 3 * arr_bytes(nx, ny, g, 8);
+        return (size_t)(28 + 3 + 11 + 8) * arr_bytes(nx, ny, g, 4);
     return (size_t)42 * arr_bytes(nx, ny, g, 8);
 }
 
@@ -585,11 +593,14 @@ int wm_batch_set(wm_batch *b, int slot, const wm_solve_desc *d, void *workspace,
     }
     S.t_end = d->t_end;
     S.max_steps = d->max_steps;
+    S.dt_log = nullptr;  // no dt record / replay until wm_batch_dt_log
+    S.dt_log_len = 0;
+    S.dt_mode = 0;
     char *cur = static_cast<char *>(workspace);
     if (b->P.precision == WM_PREC_FP32) {
-        size_t a4 = arr_bytes(d->nx, d->ny, g, 4), a8 = arr_bytes(d->nx, d->ny, g, 8);
-        float *f4[28 + 11 + 8];
-        for (int a = 0; a < 28 + 11 + 8; ++a) {
+        size_t a4 = arr_bytes(d->nx, d->ny, g, 4);
+        float *f4[28 + 11 + 8 + 3];
+        for (int a = 0; a < 28 + 11 + 8 + 3; ++a) {
             f4[a] = reinterpret_cast<float *>(cur);
             cur += a4;
         }
@@ -602,10 +613,7 @@ int wm_batch_set(wm_batch *b, int slot, const wm_solve_desc *d, void *workspace,
         Cells32 &C = S.cells32;
         C.ar1 = f4[39]; C.ar2 = f4[40]; C.ru = f4[41]; C.rv = f4[42]; C.p = f4[43]; C.al = f4[44];
         C.u = f4[45]; C.v = f4[46];
-        for (int k = 0; k < 3; ++k) {
-            S.theta[k] = reinterpret_cast<double *>(cur);
-            cur += a8;
-        }
+        for (int k = 0; k < 3; ++k) S.theta32[k] = f4[47 + k];
     } else {
         size_t a8 = arr_bytes(d->nx, d->ny, g, 8);
         double *f8[42];
@@ -766,6 +774,19 @@ int wm_batch_scalars(wm_batch *b, void *host, int write, void *stream)
         set_err("wm_batch_scalars", e);
         return WM_ERR_CUDA;
     }
+    return WM_OK;
+}
+
+int wm_batch_dt_log(wm_batch *b, int slot, double *log, long long len, int mode)
+{
+    if (!b || slot < 0 || slot >= b->capacity || !b->used[slot] || mode < 0 || mode > 2 ||
+        (mode != 0 && (!log || len < 1)))
+        return WM_ERR_INVALID;
+    SolveDev &S = b->host[slot];
+    S.dt_log = mode ? log : nullptr;
+    S.dt_log_len = mode ? len : 0;
+    S.dt_mode = mode;
+    b->dirty = true;
     return WM_OK;
 }
 

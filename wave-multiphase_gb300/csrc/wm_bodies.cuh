@@ -97,16 +97,20 @@ __device__ __forceinline__ void sensor_body(const Grid &g, const Fields &q, cons
 // cells (i, j) and (i+1, j) takes min(1, theta(i, j), theta(i+1, j)) over its interior neighbours,
 // in that order; the y face between (i, j) and (i, j+1) likewise. Shared by blend_body, which
 // writes the blended fluxes, and CellFaces, which rebuilds them in registers.
-__device__ __forceinline__ double face_theta_x(const Grid &g, const double *theta, long long kw, int i)
+// The factors are stored in the flux type: rounding to binary32 is monotone, so the minimum of the
+// rounded factors is the rounded minimum and the blends see the same values either way.
+template <typename FT>
+__device__ __forceinline__ FT face_theta_x(const Grid &g, const FT *theta, long long kw, int i)
 {
-    double th = 1.0;
+    FT th = FT(1);
     if (i >= g.g) th = wmin(th, theta[kw]);
     if (i + 1 < g.g + g.nx) th = wmin(th, theta[kw + g.nyg]);
     return th;
 }
-__device__ __forceinline__ double face_theta_y(const Grid &g, const double *theta, long long kw, int j)
+template <typename FT>
+__device__ __forceinline__ FT face_theta_y(const Grid &g, const FT *theta, long long kw, int j)
 {
-    double th = 1.0;
+    FT th = FT(1);
     if (j >= g.g) th = wmin(th, theta[kw]);
     if (j + 1 < g.g + g.ny) th = wmin(th, theta[kw + 1]);
     return th;
@@ -122,17 +126,17 @@ struct CellFaces {
     long long kw, kx, ky;
     FT txp[NP > 0 ? NP : 1], txm[NP > 0 ? NP : 1], typ[NP > 0 ? NP : 1], tym[NP > 0 ? NP : 1];
 
-    __device__ __forceinline__ CellFaces(const Grid &g, double *const theta[3], int i, int j)
+    __device__ __forceinline__ CellFaces(const Grid &g, FT *const theta[3], int i, int j)
     {
         kw = kw_of(g, i, j);
         kx = kw - g.nyg;
         ky = kw - 1;
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
-            txp[p] = FT(face_theta_x(g, theta[p], kw, i));
-            txm[p] = FT(face_theta_x(g, theta[p], kx, i - 1));
-            typ[p] = FT(face_theta_y(g, theta[p], kw, j));
-            tym[p] = FT(face_theta_y(g, theta[p], ky, j - 1));
+            txp[p] = face_theta_x(g, theta[p], kw, i);
+            txm[p] = face_theta_x(g, theta[p], kx, i - 1);
+            typ[p] = face_theta_y(g, theta[p], kw, j);
+            tym[p] = face_theta_y(g, theta[p], ky, j - 1);
         }
     }
     __device__ __forceinline__ FT chain(const FT *hi, const FT *lo, long long k, const FT *t) const
@@ -157,7 +161,7 @@ template <int STAGE, typename FT, int NP = 0>
 __device__ __forceinline__ double theta_body(const Grid &g, const Eos &e, const Fields &q,
                                              const Face<FT> &fh, const Face<FT> &gh,
                                              const Face<FT> &fl, const Face<FT> &gl, double dt,
-                                             double *const theta[3], int i, int j)
+                                             FT *const theta[3], int i, int j)
 {
     const CellFaces<FT, NP> cf(g, theta, i, j);
     const long long kf = kf_of(q, i, j), kw = cf.kw, kx = cf.kx, ky = cf.ky;
@@ -191,16 +195,16 @@ __device__ __forceinline__ double theta_body(const Grid &g, const Eos &e, const 
 template <typename FT>
 __device__ __forceinline__ void blend_body(const Grid &g, const Face<FT> &fh, const Face<FT> &gh,
                                            const Face<FT> &fl, const Face<FT> &gl,
-                                           const double *theta, int i, int j)
+                                           const FT *theta, int i, int j)
 {
     long long kw = kw_of(g, i, j);
     if (j >= g.g) {  // x face between (i, j) and (i+1, j)
-        const FT t = FT(face_theta_x(g, theta, kw, i));
+        const FT t = face_theta_x(g, theta, kw, i);
 #pragma unroll
         for (int c = 0; c < 7; ++c) fh.f[c][kw] = face_blend(fl.f[c][kw], fh.f[c][kw], t);
     }
     if (i >= g.g) {  // y face between (i, j) and (i, j+1)
-        const FT t = FT(face_theta_y(g, theta, kw, j));
+        const FT t = face_theta_y(g, theta, kw, j);
 #pragma unroll
         for (int c = 0; c < 7; ++c) gh.f[c][kw] = face_blend(gl.f[c][kw], gh.f[c][kw], t);
     }
@@ -217,7 +221,7 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
                                                          const Fields &q, const Fields &old,
                                                          const Face<FT> &fh, const Face<FT> &gh,
                                                          const Face<FT> &fl, const Face<FT> &gl,
-                                                         double *const theta[3],
+                                                         FT *const theta[3],
                                                          double dt, const double *dt_dev,
                                                          double alpha, double beta,
                                                          const Counters &cnt, int i, int j)
@@ -320,11 +324,25 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
             q.f[F_ALP][kf] = a1;
             q.f[F_AL][kf] = a1;
             if (interior && (flags & FIN_DT)) {
-                double c = sound_speed_r(e, ir, pp, a1);
-                double sx = g.dx / (fabs(uu) + c);
-                double sy = g.dy / (fabs(vv) + c);
-                double d = sx * sy / (sx + sy);
-                dt_bits = (unsigned long long)__double_as_longlong(d);
+                if constexpr (sizeof(FT) == 4) {
+                    // Precision form: c^2 = ((1 + Gamma) p + Pi) / (Gamma rho), the numerator (which
+                    // cancels for p near -p_inf) in binary64, the rest of the CFL candidate in
+                    // binary32 with one division: sx sy / (sx + sy) = dx dy / (dy a + dx b),
+                    // a = |u| + c, b = |v| + c.
+                    float c2 = float(((1.0 + gb) * pp + pb) * inv);
+                    if (c2 < float(kTiny)) c2 = float(kTiny);
+                    const float c = sqrtf(c2);
+                    const float a = fabsf(float(uu)) + c, b = fabsf(float(vv)) + c;
+                    const float dxf = float(g.dx), dyf = float(g.dy);
+                    const double d = double((dxf * dyf) / (dyf * a + dxf * b));
+                    dt_bits = (unsigned long long)__double_as_longlong(d);
+                } else {
+                    double c = sound_speed_r(e, ir, pp, a1);
+                    double sx = g.dx / (fabs(uu) + c);
+                    double sy = g.dy / (fabs(vv) + c);
+                    double d = sx * sy / (sx + sy);
+                    dt_bits = (unsigned long long)__double_as_longlong(d);
+                }
             }
         }
         if (wrote_q) {
@@ -336,8 +354,9 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
 }
 
 // Binary32 copies of the cell state for the face sweep, the entropy in binary32, and the
-// first-order HLLC cell state whose pressure floor and sound speed are recovered in binary64
-// (the stiffened-gas p + p_inf cancels to round-off of p_inf ~ 6e8 in binary32).
+// first-order HLLC cell state whose pressure floor and the numerator of its sound speed are
+// recovered in binary64 (the stiffened-gas p + p_inf cancels to round-off of p_inf ~ 6e8 in
+// binary32).
 __device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const Fields &q, const PrepT<float> &p, const Cells32 &c, int i, int j)
 {
     long long kf = kf_of(q, i, j), kw = kw_of(g, i, j);
@@ -373,9 +392,10 @@ __device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const F
         mix_gamma_pinf(e, a, gg, pi);
         pl = kPpCtilde * (gg - 1.0) - pi;
     }
-    double val = (gp1 * pl + pb) / (gb * rho);
-    if (val < kTiny) val = kTiny;
+    // the numerator cancels for p near -p_inf and stays binary64; the quotient and root do not
     const float rhof = ar1f + ar2f;
+    float val = float(gp1 * pl + pb) / (float(gb) * float(rho));
+    if (val < float(kTiny)) val = float(kTiny);
     const float irf = 1.0f / rhof;
     const float u = ruf * irf, v = rvf * irf;
     const float af = float(a), plf = float(pl);
@@ -383,7 +403,7 @@ __device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const F
     p.lv[kw] = v;
     p.lp[kw] = plf;
     p.la[kw] = af;
-    p.lc[kw] = float(sqrt(val));
+    p.lc[kw] = sqrtf(val);
     p.lE[kw] = prim_to_energy(e, rhof, u, v, plf, af);
 }
 

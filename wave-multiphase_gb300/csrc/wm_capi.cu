@@ -44,12 +44,12 @@ size_t array_bytes(int nx, int ny, int g, size_t elem = sizeof(double))
 }
 
 // Workspace of the plain form: 42 binary64 arrays. Precision form: 28 binary32 face arrays, 3
-// binary64 limiter factors, 11 binary32 per-cell arrays and 8 binary32 cell copies.
+// binary32 limiter factors (bound solves in binary64, stored in the flux type), 11 binary32
+// per-cell arrays and 8 binary32 cell copies.
 size_t layout_bytes(int precision, int nx, int ny, int g)
 {
     if (precision == WM_PREC_FP32)
-        return (size_t)(kFaceArrays + kPrepArrays + kCellCopies) * array_bytes(nx, ny, g, sizeof(float)) +
-               (size_t)kThetaArrays * array_bytes(nx, ny, g) + kTailBytes;
+        return (size_t)(kArrays + kCellCopies) * array_bytes(nx, ny, g, sizeof(float)) + kTailBytes;
     return (size_t)kArrays * array_bytes(nx, ny, g) + kTailBytes;
 }
 
@@ -89,10 +89,11 @@ struct wm_handle {
     bool own_ws = false;
     bool fp32 = false;
     double *arr[kArrays];  // binary64 arrays (plain form) by WM_WS_* index
-    float *arr32[kArrays]; // binary32 arrays (precision form) by WM_WS_* index; theta stays binary64
+    float *arr32[kArrays]; // binary32 arrays (precision form) by WM_WS_* index
     Face7 fh, gh, fl, gl;
     Face<float> fh32, gh32, fl32, gl32;
     double *theta[3];
+    float *theta32[3];
     Prep prep;
     PrepT<float> prep32;
     Cells32 cells32;
@@ -246,6 +247,9 @@ int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t
     char *base = static_cast<char *>(h->ws);
     char *tail;
     h->fp32 = p->precision == WM_PREC_FP32;
+    // measured on the triple point: rebuilding the blends in registers pays in binary32 (1525 ->
+    // 1818 Mcell-stage/s) and costs in binary64 (254 -> 229), whose pipe is the bound there
+    h->defer_limiter = h->fp32;
     if (!h->fp32) {
         size_t ab = array_bytes(nx, ny, g);
         for (int a = 0; a < kArrays; ++a) h->arr[a] = reinterpret_cast<double *>(base + (size_t)a * ab);
@@ -264,18 +268,12 @@ int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t
         P.lE = h->arr[41];
         tail = base + (size_t)kArrays * ab;
     } else {
-        size_t ab4 = array_bytes(nx, ny, g, sizeof(float)), ab8 = array_bytes(nx, ny, g);
+        size_t ab4 = array_bytes(nx, ny, g, sizeof(float));
         char *cur = base;
         for (int a = 0; a < kArrays; ++a) {
-            if (a >= WM_WS_THETA && a < WM_WS_THETA + 3) {
-                h->arr[a] = reinterpret_cast<double *>(cur);
-                h->arr32[a] = nullptr;
-                cur += ab8;
-            } else {
-                h->arr32[a] = reinterpret_cast<float *>(cur);
-                h->arr[a] = nullptr;
-                cur += ab4;
-            }
+            h->arr32[a] = reinterpret_cast<float *>(cur);
+            h->arr[a] = nullptr;
+            cur += ab4;
         }
         float *copies[kCellCopies];
         for (int c = 0; c < kCellCopies; ++c) {
@@ -288,7 +286,10 @@ int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t
             h->fl32.f[c] = h->arr32[WM_WS_FXL + c];
             h->gl32.f[c] = h->arr32[WM_WS_GYL + c];
         }
-        for (int s = 0; s < 3; ++s) h->theta[s] = h->arr[WM_WS_THETA + s];
+        for (int s = 0; s < 3; ++s) {
+            h->theta[s] = nullptr;
+            h->theta32[s] = h->arr32[WM_WS_THETA + s];
+        }
         PrepT<float> &P = h->prep32;
         P.sx = h->arr32[WM_WS_SIGMA_X];
         P.sy = h->arr32[WM_WS_SIGMA_Y];
@@ -411,7 +412,7 @@ int wm_limit_fluxes(wm_handle *h, const wm_fields *q, double dt, void *stream)
     if (!h || !fields_ok(h, q) || !std::isfinite(dt)) return WM_ERR_INVALID;
     if (!h->fluxes_ready || !h->low_ready) return WM_ERR_STATE;
     if (h->fp32)
-        launch_limiter(h->g, h->e, to_fields(q), h->fh32, h->gh32, h->fl32, h->gl32, h->theta, dt,
+        launch_limiter(h->g, h->e, to_fields(q), h->fh32, h->gh32, h->fl32, h->gl32, h->theta32, dt,
                        nullptr, h->cnt, false, as_stream(stream));
     else
         launch_limiter(h->g, h->e, to_fields(q), h->fh, h->gh, h->fl, h->gl, h->theta, dt, nullptr,
@@ -428,7 +429,7 @@ int wm_rk3_update(wm_handle *h, const wm_fields *q, const wm_fields *q_old, doub
     Fields F = to_fields(q), O = q_old ? to_fields(q_old) : F;
     const unsigned fl = FIN_RK3 | (alpha != 0.0 ? FIN_OLD_READ : 0u);
     if (h->fp32)
-        launch_final(h->g, h->e, fl, F, O, h->fh32, h->gh32, h->fl32, h->gl32, h->theta, false, dt,
+        launch_final(h->g, h->e, fl, F, O, h->fh32, h->gh32, h->fl32, h->gl32, h->theta32, false, dt,
                      nullptr, alpha, beta, h->cnt, as_stream(stream));
     else
         launch_final(h->g, h->e, fl, F, O, h->fh, h->gh, h->fl, h->gl, h->theta, false, dt, nullptr,
@@ -514,9 +515,9 @@ static int run_stage(wm_handle *h, const Fields &F, const Fields &O, double dt, 
                          true, true, s);
     }
     {
-        ProfScope ps(h, WM_PROF_LIMITER, 6, s);
+        ProfScope ps(h, WM_PROF_LIMITER, h->defer_limiter ? 3 : 6, s);
         if (h->fp32)
-            launch_limiter(h->g, h->e, F, h->fh32, h->gh32, h->fl32, h->gl32, h->theta, dt, dt_dev,
+            launch_limiter(h->g, h->e, F, h->fh32, h->gh32, h->fl32, h->gl32, h->theta32, dt, dt_dev,
                            h->cnt, h->defer_limiter, s);
         else
             launch_limiter(h->g, h->e, F, h->fh, h->gh, h->fl, h->gl, h->theta, dt, dt_dev, h->cnt,
@@ -531,7 +532,7 @@ static int run_stage(wm_handle *h, const Fields &F, const Fields &O, double dt, 
             launch_dt_reset(h->cnt, s);
         }
         if (h->fp32)
-            launch_final(h->g, h->e, flags, F, O, h->fh32, h->gh32, h->fl32, h->gl32, h->theta,
+            launch_final(h->g, h->e, flags, F, O, h->fh32, h->gh32, h->fl32, h->gl32, h->theta32,
                          h->defer_limiter, dt, dt_dev, alpha, beta, h->cnt, s);
         else
             launch_final(h->g, h->e, flags, F, O, h->fh, h->gh, h->fl, h->gl, h->theta, h->defer_limiter,

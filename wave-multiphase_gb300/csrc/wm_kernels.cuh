@@ -41,8 +41,8 @@ struct Counters {
     unsigned long long *dt_bits;  // atomic min of the positive dt candidates (bit pattern)
 };
 
-struct Theta3 {
-    double *t[3];  // cell limiter factors of the three passes
+template <typename FT> struct Theta3 {
+    FT *t[3];  // cell limiter factors of the three passes, in the flux type
 };
 
 // Flags of final_kernel.
@@ -67,12 +67,12 @@ void launch_faces(const Grid &g, const Eos &e, int variant, int recon, const Fie
 template <typename FT>
 void launch_limiter(const Grid &g, const Eos &e, const Fields &q, const Face<FT> &fh,
                     const Face<FT> &gh, const Face<FT> &fl, const Face<FT> &gl,
-                    double *const theta[3], double dt, const double *dt_dev, const Counters &cnt,
+                    FT *const theta[3], double dt, const double *dt_dev, const Counters &cnt,
                     bool deferred, cudaStream_t s);
 template <typename FT>
 void launch_final(const Grid &g, const Eos &e, unsigned flags, const Fields &q, const Fields &old,
                   const Face<FT> &fh, const Face<FT> &gh, const Face<FT> &fl, const Face<FT> &gl,
-                  double *const theta[3], bool deferred, double dt, const double *dt_dev,
+                  FT *const theta[3], bool deferred, double dt, const double *dt_dev,
                   double alpha, double beta, const Counters &cnt, cudaStream_t s);
 void launch_copy_old(const Grid &g, const Fields &q, const Fields &old, cudaStream_t s);
 void launch_dt_reset(const Counters &cnt, cudaStream_t s);

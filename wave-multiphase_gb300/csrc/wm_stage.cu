@@ -88,20 +88,20 @@ __global__ void __launch_bounds__(BX *BY) sensor_kernel(Grid g, Fields q, Prep p
 template <int STAGE, typename FT, int NP>
 __global__ void __launch_bounds__(BX *BY)
 theta_kernel(Grid g, Eos e, Fields q, Face<FT> fh, Face<FT> gh, Face<FT> fl, Face<FT> gl,
-             Theta3 th3, double dt, const double *dt_dev, unsigned long long *limited)
+             Theta3<FT> th3, double dt, const double *dt_dev, unsigned long long *limited)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x + g.g;
     int i = blockIdx.y * blockDim.y + threadIdx.y + g.g;
     if (i >= g.g + g.nx || j >= g.g + g.ny) return;
     if (dt_dev) dt = *dt_dev;
     double th = theta_body<STAGE, FT, NP>(g, e, q, fh, gh, fl, gl, dt, th3.t, i, j);
-    th3.t[STAGE][kw_of(g, i, j)] = th;
+    th3.t[STAGE][kw_of(g, i, j)] = FT(th);
     if (limited) count_if(limited, th < 1.0);
 }
 
 template <typename FT>
 __global__ void __launch_bounds__(BX *BY)
-blend_kernel(Grid g, Face<FT> fh, Face<FT> gh, Face<FT> fl, Face<FT> gl, const double *theta)
+blend_kernel(Grid g, Face<FT> fh, Face<FT> gh, Face<FT> fl, Face<FT> gl, const FT *theta)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x + g.g - 1;
     int i = blockIdx.y * blockDim.y + threadIdx.y + g.g - 1;
@@ -112,7 +112,7 @@ blend_kernel(Grid g, Face<FT> fh, Face<FT> gh, Face<FT> fl, Face<FT> gl, const d
 template <typename FT, int NP>
 __global__ void __launch_bounds__(BX *BY)
 final_kernel(Grid g, Eos e, unsigned flags, Fields q, Fields old, Face<FT> fh, Face<FT> gh, Face<FT> fl,
-             Face<FT> gl, Theta3 th3, double dt, const double *dt_dev, double alpha, double beta, Counters cnt)
+             Face<FT> gl, Theta3<FT> th3, double dt, const double *dt_dev, double alpha, double beta, Counters cnt)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     int i = blockIdx.y * blockDim.y + threadIdx.y;
@@ -225,11 +225,11 @@ void launch_prep(const Grid &g, const Eos &e, const Fields &q, const Prep &p, in
 template <typename FT>
 void launch_limiter(const Grid &g, const Eos &e, const Fields &q, const Face<FT> &fh,
                     const Face<FT> &gh, const Face<FT> &fl, const Face<FT> &gl,
-                    double *const theta[3], double dt, const double *dt_dev, const Counters &cnt,
+                    FT *const theta[3], double dt, const double *dt_dev, const Counters &cnt,
                     bool deferred, cudaStream_t s)
 {
     const dim3 gt = grid2(g.ny, g.nx), gb = grid2(g.ny + 1, g.nx + 1), bl(BX, BY);
-    const Theta3 t3{{theta[0], theta[1], theta[2]}};
+    const Theta3<FT> t3{{theta[0], theta[1], theta[2]}};
     if (deferred) {  // blends rebuilt by the next pass and by the combine
         theta_kernel<0, FT, 0><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited);
         theta_kernel<1, FT, 1><<<gt, bl, 0, s>>>(g, e, q, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited);
@@ -247,10 +247,10 @@ void launch_limiter(const Grid &g, const Eos &e, const Fields &q, const Face<FT>
 template <typename FT>
 void launch_final(const Grid &g, const Eos &e, unsigned flags, const Fields &q, const Fields &old,
                   const Face<FT> &fh, const Face<FT> &gh, const Face<FT> &fl, const Face<FT> &gl,
-                  double *const theta[3], bool deferred, double dt, const double *dt_dev,
+                  FT *const theta[3], bool deferred, double dt, const double *dt_dev,
                   double alpha, double beta, const Counters &cnt, cudaStream_t s)
 {
-    const Theta3 t3{{theta[0], theta[1], theta[2]}};
+    const Theta3<FT> t3{{theta[0], theta[1], theta[2]}};
     if (deferred && (flags & FIN_RK3))
         final_kernel<FT, 3><<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, e, flags, q, old, fh, gh, fl, gl,
                                                                           t3, dt, dt_dev, alpha, beta, cnt);
@@ -265,7 +265,7 @@ template void launch_limiter<double>(const Grid &, const Eos &, const Fields &, 
                                      cudaStream_t);
 template void launch_limiter<float>(const Grid &, const Eos &, const Fields &, const Face<float> &,
                                     const Face<float> &, const Face<float> &, const Face<float> &,
-                                    double *const[3], double, const double *, const Counters &, bool,
+                                    float *const[3], double, const double *, const Counters &, bool,
                                     cudaStream_t);
 template void launch_final<double>(const Grid &, const Eos &, unsigned, const Fields &, const Fields &,
                                    const Face<double> &, const Face<double> &, const Face<double> &,
@@ -273,7 +273,7 @@ template void launch_final<double>(const Grid &, const Eos &, unsigned, const Fi
                                    double, double, const Counters &, cudaStream_t);
 template void launch_final<float>(const Grid &, const Eos &, unsigned, const Fields &, const Fields &,
                                   const Face<float> &, const Face<float> &, const Face<float> &,
-                                  const Face<float> &, double *const[3], bool, double, const double *,
+                                  const Face<float> &, float *const[3], bool, double, const double *,
                                   double, double, const Counters &, cudaStream_t);
 
 void launch_prep32(const Grid &g, const Eos &e, const Fields &q, const PrepT<float> &p,

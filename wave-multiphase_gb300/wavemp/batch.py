@@ -101,9 +101,11 @@ class Batch:
                 return k
         return None
 
-    def add(self, spec: SolveSpec, slot: int | None = None) -> int:
+    def add(self, spec: SolveSpec, slot: int | None = None, dt_log=None, dt_mode: str = "") -> int:
         """Place a solve in a free slot: allocate its memory, run the start-up sequence on its
-        state, compute its first dt on the device, and register it with the batch."""
+        state, compute its first dt on the device, and register it with the batch. dt_log: a
+        float64 device tensor that records (dt_mode "record") or supplies (dt_mode "replay") the
+        dt of every step."""
         if slot is None:
             slot = self.free_slot()
         if slot is None or self.slots[slot] is not None:
@@ -131,8 +133,14 @@ class Batch:
         d.q_old = s._fields(old, need_prims=False)
         _lib.check(self.L.wm_batch_set(self._h, slot, ctypes.byref(d), ctypes.c_void_p(ws.data_ptr()), nbytes),
                    "wm_batch_set")
+        if dt_mode:
+            mode = {"record": 1, "replay": 2}[dt_mode]
+            if dt_log is None or dt_log.dtype != torch.float64 or not dt_log.is_cuda:
+                raise ValueError("dt_log must be a float64 device tensor")
+            _lib.check(self.L.wm_batch_dt_log(self._h, slot, ctypes.c_void_p(dt_log.data_ptr()), dt_log.numel(), mode),
+                       "wm_batch_dt_log")
         _lib.check(self.L.wm_batch_init_dt(self._h, slot, _stream()), "wm_batch_init_dt")
-        self.slots[slot] = {"spec": spec, "q": q, "old": old, "ws": ws}
+        self.slots[slot] = {"spec": spec, "q": q, "old": old, "ws": ws, "dt_log": dt_log}
         return slot
 
     def remove(self, slot: int) -> dict:

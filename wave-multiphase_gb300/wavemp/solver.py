@@ -207,8 +207,9 @@ class Solver:
         return sch.t, sch.step
 
     def set_limiter_sweeps(self, in_place: bool):
-        """Fused stage: blend sweeps in place (default, the reference's form) or rebuilt in
-        registers by the next pass and the combine (bit-identical)."""
+        """Fused stage: blend sweeps in place (the reference's form; default of the binary64
+        form) or rebuilt in registers by the next pass and the combine (bit-identical; default of
+        the binary32 form)."""
         _lib.check(self.L.wm_set_limiter_sweeps(self._h, int(bool(in_place))), "set_limiter_sweeps")
 
     def run_uses_graph(self) -> bool:
