@@ -154,6 +154,14 @@ int wm_init_dt(wm_handle *h, const wm_fields *q, void *stream);
  * place form, the unlimited ones otherwise; the closures always blend in place. */
 int wm_set_limiter_sweeps(wm_handle *h, int in_place);
 
+/* Diagnostic of the precision form's limiter pre-check (after wm_compute_fluxes and
+ * wm_compute_low_fluxes, like wm_limit_fluxes, whose work it does): every bound pass evaluates both
+ * the binary32 pre-check that lets cells skip the binary64 bound solve and the solve itself;
+ * *decided counts cells the pre-check decided, *disagreed cells where the solve did not return 1
+ * for them (0 when the pre-check's margins hold). No counterpart in the reference. */
+int wm_verify_limiter_precheck(wm_handle *h, const wm_fields *q, double dt, long long *decided,
+                               long long *disagreed, void *stream);
+
 /* ---- the time loop on the device -------------------------------------------------------------
  * wm_run runs the reference's time loop (SC:2009-2073) for one solve: per step, clamp dt to every
  * save time not yet written and to t_end (SC:2021-2026), one SSP-RK3 step, t += dt, step += 1,

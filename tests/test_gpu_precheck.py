@@ -1,0 +1,89 @@
+"""The precision form's binary32 limiter pre-check never decides a cell the binary64 bound solve
+would limit (wm_verify_limiter_precheck runs both): on the golden fixtures (the near-vacuum stress
+state included), and on seeded states pushed onto every bound's floor -- partial densities near
+1e-10, volume fractions near 1e-10 and 1 - 1e-10, energies near the rho c~^2 floor -- with time
+steps up to 4x the CFL step so that many high-order states cross the floors."""
+import numpy as np
+import pytest
+
+import parity_util as pu
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA device", allow_module_level=True)
+
+import wavemp  # noqa: E402
+from wavemp import Solver, alloc_state, ic  # noqa: E402
+
+
+def load_state(d):
+    nx, ny, g = int(d["meta_nx"]), int(d["meta_ny"]), int(d["meta_g"])
+    q = alloc_state(nx, ny, g)
+    for k in pu.ALL:
+        q[k].copy_(torch.from_numpy(np.ascontiguousarray(d["in_" + k])))
+    return q
+
+
+def verify(s, q, dt):
+    s.apply_bc(q)
+    s.compute_fluxes(q)
+    s.compute_low_fluxes(q)
+    return s.verify_limiter_precheck(q, dt)
+
+
+@pytest.mark.parametrize("case", pu.CASES)
+def test_precheck_on_fixtures(case):
+    d = pu.load_case(case)
+    nx, ny = int(d["meta_nx"]), int(d["meta_ny"])
+    s = Solver(pu.params_from(d, precision="fp32"), nx, ny)
+    for scale in (1.0, 4.0):
+        decided, disagreed = verify(s, load_state(d), scale * float(d["dt0"]))
+        assert disagreed == 0, (case, scale, decided)
+        assert decided > 0
+
+
+def near_floor_state(nx, ny, seed):
+    rng = np.random.default_rng(seed)
+    q = ic.random_valid(nx, ny, rng)
+    g = 5
+    inner = (slice(g, g + nx), slice(g, g + ny))
+    shape = (nx, ny)
+    pick = lambda frac: torch.from_numpy(rng.random(shape) < frac).cuda()  # noqa: E731
+    rel = lambda: torch.from_numpy(1.0 + 1e-6 * rng.standard_normal(shape)).cuda()  # noqa: E731
+    ar1, ar2, al = q["ar1"][inner], q["ar2"][inner], q["al"][inner]
+    m = pick(0.15)
+    ar1[m] = (1e-10 * rel())[m]
+    m = pick(0.15)
+    ar2[m] = (1e-10 * rel())[m]
+    m = pick(0.1)
+    al[m] = (1e-10 * rel())[m]
+    m = pick(0.1)
+    al[m] = (1.0 - 1e-10 * rel())[m]
+    q["al_prim"].copy_(q["al"])
+    # energies just above the rho c~^2 floor: E = kin + p_inf + 1e-8 (1 + noise)
+    p = wavemp.SolverParams(dx=1.0 / nx, dy=0.5 / ny, gamma1=4.4, pinf1=6e8, precision="fp32")
+    a = al.clamp(1e-10, 1 - 1e-10)
+    gb = a / (p.gamma1 - 1) + (1 - a) / (p.gamma2 - 1)
+    pb = a * p.gamma1 * p.pinf1 / (p.gamma1 - 1) + (1 - a) * p.gamma2 * p.pinf2 / (p.gamma2 - 1)
+    rho = ar1 + ar2
+    kin = 0.5 * (q["ru"][inner] ** 2 + q["rv"][inner] ** 2) / rho
+    m = pick(0.1)
+    q["E"][inner][m] = (kin + pb / (1 + gb) + 1e-8 * rel())[m]
+    return p, q
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_precheck_near_the_floors(seed):
+    nx, ny = 96, 48
+    p, q = near_floor_state(nx, ny, seed)
+    s = Solver(p, nx, ny)
+    s.initialize(q)
+    dt = s.get_dt(q)
+    total_decided = 0
+    for scale in (0.5, 1.0, 4.0):
+        decided, disagreed = verify(s, {k: v.clone() for k, v in q.items()}, scale * dt)
+        assert disagreed == 0, (seed, scale, decided)
+        total_decided += decided
+    assert 0 < total_decided < 3 * 3 * 3 * nx * ny  # some cells decided, not all

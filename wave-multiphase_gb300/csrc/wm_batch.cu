@@ -231,14 +231,16 @@ __device__ __forceinline__ void run_phase(const BatchDev &B, int phase, int stag
                 double th;
                 const int p = phase - PH_THETA0;
                 if (FP32) {
-                    th = p == 0 ? theta_body<0, float, 0>(g, S.e, S.q, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta32, i, j)
-                       : p == 1 ? theta_body<1, float, 1>(g, S.e, S.q, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta32, i, j)
-                                : theta_body<2, float, 2>(g, S.e, S.q, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta32, i, j);
+                    const Cells32 &c = S.cells32;
+                    th = p == 0 ? theta_body<0, float, 0>(g, S.e, S.q, c, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta32, i, j)
+                       : p == 1 ? theta_body<1, float, 1>(g, S.e, S.q, c, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta32, i, j)
+                                : theta_body<2, float, 2>(g, S.e, S.q, c, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta32, i, j);
                     S.theta32[p][kw_of(g, i, j)] = float(th);
                 } else {
-                    th = p == 0 ? theta_body<0, double, 0>(g, S.e, S.q, S.fh, S.gh, S.fl, S.gl, dt, S.theta, i, j)
-                       : p == 1 ? theta_body<1, double, 1>(g, S.e, S.q, S.fh, S.gh, S.fl, S.gl, dt, S.theta, i, j)
-                                : theta_body<2, double, 2>(g, S.e, S.q, S.fh, S.gh, S.fl, S.gl, dt, S.theta, i, j);
+                    const Cells32 none32{};
+                    th = p == 0 ? theta_body<0, double, 0>(g, S.e, S.q, none32, S.fh, S.gh, S.fl, S.gl, dt, S.theta, i, j)
+                       : p == 1 ? theta_body<1, double, 1>(g, S.e, S.q, none32, S.fh, S.gh, S.fl, S.gl, dt, S.theta, i, j)
+                                : theta_body<2, double, 2>(g, S.e, S.q, none32, S.fh, S.gh, S.fl, S.gl, dt, S.theta, i, j);
                     S.theta[p][kw_of(g, i, j)] = th;
                 }
             }
@@ -492,7 +494,7 @@ size_t wm_solve_workspace_bytes(const wm_batch_params *p, int nx, int ny)
     if (!p || nx < 1 || ny < 1) return 0;
     const int g = p->g;
     if (p->precision == WM_PREC_FP32)
-        return (size_t)(28 + 3 + 11 + 8) * arr_bytes(nx, ny, g, 4);
+        return (size_t)(28 + 3 + 11 + 9) * arr_bytes(nx, ny, g, 4);
     return (size_t)42 * arr_bytes(nx, ny, g, 8);
 }
 
@@ -576,12 +578,7 @@ int wm_batch_set(wm_batch *b, int slot, const wm_solve_desc *d, void *workspace,
     Grid &G = S.g;
     G.nx = d->nx; G.ny = d->ny; G.g = g; G.nxg = d->nx + 2 * g; G.nyg = nyg; G.pitch = nyg;
     G.dx = d->dx; G.dy = d->dy; G.inv_dx = 1.0 / d->dx; G.inv_dy = 1.0 / d->dy; G.cfl = b->P.cfl;
-    Eos &E = S.e;
-    E.g1 = d->gamma1; E.p1 = d->pinf1; E.g2 = d->gamma2; E.p2 = d->pinf2;
-    E.r1 = 1.0 / (d->gamma1 - 1.0); E.r2 = 1.0 / (d->gamma2 - 1.0);
-    E.k1 = d->gamma1 * d->pinf1 / (d->gamma1 - 1.0); E.k2 = d->gamma2 * d->pinf2 / (d->gamma2 - 1.0);
-    E.thinc_t1 = std::tanh(1.8 * 0.5);
-    E.thinc_inv_t1 = 1.0 / E.thinc_t1;
+    S.e = make_eos(d->gamma1, d->pinf1, d->gamma2, d->pinf2);
     for (int k = 0; k < 4; ++k) S.bc[k] = d->bc[k];
     Fields *dst[2] = {&S.q, &S.old};
     for (int w = 0; w < 2; ++w) {
@@ -599,8 +596,8 @@ int wm_batch_set(wm_batch *b, int slot, const wm_solve_desc *d, void *workspace,
     char *cur = static_cast<char *>(workspace);
     if (b->P.precision == WM_PREC_FP32) {
         size_t a4 = arr_bytes(d->nx, d->ny, g, 4);
-        float *f4[28 + 11 + 8 + 3];
-        for (int a = 0; a < 28 + 11 + 8 + 3; ++a) {
+        float *f4[28 + 11 + 9 + 3];
+        for (int a = 0; a < 28 + 11 + 9 + 3; ++a) {
             f4[a] = reinterpret_cast<float *>(cur);
             cur += a4;
         }
@@ -612,8 +609,8 @@ int wm_batch_set(wm_batch *b, int slot, const wm_solve_desc *d, void *workspace,
         P.lv = f4[34]; P.lp = f4[35]; P.la = f4[36]; P.lc = f4[37]; P.lE = f4[38];
         Cells32 &C = S.cells32;
         C.ar1 = f4[39]; C.ar2 = f4[40]; C.ru = f4[41]; C.rv = f4[42]; C.p = f4[43]; C.al = f4[44];
-        C.u = f4[45]; C.v = f4[46];
-        for (int k = 0; k < 3; ++k) S.theta32[k] = f4[47 + k];
+        C.u = f4[45]; C.v = f4[46]; C.E = f4[47];
+        for (int k = 0; k < 3; ++k) S.theta32[k] = f4[48 + k];
     } else {
         size_t a8 = arr_bytes(d->nx, d->ny, g, 8);
         double *f8[42];

@@ -152,40 +152,125 @@ struct CellFaces {
     __device__ __forceinline__ FT ym(const Face<FT> &h, const Face<FT> &l, int c) const { return chain(h.f[c], l.f[c], ky, tym); }
 };
 
+// Binary32 pre-check of a limiter pass (precision form). The pass's factor is exactly 1 when the
+// binary64 low- and high-order states l = Q - dt R_L, h = Q - dt R_H are finite and h clears the
+// pass's bound (theta_cons_stage, SC:268-292; for pass 2, the division-free test of theta_ctilde).
+// The same states formed in binary32 from the stage-start binary32 copies of Q differ from them by
+// at most 3 * 2^-24 (|Q| + |dt R|) each (the rounding of Q and dt to binary32 and of the
+// multiply-add, 1.8e-7 of those magnitudes); every test below demands a margin of 3e-7 of them,
+// and for pass 2 a first-order bound of how those input errors and the binary32 evaluation move
+// the test's value, doubled. When this returns true the binary64 bound solve would return 1, so
+// it is skipped; otherwise the caller runs it. The results are the same bits either way.
+template <int STAGE>
+__device__ __forceinline__ bool theta_one_f32(const Eos &e, const Cells32 &c, long long kw, const float *rh,
+                                              const float *rl, float dtf)
+{
+    constexpr float kRel = 3.0e-7f;
+    if (STAGE == 0) {
+        bool ok = true;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const float qv = (k == 0 ? c.ar1 : c.ar2)[kw];
+            const float dh = dtf * rh[k], hf = qv - dh, lf = qv - dtf * rl[k];
+            const float m = kRel * (fabsf(qv) + fabsf(dh));
+            ok = ok && isfinite(lf) && isfinite(hf) && hf >= float(kPpRho) * 1.000001f + m;
+        }
+        return ok;
+    } else if (STAGE == 1) {
+        const float qv = c.al[kw];
+        const float dh = dtf * rh[5], hf = qv - dh, lf = qv - dtf * rl[5];
+        const float m = kRel * (fabsf(qv) + fabsf(dh));
+        const float lo = float(kPpAlpha) * 1.000001f + m;
+        return isfinite(lf) && isfinite(hf) && hf >= lo && 1.0f - hf >= lo;
+    } else {
+        float hx[6], dx[6];
+        bool ok = true;
+        const float *src[6] = {c.ar1, c.ar2, c.ru, c.rv, c.E, c.al};
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const float qv = src[k][kw];
+            const float dh = dtf * rh[k];
+            hx[k] = qv - dh;
+            dx[k] = kRel * (fabsf(qv) + fabsf(dh));
+            ok = ok && isfinite(hx[k]);
+            if (k >= 2 && k <= 4) ok = ok && isfinite(qv - dtf * rl[k]);
+        }
+        if (!ok) return false;
+        // ctilde_surely_above in binary32: V = 2 rho (1+G)(E - floor) - (1+G)(mx^2+my^2) - 2 rho Pi
+        float a1 = hx[5];
+        if (a1 < float(kPpAlpha)) a1 = float(kPpAlpha);
+        if (a1 > 1.0f - float(kPpAlpha)) a1 = 1.0f - float(kPpAlpha);
+        const float m1 = fmaxf(hx[0], float(kPpRho)), m2 = fmaxf(hx[1], float(kPpRho));
+        const float rho = m1 + m2, a2 = 1.0f - a1;
+        const float gb = a1 * e.r1f + a2 * e.r2f, pb = a1 * e.k1f + a2 * e.k2f, gp1 = 1.0f + gb;
+        const float Ef = hx[4] - float(kPpCtilde);
+        const float mom = hx[2] * hx[2] + hx[3] * hx[3];
+        const float t1 = 2.0f * rho * gp1 * Ef, t2 = gp1 * mom, t3 = 2.0f * rho * pb;
+        const float V = t1 - t2 - t3;
+        const float T = fabsf(t1) + t2 + fabsf(t3);
+        // first-order movement of V under the input errors (upper bounds of the magnitudes)
+        const float drho = dx[0] + dx[1];
+        const float rho_u = rho + drho, E_u = fabsf(Ef) + dx[4];
+        const float mx_u = fabsf(hx[2]) + dx[2], my_u = fabsf(hx[3]) + dx[3];
+        const float dV = (2.0f * gp1 * E_u + 2.0f * fabsf(pb)) * drho + 2.0f * rho_u * gp1 * dx[4] +
+                         2.0f * gp1 * (mx_u * dx[2] + my_u * dx[3]) +
+                         (fabsf(e.r1f - e.r2f) * (2.0f * rho_u * E_u + mx_u * mx_u + my_u * my_u) +
+                          2.0f * rho_u * fabsf(e.k1f - e.k2f)) * dx[5];
+        return isfinite(V) && isfinite(T) && isfinite(dV) && V > 2.0f * dV + 1.0e-6f * T;
+    }
+}
+
 // pp_cell_theta_kernel (SC:1397-1476): residuals of the current (partly blended) high-order and of
 // the first-order fluxes, bound solve of this pass. Pass 0 bounds the partial densities, pass 1
 // alpha and 1 - alpha, pass 2 rho c~^2 (theta_cons_stage, SC:268-292); each pass forms only the
 // residual components its bound uses. NP: limiter passes whose blends are deferred (0 when the
 // high-order arrays already hold the blended fluxes, STAGE when they are rebuilt in registers).
-template <int STAGE, typename FT, int NP = 0>
-__device__ __forceinline__ double theta_body(const Grid &g, const Eos &e, const Fields &q,
+// Precision form: the binary32 pre-check above decides most cells without binary64 arithmetic;
+// VERIFY runs the binary64 solve as well and counts (verify[0]) cells the pre-check decided and
+// (verify[1]) cells where the solve disagreed with it -- a diagnostic of the pre-check's margins.
+template <int STAGE, typename FT, int NP = 0, int VERIFY = 0>
+__device__ __forceinline__ double theta_body(const Grid &g, const Eos &e, const Fields &q, const Cells32 &c32,
                                              const Face<FT> &fh, const Face<FT> &gh,
                                              const Face<FT> &fl, const Face<FT> &gl, double dt,
-                                             FT *const theta[3], int i, int j)
+                                             FT *const theta[3], int i, int j,
+                                             unsigned long long *verify = nullptr)
 {
     const CellFaces<FT, NP> cf(g, theta, i, j);
     const long long kf = kf_of(q, i, j), kw = cf.kw, kx = cf.kx, ky = cf.ky;
     const FT idx = FT(g.inv_dx), idy = FT(g.inv_dy);
-    double l[6], h[6];
     constexpr int C0 = STAGE == 1 ? 5 : 0, C1 = STAGE == 0 ? 2 : 6;
+    FT rh[6], rl[6];
 #pragma unroll
     for (int c = C0; c < C1; ++c) {
-        FT rh = (cf.xp(fh, fl, c) - cf.xm(fh, fl, c)) * idx + (cf.yp(gh, gl, c) - cf.ym(gh, gl, c)) * idy;
-        FT rl = (fl.f[c][kw] - fl.f[c][kx]) * idx + (gl.f[c][kw] - gl.f[c][ky]) * idy;
+        rh[c] = (cf.xp(fh, fl, c) - cf.xm(fh, fl, c)) * idx + (cf.yp(gh, gl, c) - cf.ym(gh, gl, c)) * idy;
+        rl[c] = (fl.f[c][kw] - fl.f[c][kx]) * idx + (gl.f[c][kw] - gl.f[c][ky]) * idy;
         if (c == 5) {
             FT a = FT(q.f[F_ALP][kf]);
-            rh = rh - a * (cf.xp(fh, fl, 6) - cf.xm(fh, fl, 6)) * idx - a * (cf.yp(gh, gl, 6) - cf.ym(gh, gl, 6)) * idy;
-            rl = rl - a * (fl.f[6][kw] - fl.f[6][kx]) * idx - a * (gl.f[6][kw] - gl.f[6][ky]) * idy;
+            rh[c] = rh[c] - a * (cf.xp(fh, fl, 6) - cf.xm(fh, fl, 6)) * idx - a * (cf.yp(gh, gl, 6) - cf.ym(gh, gl, 6)) * idy;
+            rl[c] = rl[c] - a * (fl.f[6][kw] - fl.f[6][kx]) * idx - a * (gl.f[6][kw] - gl.f[6][ky]) * idy;
         }
+    }
+    bool one = false;
+    if constexpr (sizeof(FT) == 4) {
+        one = theta_one_f32<STAGE>(e, c32, kw, rh, rl, float(dt));
+        if (!VERIFY && one) return 1.0;
+    }
+    double l[6], h[6];
+#pragma unroll
+    for (int c = C0; c < C1; ++c) {
         double qc = q.f[c][kf];
-        l[c] = qc - dt * double(rl);
-        h[c] = qc - dt * double(rh);
+        l[c] = qc - dt * double(rl[c]);
+        h[c] = qc - dt * double(rh[c]);
     }
     double th;
     if (STAGE == 2) {
         th = theta_ctilde(e, l, h);
     } else {
         th = theta_cons_stage(e, l, h, STAGE);
+    }
+    if (VERIFY && verify) {
+        count_if(&verify[0], one);
+        count_if(&verify[1], one && th != 1.0);
     }
     return th;
 }
@@ -372,6 +457,7 @@ __device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const F
     c.al[kw] = alf;
     c.u[kw] = float(q.f[F_U][kf]);
     c.v[kw] = float(q.f[F_V][kf]);
+    c.E[kw] = float(q.f[F_E][kf]);
 
     float ge, pie;
     mix_gamma_pinf(e, alf, ge, pie);

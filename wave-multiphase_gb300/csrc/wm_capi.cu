@@ -33,7 +33,7 @@ int check_launch(const char *where)
 
 constexpr int kFaceArrays = 28, kThetaArrays = 3, kPrepArrays = 11;
 constexpr int kArrays = kFaceArrays + kThetaArrays + kPrepArrays;
-constexpr int kCellCopies = 8;  // binary32 cell copies of the precision form
+constexpr int kCellCopies = 9;  // binary32 cell copies of the precision form
 constexpr size_t kAlign = 256;
 constexpr size_t kTailBytes = 256;  // counters and dt slots
 
@@ -45,7 +45,7 @@ size_t array_bytes(int nx, int ny, int g, size_t elem = sizeof(double))
 
 // Workspace of the plain form: 42 binary64 arrays. Precision form: 28 binary32 face arrays, 3
 // binary32 limiter factors (bound solves in binary64, stored in the flux type), 11 binary32
-// per-cell arrays and 8 binary32 cell copies.
+// per-cell arrays and 9 binary32 cell copies.
 size_t layout_bytes(int precision, int nx, int ny, int g)
 {
     if (precision == WM_PREC_FP32)
@@ -219,12 +219,7 @@ int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t
     Grid &G = h->g;
     G.nx = nx; G.ny = ny; G.g = g; G.nxg = nx + 2 * g; G.nyg = ny + 2 * g; G.pitch = G.nyg;
     G.dx = p->dx; G.dy = p->dy; G.inv_dx = 1.0 / p->dx; G.inv_dy = 1.0 / p->dy; G.cfl = p->cfl;
-    Eos &E = h->e;
-    E.g1 = p->gamma1; E.p1 = p->pinf1; E.g2 = p->gamma2; E.p2 = p->pinf2;
-    E.r1 = 1.0 / (p->gamma1 - 1.0); E.r2 = 1.0 / (p->gamma2 - 1.0);
-    E.k1 = p->gamma1 * p->pinf1 / (p->gamma1 - 1.0); E.k2 = p->gamma2 * p->pinf2 / (p->gamma2 - 1.0);
-    E.thinc_t1 = std::tanh(1.8 * 0.5);
-    E.thinc_inv_t1 = 1.0 / E.thinc_t1;
+    h->e = make_eos(p->gamma1, p->pinf1, p->gamma2, p->pinf2);
 
     if (workspace) {
         h->ws = workspace;
@@ -298,7 +293,7 @@ int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t
         P.lc = h->arr32[40]; P.lE = h->arr32[41];
         Cells32 &C = h->cells32;
         C.ar1 = copies[0]; C.ar2 = copies[1]; C.ru = copies[2]; C.rv = copies[3];
-        C.p = copies[4]; C.al = copies[5]; C.u = copies[6]; C.v = copies[7];
+        C.p = copies[4]; C.al = copies[5]; C.u = copies[6]; C.v = copies[7]; C.E = copies[8];
         tail = cur;
     }
     h->ctr_base = reinterpret_cast<unsigned long long *>(tail);
@@ -412,10 +407,10 @@ int wm_limit_fluxes(wm_handle *h, const wm_fields *q, double dt, void *stream)
     if (!h || !fields_ok(h, q) || !std::isfinite(dt)) return WM_ERR_INVALID;
     if (!h->fluxes_ready || !h->low_ready) return WM_ERR_STATE;
     if (h->fp32)
-        launch_limiter(h->g, h->e, to_fields(q), h->fh32, h->gh32, h->fl32, h->gl32, h->theta32, dt,
+        launch_limiter(h->g, h->e, to_fields(q), h->cells32, h->fh32, h->gh32, h->fl32, h->gl32, h->theta32, dt,
                        nullptr, h->cnt, false, as_stream(stream));
     else
-        launch_limiter(h->g, h->e, to_fields(q), h->fh, h->gh, h->fl, h->gl, h->theta, dt, nullptr,
+        launch_limiter(h->g, h->e, to_fields(q), Cells32{}, h->fh, h->gh, h->fl, h->gl, h->theta, dt, nullptr,
                        h->cnt, false, as_stream(stream));
     return check_launch("wm_limit_fluxes");
 }
@@ -517,10 +512,10 @@ static int run_stage(wm_handle *h, const Fields &F, const Fields &O, double dt, 
     {
         ProfScope ps(h, WM_PROF_LIMITER, h->defer_limiter ? 3 : 6, s);
         if (h->fp32)
-            launch_limiter(h->g, h->e, F, h->fh32, h->gh32, h->fl32, h->gl32, h->theta32, dt, dt_dev,
+            launch_limiter(h->g, h->e, F, h->cells32, h->fh32, h->gh32, h->fl32, h->gl32, h->theta32, dt, dt_dev,
                            h->cnt, h->defer_limiter, s);
         else
-            launch_limiter(h->g, h->e, F, h->fh, h->gh, h->fl, h->gl, h->theta, dt, dt_dev, h->cnt,
+            launch_limiter(h->g, h->e, F, Cells32{}, h->fh, h->gh, h->fl, h->gl, h->theta, dt, dt_dev, h->cnt,
                            h->defer_limiter, s);
     }
     unsigned flags = final_flags(h, alpha);
@@ -777,6 +772,33 @@ int wm_run(wm_handle *h, const wm_fields *q, const wm_fields *q_old, wm_schedule
 }
 
 int wm_run_uses_graph(wm_handle *h) { return h && h->run_exec ? 1 : 0; }
+
+int wm_verify_limiter_precheck(wm_handle *h, const wm_fields *q, double dt, long long *decided,
+                               long long *disagreed, void *stream)
+{
+    if (!h || !fields_ok(h, q) || !std::isfinite(dt) || !decided || !disagreed) return WM_ERR_INVALID;
+    if (!h->fp32) return WM_ERR_INVALID;  // the pre-check belongs to the precision form
+    if (!h->fluxes_ready || !h->low_ready) return WM_ERR_STATE;
+    unsigned long long *ctr = nullptr, host[2] = {0, 0};
+    cudaStream_t s = as_stream(stream);
+    cudaError_t err = cudaMalloc(&ctr, sizeof host);
+    if (err == cudaSuccess) err = cudaMemsetAsync(ctr, 0, sizeof host, s);
+    if (err == cudaSuccess) {
+        launch_limiter(h->g, h->e, to_fields(q), h->cells32, h->fh32, h->gh32, h->fl32, h->gl32, h->theta32, dt,
+                       nullptr, h->cnt, false, s, ctr);
+        err = cudaGetLastError();
+    }
+    if (err == cudaSuccess) err = cudaMemcpyAsync(host, ctr, sizeof host, cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    cudaFree(ctr);
+    if (err != cudaSuccess) {
+        set_error("wm_verify_limiter_precheck", err);
+        return WM_ERR_CUDA;
+    }
+    *decided = (long long)host[0];
+    *disagreed = (long long)host[1];
+    return WM_OK;
+}
 
 int wm_set_limiter_sweeps(wm_handle *h, int in_place)
 {

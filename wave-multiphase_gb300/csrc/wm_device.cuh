@@ -7,6 +7,7 @@
 // replaced by multiplications with host-computed reciprocals, and divisions by the same value are
 // shared (a relative difference of a few ulp, far inside the 1e-10 parity tolerance).
 #pragma once
+#include <cmath>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -21,7 +22,21 @@ struct Eos {
     double k1, k2;          // g1*p1/(g1-1), g2*p2/(g2-1)
     double thinc_t1;        // tanh(beta/2), beta = 1.8 (computed once on the host)
     double thinc_inv_t1;    // 1/tanh(beta/2)
+    float r1f, r2f, k1f, k2f;  // binary32 copies (the precision form's limiter pre-checks)
 };
+
+// The run's constants of the stiffened-gas mixture (host side).
+inline Eos make_eos(double g1, double p1, double g2, double p2)
+{
+    Eos E;
+    E.g1 = g1; E.p1 = p1; E.g2 = g2; E.p2 = p2;
+    E.r1 = 1.0 / (g1 - 1.0); E.r2 = 1.0 / (g2 - 1.0);
+    E.k1 = g1 * p1 / (g1 - 1.0); E.k2 = g2 * p2 / (g2 - 1.0);
+    E.thinc_t1 = std::tanh(1.8 * 0.5);
+    E.thinc_inv_t1 = 1.0 / E.thinc_t1;
+    E.r1f = float(E.r1); E.r2f = float(E.r2); E.k1f = float(E.k1); E.k2f = float(E.k2);
+    return E;
+}
 
 struct Grid {
     int nx, ny, g;       // interior size and ghost width

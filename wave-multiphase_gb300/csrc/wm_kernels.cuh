@@ -34,6 +34,7 @@ using Prep = PrepT<double>;
 // Binary32 copies of the cell state read by the precision form's face sweep (workspace pitch).
 struct Cells32 {
     float *ar1, *ar2, *ru, *rv, *p, *al, *u, *v;
+    float *E;  // read by the limiter's binary32 pre-checks only
 };
 
 struct Counters {
@@ -64,11 +65,13 @@ void launch_faces(const Grid &g, const Eos &e, int variant, int recon, const Fie
                   bool high, bool low, cudaStream_t s);
 // The three limiter passes. deferred: no in-place blend sweeps -- each pass and the combine rebuild
 // the blended fluxes in registers (bit-identical); fh/gh keep the unlimited high-order fluxes.
+// c32: the binary32 cell copies of the precision form (its limiter pre-checks read them; unused
+// for FT = double). verify: the pre-check diagnostic's two counters, or null.
 template <typename FT>
-void launch_limiter(const Grid &g, const Eos &e, const Fields &q, const Face<FT> &fh,
+void launch_limiter(const Grid &g, const Eos &e, const Fields &q, const Cells32 &c32, const Face<FT> &fh,
                     const Face<FT> &gh, const Face<FT> &fl, const Face<FT> &gl,
                     FT *const theta[3], double dt, const double *dt_dev, const Counters &cnt,
-                    bool deferred, cudaStream_t s);
+                    bool deferred, cudaStream_t s, unsigned long long *verify = nullptr);
 template <typename FT>
 void launch_final(const Grid &g, const Eos &e, unsigned flags, const Fields &q, const Fields &old,
                   const Face<FT> &fh, const Face<FT> &gh, const Face<FT> &fl, const Face<FT> &gl,

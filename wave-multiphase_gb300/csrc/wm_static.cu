@@ -126,12 +126,7 @@ extern "C" int wm_rhs_stage_static(const wm_params *p, int nx, int ny, int g, co
     Grid G;
     G.nx = nx; G.ny = ny; G.g = g; G.nxg = nx + 2 * g; G.nyg = ny + 2 * g; G.pitch = G.nyg;
     G.dx = p->dx; G.dy = p->dy; G.inv_dx = 1.0 / p->dx; G.inv_dy = 1.0 / p->dy; G.cfl = p->cfl;
-    Eos E;
-    E.g1 = p->gamma1; E.p1 = p->pinf1; E.g2 = p->gamma2; E.p2 = p->pinf2;
-    E.r1 = 1.0 / (p->gamma1 - 1.0); E.r2 = 1.0 / (p->gamma2 - 1.0);
-    E.k1 = p->gamma1 * p->pinf1 / (p->gamma1 - 1.0); E.k2 = p->gamma2 * p->pinf2 / (p->gamma2 - 1.0);
-    E.thinc_t1 = std::tanh(1.8 * 0.5);
-    E.thinc_inv_t1 = 1.0 / E.thinc_t1;
+    const Eos E = make_eos(p->gamma1, p->pinf1, p->gamma2, p->pinf2);
 
     double *arr[kArrays];
     for (int a = 0; a < kArrays; ++a)
@@ -154,7 +149,7 @@ extern "C" int wm_rhs_stage_static(const wm_params *p, int nx, int ny, int g, co
     launch_bc(G, p->bc, F, nullptr, s);
     launch_prep(G, E, F, P, p->variant, s);
     launch_faces(G, E, p->variant, p->recon, F, P, fh, gh, fl, gl, true, true, s);
-    launch_limiter(G, E, F, fh, gh, fl, gl, theta, dt, nullptr, none, false, s);
+    launch_limiter(G, E, F, Cells32{}, fh, gh, fl, gl, theta, dt, nullptr, none, false, s);
     unsigned flags = FIN_RK3 | FIN_PRIM;
     if (p->emergency_repair) flags |= FIN_ADMISSIBLE;
     if (alpha != 0.0) flags |= FIN_OLD_READ;

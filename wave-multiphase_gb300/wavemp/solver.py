@@ -206,6 +206,16 @@ class Solver:
         self.schedule = sch
         return sch.t, sch.step
 
+    def verify_limiter_precheck(self, q, dt: float) -> tuple[int, int]:
+        """Precision form diagnostic (after compute_fluxes / compute_low_fluxes; does the work of
+        limit_fluxes): (cells whose bound pass the binary32 pre-check decided, cells where the
+        binary64 solve disagreed -- 0 when its margins hold)."""
+        a, b = ctypes.c_longlong(), ctypes.c_longlong()
+        _lib.check(self.L.wm_verify_limiter_precheck(self._h, ctypes.byref(self._fields(q)), float(dt),
+                                                     ctypes.byref(a), ctypes.byref(b), _stream()),
+                   "verify_limiter_precheck")
+        return a.value, b.value
+
     def set_limiter_sweeps(self, in_place: bool):
         """Fused stage: blend sweeps in place (the reference's form; default of the binary64
         form) or rebuilt in registers by the next pass and the combine (bit-identical; default of
