@@ -272,8 +272,12 @@ __device__ __forceinline__ void run_phase(const BatchDev &B, int phase, int stag
     }
 }
 
+// Binary32 form: registers capped for 6 resident blocks per SM (a few dozen bytes of spills in the
+// face phase, 50 % more warps for the memory- and binary64-bound phases); binary64: uncapped.
+constexpr int kMinBlocksFp32 = 8;
+
 template <int VAR, int REC, int FP32>
-__global__ void __launch_bounds__(kThreads) batch_kernel(BatchDev B, int nsteps)
+__global__ void __launch_bounds__(kThreads, FP32 ? kMinBlocksFp32 : 1) batch_kernel(BatchDev B, int nsteps)
 {
     // Phase timing: a phase ends when the grid barrier after it opens, so block 0's clock between
     // successive barrier exits is the phase's duration across the whole grid.
