@@ -154,6 +154,10 @@ int wm_init_dt(wm_handle *h, const wm_fields *q, void *stream);
  * place form, the unlimited ones otherwise; the closures always blend in place. */
 int wm_set_limiter_sweeps(wm_handle *h, int in_place);
 
+/* Precision form: binary32 pre-checks that let cells skip binary64 tests whose outcome they prove
+ * (the limiter's bound solves, the combine's clamp / floor / NaN / repair tests), on (1, default)
+ * or off (0). Results are the same bits either way; off exists to show that. */
+int wm_set_prechecks(wm_handle *h, int on);
 /* Diagnostic of the precision form's limiter pre-check (after wm_compute_fluxes and
  * wm_compute_low_fluxes, like wm_limit_fluxes, whose work it does): every bound pass evaluates both
  * the binary32 pre-check that lets cells skip the binary64 bound solve and the solve itself;
@@ -264,6 +268,12 @@ int wm_schlieren(const wm_fields *q, int nx, int ny, int g, const double *xh, co
                  void *stream);
 
 /* ---- diagnostics ---------------------------------------------------------------------------- */
+/* The precision form's integer-pipe binary64 -> binary32 and binary32 -> binary64 conversions
+ * against the hardware ones on n device bit patterns (each read as a binary64 and, by its low 32
+ * bits, as a binary32): the numbers of results that differ (0 expected; NaN counts as equal to
+ * NaN). No counterpart in the reference. */
+int wm_check_conversions(const unsigned long long *bits, long long n, long long *bad_f32,
+                         long long *bad_f64, void *stream);
 /* Copy workspace array `which` (WM_WS_*) of the padded grid into the caller's device buffer dst
  * (same padded shape, contiguous rows of ny + 2g). */
 #define WM_WS_FX 0      /* 7 arrays: high-order x fluxes 0..5 and srcx (after limit_fluxes: blended) */

@@ -1,0 +1,52 @@
+"""The precision form's integer-pipe conversions (to_f32 / to_f64) equal the hardware
+binary64 <-> binary32 conversions bit for bit, on random bit patterns and on every boundary the
+rounding code distinguishes: ties to even, carries into the exponent, the edges of binary32's
+normal range (subnormal results, overflow to infinity), zeros, infinities, NaN."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA device", allow_module_level=True)
+
+from wavemp import _lib  # noqa: E402
+from wavemp.solver import _stream  # noqa: E402
+
+
+def check(values_u64: np.ndarray):
+    L = _lib.load()
+    t = torch.from_numpy(values_u64.view(np.int64)).cuda()
+    a, b = ctypes.c_longlong(), ctypes.c_longlong()
+    _lib.check(L.wm_check_conversions(ctypes.c_void_p(t.data_ptr()), t.numel(), ctypes.byref(a),
+                                      ctypes.byref(b), _stream()), "wm_check_conversions")
+    return a.value, b.value
+
+
+def test_random_bit_patterns():
+    rng = np.random.default_rng(0)
+    bits = rng.integers(0, 2**63, size=4_000_000, dtype=np.uint64) * np.uint64(2)
+    bits |= rng.integers(0, 2, size=bits.size, dtype=np.uint64)
+    assert check(bits) == (0, 0)
+
+
+def test_values_in_binary32_range_and_boundaries():
+    rng = np.random.default_rng(1)
+    x = np.concatenate([
+        rng.standard_normal(1_000_000) * 10.0 ** rng.uniform(-45, 39, 1_000_000),
+        np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 1.0, -1.0, 3.4028234663852886e38,
+                  3.4028235677973366e38, 3.402823567797337e38, 1.1754943508222875e-38,
+                  1.1754942106924411e-38, 1.401298464324817e-45, 7.006492321624085e-46,
+                  2.0 ** -149, 2.0 ** -150, 2.0 ** 128, 6.0e8, 1e-10, 1e-13, 1.0 - 1e-10]),
+    ])
+    bits = x.view(np.uint64).copy()
+    # exact ties and their neighbours at the rounding bit, odd and even significands
+    base = rng.standard_normal(200_000).view(np.uint64) & ~np.uint64(0x1FFFFFFF)
+    ties = np.concatenate([base | np.uint64(0x10000000), base | np.uint64(0x0FFFFFFF),
+                           base | np.uint64(0x10000001), base | np.uint64(0x1FFFFFFF)])
+    # the largest binary32 significand: rounding carries into the exponent
+    carry = (rng.standard_normal(100_000).view(np.uint64) | np.uint64(0x000FFFFFF0000000))
+    assert check(np.concatenate([bits, ties, carry])) == (0, 0)

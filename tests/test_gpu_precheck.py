@@ -87,3 +87,39 @@ def test_precheck_near_the_floors(seed):
         assert disagreed == 0, (seed, scale, decided)
         total_decided += decided
     assert 0 < total_decided < 3 * 3 * 3 * nx * ny  # some cells decided, not all
+
+
+def run_steps(p, q0, nx, ny, prechecks, steps=3):
+    s = Solver(p, nx, ny)
+    s.set_prechecks(prechecks)
+    q = {k: v.clone() for k, v in q0.items()}
+    old = alloc_state(nx, ny, names=wavemp.FIELDS)
+    s.initialize(q)
+    s.init_dt(q)
+    for _ in range(steps):
+        s.step(q, old, None, sync=False)
+    torch.cuda.synchronize()
+    return {k: pu.host(v) for k, v in q.items()}, s.status()
+
+
+@pytest.mark.parametrize("seed", [4, 5])
+def test_prechecks_do_not_change_bits(seed):
+    """Steps with the binary32 pre-checks (limiter and combine) equal steps without them, bit for
+    bit, on states at the floors (repairs and limiting happen) and on the golden fixtures."""
+    nx, ny = 96, 48
+    p, q0 = near_floor_state(nx, ny, seed)
+    a, sa = run_steps(p, q0, nx, ny, True)
+    b, sb = run_steps(p, q0, nx, ny, False)
+    for k in pu.ALL:
+        assert np.array_equal(a[k], b[k], equal_nan=True), k
+    assert sa["repaired_cells"] == sb["repaired_cells"] and sa["limited_cells"] == sb["limited_cells"]
+    assert sa["limited_cells"] > 0
+    for case in ("sc_mp5c6_stress", "m10_cfg2", "sc_mp5c6_triple"):
+        d = pu.load_case(case)
+        nxc, nyc = int(d["meta_nx"]), int(d["meta_ny"])
+        pc = pu.params_from(d, precision="fp32")
+        qc = load_state(d)
+        a, _ = run_steps(pc, qc, nxc, nyc, True, steps=2)
+        b, _ = run_steps(pc, qc, nxc, nyc, False, steps=2)
+        for k in pu.ALL:
+            assert np.array_equal(a[k], b[k], equal_nan=True), (case, k)

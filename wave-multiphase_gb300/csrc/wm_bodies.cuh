@@ -233,7 +233,7 @@ __device__ __forceinline__ double theta_body(const Grid &g, const Eos &e, const 
                                              const Face<FT> &fh, const Face<FT> &gh,
                                              const Face<FT> &fl, const Face<FT> &gl, double dt,
                                              FT *const theta[3], int i, int j,
-                                             unsigned long long *verify = nullptr)
+                                             unsigned long long *verify = nullptr, bool prechecks = true)
 {
     const CellFaces<FT, NP> cf(g, theta, i, j);
     const long long kf = kf_of(q, i, j), kw = cf.kw, kx = cf.kx, ky = cf.ky;
@@ -242,25 +242,36 @@ __device__ __forceinline__ double theta_body(const Grid &g, const Eos &e, const 
     FT rh[6], rl[6];
 #pragma unroll
     for (int c = C0; c < C1; ++c) {
-        rh[c] = (cf.xp(fh, fl, c) - cf.xm(fh, fl, c)) * idx + (cf.yp(gh, gl, c) - cf.ym(gh, gl, c)) * idy;
-        rl[c] = (fl.f[c][kw] - fl.f[c][kx]) * idx + (gl.f[c][kw] - gl.f[c][ky]) * idy;
+        rh[c] = div_sum(cf.xp(fh, fl, c) - cf.xm(fh, fl, c), idx, cf.yp(gh, gl, c) - cf.ym(gh, gl, c), idy);
+        rl[c] = div_sum(fl.f[c][kw] - fl.f[c][kx], idx, gl.f[c][kw] - gl.f[c][ky], idy);
         if (c == 5) {
-            FT a = FT(q.f[F_ALP][kf]);
-            rh[c] = rh[c] - a * (cf.xp(fh, fl, 6) - cf.xm(fh, fl, 6)) * idx - a * (cf.yp(gh, gl, 6) - cf.ym(gh, gl, 6)) * idy;
-            rl[c] = rl[c] - a * (fl.f[6][kw] - fl.f[6][kx]) * idx - a * (gl.f[6][kw] - gl.f[6][ky]) * idy;
+            FT a;
+            if constexpr (sizeof(FT) == 4) a = to_f32(q.f[F_ALP][kf]);
+            else a = q.f[F_ALP][kf];
+            rh[c] = rh[c] - src_term(a, cf.xp(fh, fl, 6) - cf.xm(fh, fl, 6), idx) -
+                    src_term(a, cf.yp(gh, gl, 6) - cf.ym(gh, gl, 6), idy);
+            rl[c] = rl[c] - src_term(a, fl.f[6][kw] - fl.f[6][kx], idx) - src_term(a, gl.f[6][kw] - gl.f[6][ky], idy);
         }
     }
     bool one = false;
     if constexpr (sizeof(FT) == 4) {
-        one = theta_one_f32<STAGE>(e, c32, kw, rh, rl, float(dt));
-        if (!VERIFY && one) return 1.0;
+        one = theta_one_f32<STAGE>(e, c32, kw, rh, rl, to_f32(dt));
+        if (!VERIFY && one && prechecks) return 1.0;
     }
     double l[6], h[6];
 #pragma unroll
     for (int c = C0; c < C1; ++c) {
         double qc = q.f[c][kf];
-        l[c] = qc - dt * double(rl[c]);
-        h[c] = qc - dt * double(rh[c]);
+        double rlc, rhc;
+        if constexpr (sizeof(FT) == 4) {
+            rlc = to_f64(rl[c]);
+            rhc = to_f64(rh[c]);
+        } else {
+            rlc = rl[c];
+            rhc = rh[c];
+        }
+        l[c] = __fma_rn(-dt, rlc, qc);
+        h[c] = __fma_rn(-dt, rhc, qc);
     }
     double th;
     if (STAGE == 2) {
@@ -299,6 +310,31 @@ __device__ __forceinline__ void blend_body(const Grid &g, const Face<FT> &fh, co
 // cons_to_prim_kernel (SC:840-864) + al_prim copy on every cell, then the dt candidate of
 // timestep_kernel (SC:1686-1705) -- each step selected by `flags`.
 // Returns the bit pattern of the cell's time-step candidate (all ones when it has none).
+// Binary32 pre-check of the combine's admissibility tests (precision form): true only when the
+// binary64 state Q certainly has finite components, partial densities at or above the 1e-10 floor,
+// alpha inside [1e-8, 1 - 1e-8] (so neither alpha clamp acts) and no energy repair
+// ((E - kin)(1 + Gamma) - Pi >= 1e-8 (1 + Gamma), enforce_admissible_kernel SC:918-958). Rounding
+// Q to binary32 moves each component by at most 2^-24 of it; the repair test's binary32 value is
+// within about 10 roundings (6e-7) of its magnitude, and the test demands 4e-6 of it. A true
+// result lets the caller skip those binary64 tests, whose outcome it has proved; the results are
+// the same bits.
+__device__ __forceinline__ bool cell_surely_admissible(const Eos &e, const double *Q)
+{
+    const float m1 = to_f32(Q[0]), m2 = to_f32(Q[1]), mx = to_f32(Q[2]), my = to_f32(Q[3]);
+    const float E = to_f32(Q[4]), a = to_f32(Q[5]);
+    if (!(isfinite(m1) && isfinite(m2) && isfinite(mx) && isfinite(my) && isfinite(E) && isfinite(a)))
+        return false;
+    const float lo = float(kPpRho) * 1.000001f;
+    if (!(m1 >= lo && m2 >= lo)) return false;
+    if (!(a >= float(kPrimAlphaFloor) * 1.000001f && 1.0f - a >= 5.0e-8f)) return false;
+    const float rho = m1 + m2, kin = 0.5f * (mx * mx + my * my) / rho;
+    const float a2 = 1.0f - a, gb = a * e.r1f + a2 * e.r2f, pb = a * e.k1f + a2 * e.k2f;
+    const float gp1 = 1.0f + gb;
+    const float v = (E - kin) * gp1 - pb - float(kPpCtilde) * gp1;
+    const float mag = (fabsf(E) + kin) * gp1 + fabsf(pb) + float(kPpCtilde) * gp1;
+    return v > 4.0e-6f * mag;
+}
+
 // NP: limiter passes whose blends are deferred (3 in the fused stage: the limited fluxes are rebuilt
 // from fh/gh, fl/gl and the three theta arrays; 0 when fh/gh already hold them).
 template <typename FT, int NP = 0>
@@ -329,27 +365,45 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
             if (dt_dev) dt = *dt_dev;
             const CellFaces<FT, NP> cf(g, theta, i, j);
             const FT idx = FT(g.inv_dx), idy = FT(g.inv_dy);
-            FT ap = FT(q.f[F_ALP][kf]);
+            FT ap;
+            if constexpr (sizeof(FT) == 4) ap = to_f32(q.f[F_ALP][kf]);
+            else ap = q.f[F_ALP][kf];
             FT res[6];
 #pragma unroll
             for (int c = 0; c < 5; ++c)
-                res[c] = (cf.xp(fh, fl, c) - cf.xm(fh, fl, c)) * idx + (cf.yp(gh, gl, c) - cf.ym(gh, gl, c)) * idy;
-            FT src6x = ap * (cf.xp(fh, fl, 6) - cf.xm(fh, fl, 6)) * idx;
-            FT src6y = ap * (cf.yp(gh, gl, 6) - cf.ym(gh, gl, 6)) * idy;
-            res[5] = (cf.xp(fh, fl, 5) - cf.xm(fh, fl, 5)) * idx + (cf.yp(gh, gl, 5) - cf.ym(gh, gl, 5)) * idy -
+                res[c] = div_sum(cf.xp(fh, fl, c) - cf.xm(fh, fl, c), idx, cf.yp(gh, gl, c) - cf.ym(gh, gl, c), idy);
+            FT src6x = src_term(ap, cf.xp(fh, fl, 6) - cf.xm(fh, fl, 6), idx);
+            FT src6y = src_term(ap, cf.yp(gh, gl, 6) - cf.ym(gh, gl, 6), idy);
+            res[5] = div_sum(cf.xp(fh, fl, 5) - cf.xm(fh, fl, 5), idx, cf.yp(gh, gl, 5) - cf.ym(gh, gl, 5), idy) -
                      src6x - src6y;
             long long ko = (long long)i * old.pitch + j;
 #pragma unroll
             for (int c = 0; c < 6; ++c) {
-                double base = beta * (Q[c] - dt * double(res[c]));
-                Q[c] = (flags & FIN_OLD_READ) ? alpha * old.f[c][ko] + base : base;
+                double rc;
+                if constexpr (sizeof(FT) == 4) rc = to_f64(res[c]);
+                else rc = res[c];
+                double base = __dmul_rn(beta, __fma_rn(-dt, rc, Q[c]));
+                Q[c] = (flags & FIN_OLD_READ) ? __fma_rn(alpha, old.f[c][ko], base) : base;
             }
             wrote_q = true;
         }
         // 1/(rho Gamma) of the admissibility check, reused by the primitive recovery when alpha
         // is unchanged by the second clamp
         double rg_a1 = -1.0, rg_rho = 0.0, rg_inv = 0.0, rg_gb = 0.0, rg_pb = 0.0;
-        if (flags & FIN_ADMISSIBLE) {
+        // Precision form: a binary32 pre-check proves most cells need no clamp, floor, NaN
+        // handling or repair; they skip those binary64 tests (the recovery is unchanged)
+        bool fast = false;
+        if constexpr (sizeof(FT) == 4) {
+            if ((flags & FIN_ADMISSIBLE) && (flags & FIN_PRIM) && !(flags & FIN_EXACT_CHECKS))
+                fast = cell_surely_admissible(e, Q);
+        }
+        if ((flags & FIN_ADMISSIBLE) && fast) {
+            const double a1 = Q[F_AL], rho = Q[0] + Q[1];
+            double gb, pb;
+            mix_gamma_pibig(e, a1, gb, pb);
+            rg_a1 = a1; rg_rho = rho; rg_inv = 1.0 / (rho * gb); rg_gb = gb; rg_pb = pb;
+            wrote_q = true;
+        } else if (flags & FIN_ADMISSIBLE) {
             double a1 = clamp01_pp(Q[F_AL]);
             double m1 = Q[0], m2 = Q[1], mx = Q[2], my = Q[3], E = Q[4];
             bool nonfinite = isnan(m1) || isnan(m2) || isnan(mx) || isnan(my) || isnan(E);
@@ -389,12 +443,14 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
         }
         if (flags & FIN_PRIM) {
             double a1 = Q[F_AL];
-            if (a1 < kPrimAlphaFloor) a1 = kPrimAlphaFloor;
-            if (a1 > 1.0 - kPrimAlphaFloor) a1 = 1.0 - kPrimAlphaFloor;
+            if (!fast) {
+                if (a1 < kPrimAlphaFloor) a1 = kPrimAlphaFloor;
+                if (a1 > 1.0 - kPrimAlphaFloor) a1 = 1.0 - kPrimAlphaFloor;
+            }
             Q[F_AL] = a1;
             double rho = Q[0] + Q[1];
             double gb, pb, inv;
-            if (a1 == rg_a1 && rho == rg_rho) {
+            if (fast || (a1 == rg_a1 && rho == rg_rho)) {
                 gb = rg_gb; pb = rg_pb; inv = rg_inv;
             } else {
                 mix_gamma_pibig(e, a1, gb, pb);
@@ -414,12 +470,12 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
                     // cancels for p near -p_inf) in binary64, the rest of the CFL candidate in
                     // binary32 with one division: sx sy / (sx + sy) = dx dy / (dy a + dx b),
                     // a = |u| + c, b = |v| + c.
-                    float c2 = float(((1.0 + gb) * pp + pb) * inv);
+                    float c2 = to_f32(((1.0 + gb) * pp + pb) * inv);
                     if (c2 < float(kTiny)) c2 = float(kTiny);
                     const float c = sqrtf(c2);
-                    const float a = fabsf(float(uu)) + c, b = fabsf(float(vv)) + c;
-                    const float dxf = float(g.dx), dyf = float(g.dy);
-                    const double d = double((dxf * dyf) / (dyf * a + dxf * b));
+                    const float a = fabsf(to_f32(uu)) + c, b = fabsf(to_f32(vv)) + c;
+                    const float dxf = to_f32(g.dx), dyf = to_f32(g.dy);
+                    const double d = to_f64((dxf * dyf) / (dyf * a + dxf * b));
                     dt_bits = (unsigned long long)__double_as_longlong(d);
                 } else {
                     double c = sound_speed_r(e, ir, pp, a1);
@@ -447,17 +503,17 @@ __device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const F
     long long kf = kf_of(q, i, j), kw = kw_of(g, i, j);
     const double ar1 = q.f[F_AR1][kf], ar2 = q.f[F_AR2][kf], ru = q.f[F_RU][kf], rv = q.f[F_RV][kf];
     const double pp = q.f[F_P][kf], al = q.f[F_AL][kf];
-    const float ar1f = float(ar1), ar2f = float(ar2), ruf = float(ru), rvf = float(rv);
-    const float pf = float(pp), alf = float(al);
+    const float ar1f = to_f32(ar1), ar2f = to_f32(ar2), ruf = to_f32(ru), rvf = to_f32(rv);
+    const float pf = to_f32(pp), alf = to_f32(al);
     c.ar1[kw] = ar1f;
     c.ar2[kw] = ar2f;
     c.ru[kw] = ruf;
     c.rv[kw] = rvf;
     c.p[kw] = pf;
     c.al[kw] = alf;
-    c.u[kw] = float(q.f[F_U][kf]);
-    c.v[kw] = float(q.f[F_V][kf]);
-    c.E[kw] = float(q.f[F_E][kf]);
+    c.u[kw] = to_f32(q.f[F_U][kf]);
+    c.v[kw] = to_f32(q.f[F_V][kf]);
+    c.E[kw] = to_f32(q.f[F_E][kf]);
 
     float ge, pie;
     mix_gamma_pinf(e, alf, ge, pie);
@@ -480,11 +536,11 @@ __device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const F
     }
     // the numerator cancels for p near -p_inf and stays binary64; the quotient and root do not
     const float rhof = ar1f + ar2f;
-    float val = float(gp1 * pl + pb) / (float(gb) * float(rho));
+    float val = to_f32(gp1 * pl + pb) / (to_f32(gb) * to_f32(rho));
     if (val < float(kTiny)) val = float(kTiny);
     const float irf = 1.0f / rhof;
     const float u = ruf * irf, v = rvf * irf;
-    const float af = float(a), plf = float(pl);
+    const float af = to_f32(a), plf = to_f32(pl);
     p.lu[kw] = u;
     p.lv[kw] = v;
     p.lp[kw] = plf;

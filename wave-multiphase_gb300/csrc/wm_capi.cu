@@ -105,6 +105,7 @@ struct wm_handle {
     long long steps = 0;
     bool fluxes_ready = false, low_ready = false;
     bool defer_limiter = false;  // fused stage: limiter blends rebuilt in registers (wm_set_limiter_sweeps)
+    bool prechecks = true;       // precision form: binary32 pre-checks of binary64 tests (wm_set_prechecks)
     // device-side time loop (wm_run): clock block, graph with a conditional while node
     struct RunClock *clock = nullptr;
     cudaGraph_t run_graph = nullptr;
@@ -408,7 +409,7 @@ int wm_limit_fluxes(wm_handle *h, const wm_fields *q, double dt, void *stream)
     if (!h->fluxes_ready || !h->low_ready) return WM_ERR_STATE;
     if (h->fp32)
         launch_limiter(h->g, h->e, to_fields(q), h->cells32, h->fh32, h->gh32, h->fl32, h->gl32, h->theta32, dt,
-                       nullptr, h->cnt, false, as_stream(stream));
+                       nullptr, h->cnt, false, as_stream(stream), nullptr, h->prechecks);
     else
         launch_limiter(h->g, h->e, to_fields(q), Cells32{}, h->fh, h->gh, h->fl, h->gl, h->theta, dt, nullptr,
                        h->cnt, false, as_stream(stream));
@@ -513,12 +514,13 @@ static int run_stage(wm_handle *h, const Fields &F, const Fields &O, double dt, 
         ProfScope ps(h, WM_PROF_LIMITER, h->defer_limiter ? 3 : 6, s);
         if (h->fp32)
             launch_limiter(h->g, h->e, F, h->cells32, h->fh32, h->gh32, h->fl32, h->gl32, h->theta32, dt, dt_dev,
-                           h->cnt, h->defer_limiter, s);
+                           h->cnt, h->defer_limiter, s, nullptr, h->prechecks);
         else
             launch_limiter(h->g, h->e, F, Cells32{}, h->fh, h->gh, h->fl, h->gl, h->theta, dt, dt_dev, h->cnt,
                            h->defer_limiter, s);
     }
     unsigned flags = final_flags(h, alpha);
+    if (!h->prechecks) flags |= FIN_EXACT_CHECKS;
     if (save_old) flags |= FIN_SAVE_OLD;
     {
         ProfScope ps(h, WM_PROF_FINAL, want_dt ? 2 : 1, s);
@@ -797,6 +799,14 @@ int wm_verify_limiter_precheck(wm_handle *h, const wm_fields *q, double dt, long
     }
     *decided = (long long)host[0];
     *disagreed = (long long)host[1];
+    return WM_OK;
+}
+
+int wm_set_prechecks(wm_handle *h, int on)
+{
+    if (!h) return WM_ERR_INVALID;
+    if ((on != 0) != h->prechecks) drop_run_graph(h);
+    h->prechecks = on != 0;
     return WM_OK;
 }
 

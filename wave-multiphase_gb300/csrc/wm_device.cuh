@@ -64,6 +64,37 @@ constexpr double kSigmaSmooth = 0.01;
 constexpr double kPrimAlphaFloor = 1.0e-8;  // cons_to_prim clamp (SC:852-853)
 
 // Warp's float builtins: min/max as a<b?a:b / a>b?a:b; sign(x) = x<0 ? -1 : +1.
+// binary64 <-> binary32 conversions on the integer pipe. GB300 issues the hardware conversions on
+// its narrow binary64 pipe (about 17 clocks a warp); these take about 4. Both give the IEEE 754
+// round-to-nearest-even result bit for bit: to_f32 keeps the top 23 fraction bits and rounds at bit
+// 28 of the low word (ties to the even significand; a carry into the exponent is the correct
+// rounding, up to infinity), to_f64 widens exactly; zeros, subnormals, results outside binary32's
+// normal range, infinities and NaN take the hardware instruction.
+__device__ __forceinline__ float to_f32(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const int e = (int)((hi >> 20) & 0x7ffu);  // binary64 biased exponent
+    if (e >= 897 && e <= 1150) {              // binary32 biased exponent e - 896 in [1, 254]
+        const unsigned f = ((hi & 0xfffffu) << 3) | (lo >> 29);
+        const unsigned r = lo & 0x1fffffffu;
+        unsigned bits = (hi & 0x80000000u) | ((unsigned)(e - 896) << 23) | f;
+        bits += (r > 0x10000000u || (r == 0x10000000u && (f & 1u))) ? 1u : 0u;
+        return __uint_as_float(bits);
+    }
+    return __double2float_rn(x);
+}
+__device__ __forceinline__ double to_f64(float x)
+{
+    const unsigned b = __float_as_uint(x);
+    const unsigned e = (b >> 23) & 0xffu;
+    if (e != 0u && e != 0xffu) {
+        const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+        return __hiloint2double((int)hi, (int)(b << 29));
+    }
+    return (double)x;
+}
+
 template <typename T> __device__ __forceinline__ T wmin(T a, T b) { return a < b ? a : b; }
 template <typename T> __device__ __forceinline__ T wmax(T a, T b) { return a > b ? a : b; }
 template <typename T> __device__ __forceinline__ T wsign(T x) { return x < T(0) ? T(-1) : T(1); }
@@ -552,11 +583,28 @@ __device__ __forceinline__ void hllc(const Side<T> &L, const Side<T> &R, T f[6],
 // SC:1506-1512). Shared by the in-place limiter and the fused stage so both round alike.
 __device__ __forceinline__ double face_blend(double low, double high, double theta)
 {
-    return low + theta * (high - low);
+    return __fma_rn(theta, high - low, low);
 }
 __device__ __forceinline__ float face_blend(float low, float high, float theta)
 {
-    return low + theta * (high - low);
+    return __fmaf_rn(theta, high - low, low);
 }
+
+// Flux difference terms with their rounding pinned (explicit fused multiply-add and products, which
+// the compiler does not re-associate or contract): every kernel that forms a residual or a limiter
+// state -- in-place or rebuilt blends, per-solve or batched -- rounds it the same way.
+__device__ __forceinline__ double div_sum(double dfx, double idx, double dgy, double idy)
+{
+    return __fma_rn(dfx, idx, __dmul_rn(dgy, idy));  // dfx / dx + dgy / dy
+}
+__device__ __forceinline__ float div_sum(float dfx, float idx, float dgy, float idy)
+{
+    return __fmaf_rn(dfx, idx, __fmul_rn(dgy, idy));
+}
+__device__ __forceinline__ double src_term(double a, double d, double id)
+{
+    return __dmul_rn(__dmul_rn(a, d), id);  // a * d / dx
+}
+__device__ __forceinline__ float src_term(float a, float d, float id) { return __fmul_rn(__fmul_rn(a, d), id); }
 
 }  // namespace wm

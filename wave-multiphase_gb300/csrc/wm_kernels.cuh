@@ -54,6 +54,7 @@ enum : unsigned {
     FIN_SAVE_OLD = 8u,    // copy the pre-update interior state to q_old (copy_old fused)
     FIN_DT = 16u,         // accumulate the time-step candidate of interior cells
     FIN_OLD_READ = 32u,   // rk3 reads q_old (alpha != 0)
+    FIN_EXACT_CHECKS = 64u,  // precision form: no binary32 pre-check of the admissibility tests
 };
 
 void launch_bc(const Grid &g, const int bc[4], const Fields &q, const Fields *save_old,
@@ -71,7 +72,8 @@ template <typename FT>
 void launch_limiter(const Grid &g, const Eos &e, const Fields &q, const Cells32 &c32, const Face<FT> &fh,
                     const Face<FT> &gh, const Face<FT> &fl, const Face<FT> &gl,
                     FT *const theta[3], double dt, const double *dt_dev, const Counters &cnt,
-                    bool deferred, cudaStream_t s, unsigned long long *verify = nullptr);
+                    bool deferred, cudaStream_t s, unsigned long long *verify = nullptr,
+                    bool prechecks = true);
 template <typename FT>
 void launch_final(const Grid &g, const Eos &e, unsigned flags, const Fields &q, const Fields &old,
                   const Face<FT> &fh, const Face<FT> &gh, const Face<FT> &fl, const Face<FT> &gl,

@@ -19,6 +19,7 @@
 #include <cstdio>
 
 #include "../../include/wavemp.h"
+#include "wm_device.cuh"
 
 namespace wm {
 void set_error_text(const char *msg);
@@ -98,7 +99,48 @@ __global__ void grad_kernel(const double *rho, int nx, int ny, Axis X, Axis Y, c
     pa[0] = pa[1] = pa[2] = grey;
 }
 
+// to_f32 / to_f64 against the hardware conversions, bit for bit (NaN: both NaN).
+__global__ void conv_check_kernel(const unsigned long long *in, long long n, unsigned long long *bad)
+{
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const double x = __longlong_as_double((long long)in[k]);
+        const float a = wm::to_f32(x), b = __double2float_rn(x);
+        const bool same32 = __float_as_uint(a) == __float_as_uint(b) || (a != a && b != b);
+        const float y = __uint_as_float((unsigned)in[k]);
+        const double c = wm::to_f64(y), d = (double)y;
+        const bool same64 = __double_as_longlong(c) == __double_as_longlong(d) || (c != c && d != d);
+        if (!same32) atomicAdd(&bad[0], 1ull);
+        if (!same64) atomicAdd(&bad[1], 1ull);
+    }
+}
+
 }  // namespace
+
+extern "C" int wm_check_conversions(const unsigned long long *bits, long long n, long long *bad_f32,
+                                    long long *bad_f64, void *stream)
+{
+    if (!bits || n < 0 || !bad_f32 || !bad_f64) return WM_ERR_INVALID;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    unsigned long long *ctr = nullptr, host[2] = {0, 0};
+    cudaError_t e = cudaMalloc(&ctr, sizeof host);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctr, 0, sizeof host, s);
+    if (e == cudaSuccess && n > 0) {
+        conv_check_kernel<<<1024, 256, 0, s>>>(bits, n, ctr);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host, ctr, sizeof host, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(ctr);
+    if (e != cudaSuccess) {
+        char msg[200];
+        snprintf(msg, sizeof msg, "wm_check_conversions: %s", cudaGetErrorString(e));
+        wm::set_error_text(msg);
+        return WM_ERR_CUDA;
+    }
+    *bad_f32 = (long long)host[0];
+    *bad_f64 = (long long)host[1];
+    return WM_OK;
+}
 
 extern "C" int wm_schlieren(const wm_fields *q, int nx, int ny, int g, const double *xh, const double *yh,
                             double x_h0, double y_h0, double *rho_scratch, double *grad,

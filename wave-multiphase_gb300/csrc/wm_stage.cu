@@ -89,13 +89,14 @@ template <int STAGE, typename FT, int NP, int VERIFY = 0>
 __global__ void __launch_bounds__(BX *BY)
 theta_kernel(Grid g, Eos e, Fields q, Cells32 c32, Face<FT> fh, Face<FT> gh, Face<FT> fl, Face<FT> gl,
              Theta3<FT> th3, double dt, const double *dt_dev, unsigned long long *limited,
-             unsigned long long *verify)
+             unsigned long long *verify, int prechecks)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x + g.g;
     int i = blockIdx.y * blockDim.y + threadIdx.y + g.g;
     if (i >= g.g + g.nx || j >= g.g + g.ny) return;
     if (dt_dev) dt = *dt_dev;
-    double th = theta_body<STAGE, FT, NP, VERIFY>(g, e, q, c32, fh, gh, fl, gl, dt, th3.t, i, j, verify);
+    double th = theta_body<STAGE, FT, NP, VERIFY>(g, e, q, c32, fh, gh, fl, gl, dt, th3.t, i, j, verify,
+                                                  prechecks != 0);
     th3.t[STAGE][kw_of(g, i, j)] = FT(th);
     if (limited) count_if(limited, th < 1.0);
 }
@@ -227,30 +228,31 @@ template <typename FT>
 void launch_limiter(const Grid &g, const Eos &e, const Fields &q, const Cells32 &c32, const Face<FT> &fh,
                     const Face<FT> &gh, const Face<FT> &fl, const Face<FT> &gl,
                     FT *const theta[3], double dt, const double *dt_dev, const Counters &cnt,
-                    bool deferred, cudaStream_t s, unsigned long long *verify)
+                    bool deferred, cudaStream_t s, unsigned long long *verify, bool prechecks)
 {
     const dim3 gt = grid2(g.ny, g.nx), gb = grid2(g.ny + 1, g.nx + 1), bl(BX, BY);
     const Theta3<FT> t3{{theta[0], theta[1], theta[2]}};
+    const int pc = prechecks ? 1 : 0;
     if (verify) {  // diagnostic: in-place blends, pre-check and binary64 solve both evaluated
-        theta_kernel<0, FT, 0, 1><<<gt, bl, 0, s>>>(g, e, q, c32, fh, gh, fl, gl, t3, dt, dt_dev, nullptr, verify);
+        theta_kernel<0, FT, 0, 1><<<gt, bl, 0, s>>>(g, e, q, c32, fh, gh, fl, gl, t3, dt, dt_dev, nullptr, verify, pc);
         blend_kernel<FT><<<gb, bl, 0, s>>>(g, fh, gh, fl, gl, theta[0]);
-        theta_kernel<1, FT, 0, 1><<<gt, bl, 0, s>>>(g, e, q, c32, fh, gh, fl, gl, t3, dt, dt_dev, nullptr, verify);
+        theta_kernel<1, FT, 0, 1><<<gt, bl, 0, s>>>(g, e, q, c32, fh, gh, fl, gl, t3, dt, dt_dev, nullptr, verify, pc);
         blend_kernel<FT><<<gb, bl, 0, s>>>(g, fh, gh, fl, gl, theta[1]);
-        theta_kernel<2, FT, 0, 1><<<gt, bl, 0, s>>>(g, e, q, c32, fh, gh, fl, gl, t3, dt, dt_dev, nullptr, verify);
+        theta_kernel<2, FT, 0, 1><<<gt, bl, 0, s>>>(g, e, q, c32, fh, gh, fl, gl, t3, dt, dt_dev, nullptr, verify, pc);
         blend_kernel<FT><<<gb, bl, 0, s>>>(g, fh, gh, fl, gl, theta[2]);
         return;
     }
     if (deferred) {  // blends rebuilt by the next pass and by the combine
-        theta_kernel<0, FT, 0><<<gt, bl, 0, s>>>(g, e, q, c32, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited, nullptr);
-        theta_kernel<1, FT, 1><<<gt, bl, 0, s>>>(g, e, q, c32, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited, nullptr);
-        theta_kernel<2, FT, 2><<<gt, bl, 0, s>>>(g, e, q, c32, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited, nullptr);
+        theta_kernel<0, FT, 0><<<gt, bl, 0, s>>>(g, e, q, c32, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited, nullptr, pc);
+        theta_kernel<1, FT, 1><<<gt, bl, 0, s>>>(g, e, q, c32, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited, nullptr, pc);
+        theta_kernel<2, FT, 2><<<gt, bl, 0, s>>>(g, e, q, c32, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited, nullptr, pc);
         return;
     }
-    theta_kernel<0, FT, 0><<<gt, bl, 0, s>>>(g, e, q, c32, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited, nullptr);
+    theta_kernel<0, FT, 0><<<gt, bl, 0, s>>>(g, e, q, c32, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited, nullptr, pc);
     blend_kernel<FT><<<gb, bl, 0, s>>>(g, fh, gh, fl, gl, theta[0]);
-    theta_kernel<1, FT, 0><<<gt, bl, 0, s>>>(g, e, q, c32, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited, nullptr);
+    theta_kernel<1, FT, 0><<<gt, bl, 0, s>>>(g, e, q, c32, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited, nullptr, pc);
     blend_kernel<FT><<<gb, bl, 0, s>>>(g, fh, gh, fl, gl, theta[1]);
-    theta_kernel<2, FT, 0><<<gt, bl, 0, s>>>(g, e, q, c32, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited, nullptr);
+    theta_kernel<2, FT, 0><<<gt, bl, 0, s>>>(g, e, q, c32, fh, gh, fl, gl, t3, dt, dt_dev, cnt.limited, nullptr, pc);
     blend_kernel<FT><<<gb, bl, 0, s>>>(g, fh, gh, fl, gl, theta[2]);
 }
 
@@ -272,11 +274,11 @@ void launch_final(const Grid &g, const Eos &e, unsigned flags, const Fields &q, 
 template void launch_limiter<double>(const Grid &, const Eos &, const Fields &, const Cells32 &,
                                      const Face<double> &, const Face<double> &, const Face<double> &,
                                      const Face<double> &, double *const[3], double, const double *,
-                                     const Counters &, bool, cudaStream_t, unsigned long long *);
+                                     const Counters &, bool, cudaStream_t, unsigned long long *, bool);
 template void launch_limiter<float>(const Grid &, const Eos &, const Fields &, const Cells32 &,
                                     const Face<float> &, const Face<float> &, const Face<float> &,
                                     const Face<float> &, float *const[3], double, const double *,
-                                    const Counters &, bool, cudaStream_t, unsigned long long *);
+                                    const Counters &, bool, cudaStream_t, unsigned long long *, bool);
 template void launch_final<double>(const Grid &, const Eos &, unsigned, const Fields &, const Fields &,
                                    const Face<double> &, const Face<double> &, const Face<double> &,
                                    const Face<double> &, double *const[3], bool, double, const double *,

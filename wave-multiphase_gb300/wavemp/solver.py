@@ -216,6 +216,11 @@ class Solver:
                    "verify_limiter_precheck")
         return a.value, b.value
 
+    def set_prechecks(self, on: bool):
+        """Precision form: binary32 pre-checks that skip binary64 tests they decide (default on;
+        the results are the same bits either way)."""
+        _lib.check(self.L.wm_set_prechecks(self._h, int(bool(on))), "set_prechecks")
+
     def set_limiter_sweeps(self, in_place: bool):
         """Fused stage: blend sweeps in place (the reference's form; default of the binary64
         form) or rebuilt in registers by the next pass and the combine (bit-identical; default of
