@@ -25,6 +25,7 @@ NVIDIA Warp, which is not installable here) and prints its line with "impl": "re
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import statistics
@@ -60,13 +61,15 @@ def params(nx=None, ny=None, precision="fp64"):
 LIMITER_IN_PLACE = None  # the per-solve fused stage's limiter form (--limiter; None: the default)
 
 
-def time_form(precision, steps, warmup, dev):
+def time_form(precision, steps, warmup, dev, fp64_switches=False):
     """Device-timed steps of one form on the workload; returns (ms, kernel-group profile)."""
     import torch
 
     import wavemp
 
-    s = wavemp.Solver(params(precision=precision), NX, NY)
+    p = params(precision=precision)
+    p.fp64_switches = fp64_switches
+    s = wavemp.Solver(p, NX, NY)
     if LIMITER_IN_PLACE is not None:
         s.set_limiter_sweeps(LIMITER_IN_PLACE)
     q = wavemp.ic.triple_point(NX, NY, device=dev)
@@ -198,7 +201,7 @@ def precision_m10(dev, steps, nx=4096, ny=2048):
     return out
 
 
-def batched_form(dev, steps, warmup, n=64):
+def batched_form(dev, steps, warmup, n=64, sensitivity_eps=0.0):
     """Batched form on the batched workload (64 shock-droplet solves, grids log-uniform 128x64 to
     1024x512, seed 0): `steps` SSP-RK3 steps of every solve in persistent launches, binary64 and
     binary32 forms after the tile-shape autotuner, against the same solves stepped one after the
@@ -216,8 +219,13 @@ def batched_form(dev, steps, warmup, n=64):
     # the binary64 batch records every solve's dt sequence; the binary32 batch replays it, so
     # that the two differ by their arithmetic alone (not by a drift of their time steps)
     logs = [torch.zeros(warmup + steps + 8, dtype=torch.float64, device=dev) for _ in specs]
-    for prec in ("fp64", "fp32"):
-        b = Batch(n, precision=prec, device=dev)
+
+    def density_l1(qa, qb):
+        ra, rb = (qa["ar1"] + qa["ar2"])[5:-5, 5:-5], (qb["ar1"] + qb["ar2"])[5:-5, 5:-5]
+        return float((ra - rb).abs().sum() / rb.abs().sum())
+
+    for prec in ("fp64", "fp32", "fp32_switches64"):
+        b = Batch(n, precision=prec[:4], device=dev, fp64_switches=prec.endswith("switches64"))
         for sp, log in zip(specs, logs):
             b.add(sp, dt_log=log, dt_mode="record" if prec == "fp64" else "replay")
         t0 = time.perf_counter()
@@ -250,13 +258,50 @@ def batched_form(dev, steps, warmup, n=64):
         batches[prec] = b
         if prec == "fp32":
             shapes32 = {c: int(v[0]) for c, v in report.items()}
+        if prec != "fp64":
+            l1 = [density_l1(b.slots[k]["q"], batches["fp64"].slots[k]["q"]) for k in range(n)]
+            num = den = 0.0
+            for k in range(n):
+                qa, qb = b.slots[k]["q"], batches["fp64"].slots[k]["q"]
+                ra, rb = (qa["ar1"] + qa["ar2"])[5:-5, 5:-5], (qb["ar1"] + qb["ar2"])[5:-5, 5:-5]
+                num += float((ra - rb).abs().sum())
+                den += float(rb.abs().sum())
+            out[prec]["density_l1_vs_fp64"] = {"max": max(l1), "median": float(sorted(l1)[len(l1) // 2]),
+                                              "solves_within_1e-5": sum(v <= 1e-5 for v in l1),
+                                              "all_solves_together": num / den}
+            if prec == "fp32_switches64":  # its memory back before the serial comparison
+                b.close()
+                del batches[prec]
     # density L1 of the binary32 batch against the binary64 batch after the same number of steps
-    l1 = []
-    for k in range(n):
-        a, c = batches["fp32"].slots[k]["q"], batches["fp64"].slots[k]["q"]
-        ra, rc = (a["ar1"] + a["ar2"])[5:-5, 5:-5], (c["ar1"] + c["ar2"])[5:-5, 5:-5]
-        l1.append(float((ra - rc).abs().sum() / rc.abs().sum()))
+    l1 = [density_l1(batches["fp32"].slots[k]["q"], batches["fp64"].slots[k]["q"]) for k in range(n)]
     worst = max(l1)
+    sensitivity = None
+    if sensitivity_eps:
+        # conditioning of the solves themselves: the binary64 batch again, from initial partial
+        # densities perturbed by a relative sensitivity_eps (seeded), on the same dt sequence
+        def perturbed(sp, k):
+            def make():
+                st = sp.make_state()
+                gen = torch.Generator().manual_seed(1000 + k)
+                noise = torch.randn(tuple(st["ar1"].shape), generator=gen, dtype=torch.float64)
+                st["ar1"] = st["ar1"] * (1.0 + sensitivity_eps * noise.to(st["ar1"].device))
+                return st
+            return dataclasses.replace(sp, state=None, make_state=make)
+
+        bp = Batch(n, precision="fp64", device=dev)
+        for k, (sp, log) in enumerate(zip(specs, logs)):
+            bp.add(perturbed(sp, k), dt_log=log, dt_mode="replay")
+        bp.run(warmup + steps + 2)
+        torch.cuda.synchronize()
+        l1p = [density_l1(bp.slots[k]["q"], batches["fp64"].slots[k]["q"]) for k in range(n)]
+        bp.close()
+        order = sorted(range(n), key=lambda k: -l1[k])[:4]
+        sensitivity = {"relative_perturbation": sensitivity_eps,
+                       "density_l1_fp64_perturbed_vs_fp64_max": max(l1p),
+                       "density_l1_fp64_perturbed_vs_fp64_median": float(sorted(l1p)[len(l1p) // 2]),
+                       "largest_fp32_errors_with_their_fp64_sensitivity":
+                           [{"solve": k, "grid": f"{specs[k].nx}x{specs[k].ny}", "fp32_vs_fp64": l1[k],
+                             "fp64_perturbed_vs_fp64": l1p[k]} for k in order]}
     for b in batches.values():
         b.close()
     del batches
@@ -287,6 +332,7 @@ def batched_form(dev, steps, warmup, n=64):
         "workload": f"{n} shock-droplet solves, grids log-uniform 128x64..1024x512 (seed 0), "
                     f"{cells} cells in all; {steps} steps timed after {warmup} warm-up",
         "batched_fp64": out["fp64"], "batched_fp32": out["fp32"],
+        "batched_fp32_switches64": out["fp32_switches64"],
         "serial_plain_fp64": {"value": round(serial, 3), "unit": "Mcell-stage/s",
                               "ms_per_step": round(total_ms / steps, 3)},
         "speedup_fp32_vs_serial_plain": round(out["fp32"]["value"] / serial, 3),
@@ -296,6 +342,8 @@ def batched_form(dev, steps, warmup, n=64):
         "solves_within_1e-5": sum(v <= 1e-5 for v in l1),
         "error_note": "the binary32 batch replays the binary64 batch's dt sequence",
     }
+    if sensitivity is not None:
+        summary["conditioning"] = sensitivity
     return summary, shapes32
 
 
@@ -518,7 +566,7 @@ def run_ours(args):
             res = precision_m10(dev, args.m10_steps)
             value = res["fp32"]["value"]
         elif args.form == "batched":
-            res, _ = batched_form(dev, args.batch_steps, args.warmup)
+            res, _ = batched_form(dev, args.batch_steps, args.warmup, sensitivity_eps=args.batch_sensitivity)
             value = res["batched_fp32"]["value"]
         else:
             res = served_form(dev, args.serve_requests, capacity=args.serve_slots, chunk_steps=args.serve_chunk)
@@ -660,6 +708,13 @@ def run_ours(args):
     line["forms"]["batched"] = batched
     line["forms"]["served"] = served_form(dev, args.serve_requests, shapes=shapes32,
                                           capacity=args.serve_slots, chunk_steps=args.serve_chunk)
+    ms32s, _, finite32s = time_form("fp32", args.steps, args.warmup, dev, fp64_switches=True)
+    ms32s = max_over_ranks(ms32s, world, dev)
+    v32s = whole_job_rate(cells, args.steps, world, ms32s)
+    line["forms"]["precision_fp32_switches64"] = {
+        "value": round(v32s, 3), "unit": "Mcell-stage/s", "speedup_vs_plain": round(v32s / value, 3),
+        "finite": finite32s,
+        "note": "binary32 form with the THINC indicator and Ducros sensor from binary64 entropies / primitives"}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         os.environ.setdefault("OMP_NUM_THREADS", str(cores))
@@ -689,6 +744,8 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=20,
                     help="steps of the 64-solve batched workload (300 is the full workload)")
     ap.add_argument("--serve-requests", type=int, default=24, help="requests of the serving workload")
+    ap.add_argument("--batch-sensitivity", type=float, default=0.0,
+                    help="also run the binary64 batch from initial states perturbed by this relative amount")
     ap.add_argument("--m10-steps", type=int, default=500, help="steps of the Mach-10 precision run")
     ap.add_argument("--limiter", choices=("default", "in-place", "deferred"), default="default",
                     help="per-solve fused stage: blend sweeps in place or rebuilt in registers")

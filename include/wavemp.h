@@ -65,6 +65,11 @@ typedef struct wm_params {
     int bc[4];            /* x-low, x-high, y-low, y-high: WM_BC_* */
     int emergency_repair; /* USE_EMERGENCY_REPAIR (SC:37): run enforce_admissible every stage */
     int precision;        /* WM_PREC_* */
+    int fp64_switches;    /* WM_PREC_FP32 only: the scheme's two discontinuous switches -- the THINC
+                             smoothness indicator (SC:1028-1032) and the Ducros shear sensor
+                             (SC:1035-1036) -- from binary64 entropies and primitives, so that the
+                             binary32 sweep takes the binary64 decisions (costs one binary64 pow a
+                             cell); 0: binary32 sensors */
 } wm_params;
 
 /* The reference's ten per-cell arrays (SC:1839-1841): conserved state, primitives, al_prim. */
@@ -208,6 +213,7 @@ typedef struct wm_batch_params {
     double cfl;
     int tile_shape; /* -1: per grid-size class (wm_batch_tile_shape; 32-wide tiles by default),
                        0..3: every grid in tiles of 1x128, 2x64, 4x32 or 8x16 cells */
+    int fp64_switches; /* as in wm_params */
 } wm_batch_params;
 typedef struct wm_solve_desc {
     int nx, ny;
@@ -268,12 +274,13 @@ int wm_schlieren(const wm_fields *q, int nx, int ny, int g, const double *xh, co
                  void *stream);
 
 /* ---- diagnostics ---------------------------------------------------------------------------- */
-/* The precision form's integer-pipe binary64 -> binary32 and binary32 -> binary64 conversions
- * against the hardware ones on n device bit patterns (each read as a binary64 and, by its low 32
- * bits, as a binary32): the numbers of results that differ (0 expected; NaN counts as equal to
- * NaN). No counterpart in the reference. */
+/* The integer-pipe binary64 -> binary32 and binary32 -> binary64 conversions and binary64
+ * compares / min / max / sign against the hardware ones on n device bit patterns (each read as a
+ * binary64, paired with the next one for the compares, and by its low 32 bits as a binary32): the
+ * numbers of results that differ (0 expected; NaN counts as equal to NaN). No counterpart in the
+ * reference. */
 int wm_check_conversions(const unsigned long long *bits, long long n, long long *bad_f32,
-                         long long *bad_f64, void *stream);
+                         long long *bad_f64, long long *bad_cmp, void *stream);
 /* Copy workspace array `which` (WM_WS_*) of the padded grid into the caller's device buffer dst
  * (same padded shape, contiguous rows of ny + 2g). */
 #define WM_WS_FX 0      /* 7 arrays: high-order x fluxes 0..5 and srcx (after limit_fluxes: blended) */

@@ -24,9 +24,9 @@ def spec(nx, ny, mach=2.4, **kw):
                      state=ic.shock_droplet(nx, ny, 1.0, 0.5, mach=mach), **kw)
 
 
-def alone(sp: SolveSpec, steps, precision, recon="mp5c6", variant="sc"):
+def alone(sp: SolveSpec, steps, precision, recon="mp5c6", variant="sc", fp64_switches=False):
     p = SolverParams(dx=sp.dx, dy=sp.dy, gamma1=sp.gamma1, pinf1=sp.pinf1, bc=sp.bc,
-                     precision=precision, recon=recon, variant=variant)
+                     precision=precision, recon=recon, variant=variant, fp64_switches=fp64_switches)
     s = Solver(p, sp.nx, sp.ny)
     q = {k: v.clone() for k, v in sp.state.items()}
     old = alloc_state(sp.nx, sp.ny, names=wavemp.FIELDS)
@@ -57,11 +57,12 @@ def compare(q_batch, q_alone, what, precision="fp64"):
     return all(np.array_equal(got[k], ref[k], equal_nan=True) for k in pu.ALL)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_batch_matches_solves_run_alone(precision):
+@pytest.mark.parametrize("form", ["fp64", "fp32", "fp32+switches64"])
+def test_batch_matches_solves_run_alone(form):
     steps = 3
+    precision, sw = form.split("+")[0], form.endswith("switches64")
     specs = [spec(nx, ny, max_steps=steps) for nx, ny in SIZES]
-    b = Batch(len(specs) + 2, precision=precision)
+    b = Batch(len(specs) + 2, precision=precision, fp64_switches=sw)
     for sp in specs:
         b.add(sp)
     b.run(steps + 2)  # more steps than any budget: solves stop at their own count
@@ -69,8 +70,8 @@ def test_batch_matches_solves_run_alone(precision):
     bitwise = True
     for k, sp in enumerate(specs):
         assert st[k]["done"] and st[k]["steps"] == steps
-        bitwise &= compare(b.slots[k]["q"], alone(sp, steps, precision), f"{precision} slot {k} {sp.nx}x{sp.ny}",
-                           precision)
+        bitwise &= compare(b.slots[k]["q"], alone(sp, steps, precision, fp64_switches=sw),
+                           f"{form} slot {k} {sp.nx}x{sp.ny}", precision)
     assert not st[len(specs)]["used"]
     info = b.info()
     assert info["tiles"] > 0

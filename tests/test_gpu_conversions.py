@@ -1,7 +1,9 @@
-"""The precision form's integer-pipe conversions (to_f32 / to_f64) equal the hardware
-binary64 <-> binary32 conversions bit for bit, on random bit patterns and on every boundary the
-rounding code distinguishes: ties to even, carries into the exponent, the edges of binary32's
-normal range (subnormal results, overflow to infinity), zeros, infinities, NaN."""
+"""The integer-pipe conversions (to_f32 / to_f64) equal the hardware binary64 <-> binary32
+conversions bit for bit, on random bit patterns and on every boundary the rounding code
+distinguishes: ties to even, carries into the exponent, the edges of binary32's normal range
+(subnormal results, overflow to infinity), zeros, infinities, NaN. The integer binary64 compares
+(dlt, dneg and the wmin / wmax / wsign built on them) equal the hardware compares on the same
+inputs and on every pair of special values."""
 import ctypes
 
 import numpy as np
@@ -20,17 +22,17 @@ from wavemp.solver import _stream  # noqa: E402
 def check(values_u64: np.ndarray):
     L = _lib.load()
     t = torch.from_numpy(values_u64.view(np.int64)).cuda()
-    a, b = ctypes.c_longlong(), ctypes.c_longlong()
+    a, b, c = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
     _lib.check(L.wm_check_conversions(ctypes.c_void_p(t.data_ptr()), t.numel(), ctypes.byref(a),
-                                      ctypes.byref(b), _stream()), "wm_check_conversions")
-    return a.value, b.value
+                                      ctypes.byref(b), ctypes.byref(c), _stream()), "wm_check_conversions")
+    return a.value, b.value, c.value
 
 
 def test_random_bit_patterns():
     rng = np.random.default_rng(0)
     bits = rng.integers(0, 2**63, size=4_000_000, dtype=np.uint64) * np.uint64(2)
     bits |= rng.integers(0, 2, size=bits.size, dtype=np.uint64)
-    assert check(bits) == (0, 0)
+    assert check(bits) == (0, 0, 0)
 
 
 def test_values_in_binary32_range_and_boundaries():
@@ -49,4 +51,16 @@ def test_values_in_binary32_range_and_boundaries():
                            base | np.uint64(0x10000001), base | np.uint64(0x1FFFFFFF)])
     # the largest binary32 significand: rounding carries into the exponent
     carry = (rng.standard_normal(100_000).view(np.uint64) | np.uint64(0x000FFFFFF0000000))
-    assert check(np.concatenate([bits, ties, carry])) == (0, 0)
+    assert check(np.concatenate([bits, ties, carry])) == (0, 0, 0)
+
+
+def test_compares_on_special_pairs():
+    """Every pair of special values (both zeros, infinities, NaNs of both signs, the smallest and
+    largest magnitudes, equal values) in both orders, via neighbouring inputs."""
+    sp = np.array([0.0, -0.0, 1.0, -1.0, np.inf, -np.inf, np.nan, -np.nan, 5e-324, -5e-324,
+                   1.7976931348623157e308, -1.7976931348623157e308, 2.0, 1.0000000000000002,
+                   0.9999999999999999, -2.0])
+    nan_payload = np.array([0x7FF0000000000001, 0xFFF8000000000123], dtype=np.uint64).view(np.float64)
+    sp = np.concatenate([sp, nan_payload])
+    pairs = [np.array([a, b]) for a in sp for b in sp]
+    assert check(np.concatenate(pairs).view(np.uint64)) == (0, 0, 0)

@@ -140,3 +140,52 @@ def test_fp32_density_l1_within_1e5_of_fp64(cfg):
     for k in ("ar1", "ar2", "E", "al", "p_p"):
         ek = l1(b[k], a[k])
         assert ek <= 1e-4, f"{cfg}: {k} L1 {ek:.2e}"
+
+
+def lockstep_density_l1(spec, steps, fp64_switches):
+    """Density L1 of the binary32 form against binary64 after `steps` steps of one config-3 solve,
+    both on the binary64 run's dt sequence."""
+    runs = {}
+    for prec in ("fp64", "fp32"):
+        p = wavemp.SolverParams(dx=spec.dx, dy=spec.dy, gamma1=spec.gamma1, pinf1=spec.pinf1, bc=spec.bc,
+                                recon="mp5c6", variant="sc", cfl=0.4, precision=prec,
+                                fp64_switches=fp64_switches and prec == "fp32")
+        s = Solver(p, spec.nx, spec.ny)
+        q = spec.make_state()
+        old = alloc_state(spec.nx, spec.ny, names=pu.FIELDS)
+        s.initialize(q)
+        runs[prec] = (s, q, old)
+    (s64, q64, o64), (s32, q32, o32) = runs["fp64"], runs["fp32"]
+    dt = s64.get_dt(q64)
+    for _ in range(steps):
+        nxt = s64.step(q64, o64, dt)
+        s32.step(q32, o32, dt, sync=False)
+        dt = nxt
+    torch.cuda.synchronize()
+    return l1(q32["ar1"] + q32["ar2"], q64["ar1"] + q64["ar2"])
+
+
+def test_fp64_switches_hold_the_batched_outliers_to_1e5():
+    """Config-3 solves 4 (136x68) and 63 (168x84) are the two of 64 whose binary32 density error
+    exceeds 1e-5 after 300 steps when the THINC indicator and the Ducros sensor are binary32 (a
+    binary32 rounding moves a knife-edge switch; the binary64 solves are well conditioned: a 1e-14
+    perturbation stays at 1e-14). With the switches from binary64 sensors both stay below 1e-6."""
+    from wavemp.batch import config3_solves
+
+    specs = config3_solves(n=64, seed=0, steps=0)
+    for k in (4, 63):
+        e = lockstep_density_l1(specs[k], 300, fp64_switches=True)
+        assert e <= 1e-6, f"solve {k}: density L1 {e:.2e}"
+
+
+@pytest.mark.parametrize("case", FP32_CASES[:4])
+def test_fp64_switches_stage_matches_reference(case):
+    d = pu.load_case(case)
+    s = Solver(pu.params_from(d, precision="fp32", fp64_switches=True), int(d["meta_nx"]), int(d["meta_ny"]))
+    q = load_state(d, "in_")
+    old = alloc_state(s.nx, s.ny, names=pu.FIELDS)
+    s.copy_old(q, old)
+    s.rhs_stage(q, old, float(d["dt0"]), 0.0, 1.0)
+    got = {k: pu.host(v) for k, v in q.items()}
+    ref = {k: d["s1_out_" + k] for k in pu.ALL}
+    pu.assert_cells(got, ref, pu.ALL, pu.case_scales(d), f"{case} fp32+switches stage", rtol=MAX_STAGE_FP32)

@@ -76,6 +76,7 @@ struct BatchDev {
     unsigned *bar_count, *bar_gen;
     int *err;
     int repair;
+    int sw64;                  // binary32 form: binary64 switches
     unsigned long long *prof;  // per-phase nanoseconds (block 0's view), or null
 };
 
@@ -197,7 +198,7 @@ __device__ __forceinline__ void run_phase(const BatchDev &B, int phase, int stag
         case PH_PREP:
             if (in) {
                 if (FP32)
-                    prep32_body(g, S.e, S.q, S.prep32, S.cells32, i, j);
+                    prep32_body(g, S.e, S.q, S.prep32, S.cells32, B.sw64 != 0, i, j);
                 else
                     prep_body(g, S.e, S.q, S.prep, i, j);
             }
@@ -205,7 +206,7 @@ __device__ __forceinline__ void run_phase(const BatchDev &B, int phase, int stag
         case PH_SENSOR:
             if (in) {
                 if (FP32)
-                    sensor32_body(g, S.prep32, S.cells32, VAR == kSC, i, j);
+                    sensor32_body(g, S.q, S.prep32, S.cells32, VAR == kSC, B.sw64 != 0, i, j);
                 else
                     sensor_body(g, S.q, S.prep, VAR == kSC, i, j);
             }
@@ -478,6 +479,7 @@ int launch(wm_batch *b, int nsteps, cudaStream_t s)
     B.bar_gen = b->bar_gen;
     B.err = b->err;
     B.repair = b->P.emergency_repair;
+    B.sw64 = b->P.fp64_switches;
     B.prof = b->prof_on ? b->prof : nullptr;
     void *args[] = {&B, &nsteps};
     int grid = std::max(1, std::min(b->grid, b->ntiles));
@@ -498,7 +500,7 @@ size_t wm_solve_workspace_bytes(const wm_batch_params *p, int nx, int ny)
     if (!p || nx < 1 || ny < 1) return 0;
     const int g = p->g;
     if (p->precision == WM_PREC_FP32)
-        return (size_t)(28 + 3 + 11 + 9) * arr_bytes(nx, ny, g, 4);
+        return (size_t)(28 + 3 + 11 + 9) * arr_bytes(nx, ny, g, 4) + arr_bytes(nx, ny, g, 8);
     return (size_t)42 * arr_bytes(nx, ny, g, 8);
 }
 
@@ -615,6 +617,7 @@ int wm_batch_set(wm_batch *b, int slot, const wm_solve_desc *d, void *workspace,
         C.ar1 = f4[39]; C.ar2 = f4[40]; C.ru = f4[41]; C.rv = f4[42]; C.p = f4[43]; C.al = f4[44];
         C.u = f4[45]; C.v = f4[46]; C.E = f4[47];
         for (int k = 0; k < 3; ++k) S.theta32[k] = f4[48 + k];
+        P.ent64 = reinterpret_cast<double *>(cur);
     } else {
         size_t a8 = arr_bytes(d->nx, d->ny, g, 8);
         double *f8[42];

@@ -23,6 +23,14 @@ __device__ __forceinline__ void count_if(unsigned long long *ctr, bool pred)
     if (b && (threadIdx.x & 31) == (__ffs(mask) - 1)) atomicAdd(ctr, (unsigned long long)__popc(b));
 }
 
+// The cell entropy of cell_entropy (SC:308-314), binary64: p / rho^gamma, gamma = gamma(alpha).
+__device__ __forceinline__ double entropy64(double ge, double ar1, double ar2, double pp)
+{
+    double rho_e = ar1 + ar2;
+    if (rho_e < kTiny) rho_e = kTiny;
+    return pp / pow(rho_e, ge);
+}
+
 // Entropy (SC:308-314) and the first-order HLLC cell state of fx_low_kernel (SC:1309-1327), both
 // pure functions of one cell, computed once per cell instead of once per face that reads them.
 __device__ __forceinline__ void prep_body(const Grid &g, const Eos &e, const Fields &q, const Prep &p, int i, int j)
@@ -33,9 +41,7 @@ __device__ __forceinline__ void prep_body(const Grid &g, const Eos &e, const Fie
 
     double ge, pie;
     mix_gamma_pinf(e, al, ge, pie);
-    double rho_e = ar1 + ar2;
-    if (rho_e < kTiny) rho_e = kTiny;
-    p.ent[kw] = pp / pow(rho_e, ge);
+    p.ent[kw] = entropy64(ge, ar1, ar2, pp);
 
     double rho = ar1 + ar2;
     double ir = 1.0 / rho;
@@ -51,6 +57,41 @@ __device__ __forceinline__ void prep_body(const Grid &g, const Eos &e, const Fie
     p.la[kw] = a;
     p.lc[kw] = sound_speed_r(e, ir, pl, a);
     p.lE[kw] = prim_to_energy(e, rho, u, v, pl, a);
+}
+
+// Ducros x pressure sensor of an interior cell (ducros_kernel, SC:875-916), binary64.
+__device__ __forceinline__ void ducros_xy(const Fields &q, int i, int j, double &sx, double &sy)
+{
+    const double *U = q.f[F_U], *V = q.f[F_V], *P = q.f[F_P];
+    long long kf = kf_of(q, i, j), Q = q.pitch;
+    double der_ux = 0.5 * (-U[kf - Q] + U[kf + Q]);
+    double der_vx = 0.5 * (-V[kf - Q] + V[kf + Q]);
+    double der_uy = 0.5 * (-U[kf - 1] + U[kf + 1]);
+    double der_vy = 0.5 * (-V[kf - 1] + V[kf + 1]);
+    double div_u = der_ux + der_vy;
+    double curl_u = der_vx - der_uy;
+    double ducros = div_u * div_u / (div_u * div_u + curl_u * curl_u + 1.0e-30);
+    double p0 = P[kf];
+    double pm2 = P[kf - 2 * Q], pm1 = P[kf - Q], pp1 = P[kf + Q], pp2 = P[kf + 2 * Q];
+    double aa = fabs(-pm2 + 16.0 * pm1 - 30.0 * p0 + 16.0 * pp1 - pp2);
+    double bb = fabs(pm2 + 16.0 * pm1 + 30.0 * p0 + 16.0 * pp1 + pp2);
+    sx = (aa / (bb + 1.0e-30)) * ducros;
+    pm2 = P[kf - 2];
+    pm1 = P[kf - 1];
+    pp1 = P[kf + 1];
+    pp2 = P[kf + 2];
+    aa = fabs(-pm2 + 16.0 * pm1 - 30.0 * p0 + 16.0 * pp1 - pp2);
+    bb = fabs(pm2 + 16.0 * pm1 + 30.0 * p0 + 16.0 * pp1 + pp2);
+    sy = (aa / (bb + 1.0e-30)) * ducros;
+}
+
+// A sensor value reduced to its side of the face sweep's threshold: 0 below it, 1 at or above it,
+// NaN for NaN. The map is monotone, so it commutes with the reference's a<b?a:b minimum and maximum
+// over the four cells of a face (NaN included), and (encoded < threshold) holds exactly when
+// (value < threshold) does: the binary32 sweep makes the decisions of the binary64 values.
+__device__ __forceinline__ float side_of(double v, double threshold)
+{
+    return v < threshold ? 0.0f : (isnan(v) ? __int_as_float(0x7fc00000) : 1.0f);
 }
 
 // Smoothness indicator per cell and direction (cator2_val, SC:318-325) and the Ducros x pressure
@@ -70,27 +111,7 @@ __device__ __forceinline__ void sensor_body(const Grid &g, const Fields &q, cons
         p.sy[kw] = 1.0;
         return;
     }
-    const double *U = q.f[F_U], *V = q.f[F_V], *P = q.f[F_P];
-    long long kf = kf_of(q, i, j), Q = q.pitch;
-    double der_ux = 0.5 * (-U[kf - Q] + U[kf + Q]);
-    double der_vx = 0.5 * (-V[kf - Q] + V[kf + Q]);
-    double der_uy = 0.5 * (-U[kf - 1] + U[kf + 1]);
-    double der_vy = 0.5 * (-V[kf - 1] + V[kf + 1]);
-    double div_u = der_ux + der_vy;
-    double curl_u = der_vx - der_uy;
-    double ducros = div_u * div_u / (div_u * div_u + curl_u * curl_u + 1.0e-30);
-    double p0 = P[kf];
-    double pm2 = P[kf - 2 * Q], pm1 = P[kf - Q], pp1 = P[kf + Q], pp2 = P[kf + 2 * Q];
-    double aa = fabs(-pm2 + 16.0 * pm1 - 30.0 * p0 + 16.0 * pp1 - pp2);
-    double bb = fabs(pm2 + 16.0 * pm1 + 30.0 * p0 + 16.0 * pp1 + pp2);
-    p.sx[kw] = (aa / (bb + 1.0e-30)) * ducros;
-    pm2 = P[kf - 2];
-    pm1 = P[kf - 1];
-    pp1 = P[kf + 1];
-    pp2 = P[kf + 2];
-    aa = fabs(-pm2 + 16.0 * pm1 - 30.0 * p0 + 16.0 * pp1 - pp2);
-    bb = fabs(pm2 + 16.0 * pm1 + 30.0 * p0 + 16.0 * pp1 + pp2);
-    p.sy[kw] = (aa / (bb + 1.0e-30)) * ducros;
+    ducros_xy(q, i, j, p.sx[kw], p.sy[kw]);
 }
 
 // Face limiter factors of pass p (pp_blend_x/y_flux_kernel, SC:1479-1548): the x face between
@@ -498,7 +519,7 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
 // first-order HLLC cell state whose pressure floor and the numerator of its sound speed are
 // recovered in binary64 (the stiffened-gas p + p_inf cancels to round-off of p_inf ~ 6e8 in
 // binary32).
-__device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const Fields &q, const PrepT<float> &p, const Cells32 &c, int i, int j)
+__device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const Fields &q, const PrepT<float> &p, const Cells32 &c, bool sw64, int i, int j)
 {
     long long kf = kf_of(q, i, j), kw = kw_of(g, i, j);
     const double ar1 = q.f[F_AR1][kf], ar2 = q.f[F_AR2][kf], ru = q.f[F_RU][kf], rv = q.f[F_RV][kf];
@@ -515,11 +536,17 @@ __device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const F
     c.v[kw] = to_f32(q.f[F_V][kf]);
     c.E[kw] = to_f32(q.f[F_E][kf]);
 
-    float ge, pie;
-    mix_gamma_pinf(e, alf, ge, pie);
-    float rho_e = ar1f + ar2f;
-    if (rho_e < float(kTiny)) rho_e = float(kTiny);
-    p.ent[kw] = pf / powf(rho_e, ge);
+    if (sw64) {  // binary64 switches: the entropy of the binary64 form
+        double ge, pie;
+        mix_gamma_pinf(e, al, ge, pie);
+        p.ent64[kw] = entropy64(ge, ar1, ar2, pp);
+    } else {
+        float ge, pie;
+        mix_gamma_pinf(e, alf, ge, pie);
+        float rho_e = ar1f + ar2f;
+        if (rho_e < float(kTiny)) rho_e = float(kTiny);
+        p.ent[kw] = pf / powf(rho_e, ge);
+    }
 
     // With g = 1 + 1/Gamma and p_inf = Pi / (1 + Gamma): (p + p_inf) / (g - 1) < floor  <=>
     // ((1 + Gamma) p + Pi) Gamma < floor (1 + Gamma), and c^2 = ((1 + Gamma) p + Pi) / (Gamma rho).
@@ -550,10 +577,29 @@ __device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const F
 }
 
 // Smoothness indicators and Ducros sensor in binary32 (sensor_kernel's arithmetic).
-__device__ __forceinline__ void sensor32_body(const Grid &g, const PrepT<float> &p, const Cells32 &c, int sc, int i, int j)
+__device__ __forceinline__ void sensor32_body(const Grid &g, const Fields &q, const PrepT<float> &p, const Cells32 &c, int sc,
+                                              bool sw64, int i, int j)
 {
     long long kw = kw_of(g, i, j);
     const long long W = g.nyg;
+    if (sw64) {  // the binary64 sensors, stored as their side of the sweep's thresholds
+        const double *en = p.ent64;
+        if (i >= 2 && i < g.nxg - 2)
+            p.cx[kw] = side_of(cator2_val(en[kw - 2 * W], en[kw - W], en[kw], en[kw + W], en[kw + 2 * W]), kThincThresh);
+        if (j >= 2 && j < g.nyg - 2)
+            p.cy[kw] = side_of(cator2_val(en[kw - 2], en[kw - 1], en[kw], en[kw + 1], en[kw + 2]), kThincThresh);
+        if (!sc) return;
+        if (i < 2 || i >= g.nxg - 2 || j < 2 || j >= g.nyg - 2) {
+            p.sx[kw] = side_of(1.0, kSigmaSmooth);
+            p.sy[kw] = side_of(1.0, kSigmaSmooth);
+            return;
+        }
+        double sx, sy;
+        ducros_xy(q, i, j, sx, sy);
+        p.sx[kw] = side_of(sx, kSigmaSmooth);
+        p.sy[kw] = side_of(sy, kSigmaSmooth);
+        return;
+    }
     const float *en = p.ent;
     if (i >= 2 && i < g.nxg - 2)
         p.cx[kw] = cator2_val(en[kw - 2 * W], en[kw - W], en[kw], en[kw + W], en[kw + 2 * W]);

@@ -45,11 +45,12 @@ size_t array_bytes(int nx, int ny, int g, size_t elem = sizeof(double))
 
 // Workspace of the plain form: 42 binary64 arrays. Precision form: 28 binary32 face arrays, 3
 // binary32 limiter factors (bound solves in binary64, stored in the flux type), 11 binary32
-// per-cell arrays and 9 binary32 cell copies.
+// per-cell arrays, 9 binary32 cell copies and the binary64 entropy of the binary64 switches.
 size_t layout_bytes(int precision, int nx, int ny, int g)
 {
     if (precision == WM_PREC_FP32)
-        return (size_t)(kArrays + kCellCopies) * array_bytes(nx, ny, g, sizeof(float)) + kTailBytes;
+        return (size_t)(kArrays + kCellCopies) * array_bytes(nx, ny, g, sizeof(float)) + array_bytes(nx, ny, g) +
+               kTailBytes;
     return (size_t)kArrays * array_bytes(nx, ny, g) + kTailBytes;
 }
 
@@ -106,6 +107,7 @@ struct wm_handle {
     bool fluxes_ready = false, low_ready = false;
     bool defer_limiter = false;  // fused stage: limiter blends rebuilt in registers (wm_set_limiter_sweeps)
     bool prechecks = true;       // precision form: binary32 pre-checks of binary64 tests (wm_set_prechecks)
+    bool sw64 = false;           // precision form: binary64 switches (wm_params.fp64_switches)
     // device-side time loop (wm_run): clock block, graph with a conditional while node
     struct RunClock *clock = nullptr;
     cudaGraph_t run_graph = nullptr;
@@ -276,6 +278,9 @@ int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t
             copies[c] = reinterpret_cast<float *>(cur);
             cur += ab4;
         }
+        double *ent64 = reinterpret_cast<double *>(cur);
+        cur += array_bytes(nx, ny, g);
+        h->sw64 = p->fp64_switches != 0;
         for (int c = 0; c < 7; ++c) {
             h->fh32.f[c] = h->arr32[WM_WS_FX + c];
             h->gh32.f[c] = h->arr32[WM_WS_GY + c];
@@ -292,6 +297,7 @@ int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t
         P.ent = h->arr32[33]; P.cx = h->arr32[34]; P.cy = h->arr32[35];
         P.lu = h->arr32[36]; P.lv = h->arr32[37]; P.lp = h->arr32[38]; P.la = h->arr32[39];
         P.lc = h->arr32[40]; P.lE = h->arr32[41];
+        P.ent64 = ent64;
         Cells32 &C = h->cells32;
         C.ar1 = copies[0]; C.ar2 = copies[1]; C.ru = copies[2]; C.rv = copies[3];
         C.p = copies[4]; C.al = copies[5]; C.u = copies[6]; C.v = copies[7]; C.E = copies[8];
@@ -373,7 +379,7 @@ int wm_compute_fluxes(wm_handle *h, const wm_fields *q, void *stream)
     Fields F = to_fields(q);
     cudaStream_t s = as_stream(stream);
     if (h->fp32) {
-        launch_prep32(h->g, h->e, F, h->prep32, h->cells32, h->P.variant, s);
+        launch_prep32(h->g, h->e, F, h->prep32, h->cells32, h->P.variant, h->sw64, s);
         launch_faces32(h->g, h->e, h->P.variant, h->P.recon, h->cells32, h->prep32, h->fh32, h->gh32,
                        h->fl32, h->gl32, true, false, s);
     } else {
@@ -391,7 +397,7 @@ int wm_compute_low_fluxes(wm_handle *h, const wm_fields *q, void *stream)
     Fields F = to_fields(q);
     cudaStream_t s = as_stream(stream);
     if (h->fp32) {
-        launch_prep32(h->g, h->e, F, h->prep32, h->cells32, h->P.variant, s);
+        launch_prep32(h->g, h->e, F, h->prep32, h->cells32, h->P.variant, h->sw64, s);
         launch_faces32(h->g, h->e, h->P.variant, h->P.recon, h->cells32, h->prep32, h->fh32, h->gh32,
                        h->fl32, h->gl32, false, true, s);
     } else {
@@ -497,7 +503,7 @@ static int run_stage(wm_handle *h, const Fields &F, const Fields &O, double dt, 
     {
         ProfScope ps(h, WM_PROF_PREP, 2, s);
         if (h->fp32)
-            launch_prep32(h->g, h->e, F, h->prep32, h->cells32, h->P.variant, s);
+            launch_prep32(h->g, h->e, F, h->prep32, h->cells32, h->P.variant, h->sw64, s);
         else
             launch_prep(h->g, h->e, F, h->prep, h->P.variant, s);
     }

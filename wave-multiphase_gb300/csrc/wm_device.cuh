@@ -95,9 +95,33 @@ __device__ __forceinline__ double to_f64(float x)
     return (double)x;
 }
 
+// IEEE a < b on binary64 by integer compares of the bit patterns, off GB300's narrow binary64 pipe:
+// false when either operand is NaN; otherwise the order of the signed magnitudes, in which both
+// zeros map to 0 (so -0 < +0 is false, as IEEE has it).
+__device__ __forceinline__ bool dlt(double a, double b)
+{
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    const long long ma = ia & 0x7fffffffffffffffLL, mb = ib & 0x7fffffffffffffffLL;
+    const long long inf = 0x7ff0000000000000LL;
+    const long long ka = ia < 0 ? -ma : ma, kb = ib < 0 ? -mb : mb;
+    return ma <= inf && mb <= inf && ka < kb;
+}
+// x < 0 on binary64: sign bit set, not a zero, not NaN
+__device__ __forceinline__ bool dneg(double x)
+{
+    const long long ix = __double_as_longlong(x);
+    const long long m = ix & 0x7fffffffffffffffLL;
+    return ix < 0 && m != 0 && m <= 0x7ff0000000000000LL;
+}
+
+// The reference's wp.min / wp.max / wp.sign: a < b ? a : b, a > b ? a : b, x < 0 ? -1 : 1
+// (binary64: by the integer compares above, the same results).
 template <typename T> __device__ __forceinline__ T wmin(T a, T b) { return a < b ? a : b; }
 template <typename T> __device__ __forceinline__ T wmax(T a, T b) { return a > b ? a : b; }
 template <typename T> __device__ __forceinline__ T wsign(T x) { return x < T(0) ? T(-1) : T(1); }
+template <> __device__ __forceinline__ double wmin(double a, double b) { return dlt(a, b) ? a : b; }
+template <> __device__ __forceinline__ double wmax(double a, double b) { return dlt(b, a) ? a : b; }
+template <> __device__ __forceinline__ double wsign(double x) { return dneg(x) ? -1.0 : 1.0; }
 __device__ __forceinline__ double wabs(double x) { return fabs(x); }
 __device__ __forceinline__ float wabs(float x) { return fabsf(x); }
 __device__ __forceinline__ bool wisnan(double x) { return isnan(x); }

@@ -24,6 +24,7 @@ using Face7 = Face<double>;
 // Per-cell data computed once per stage and shared by the faces that use it.
 template <typename PT> struct PrepT {
     PT *ent;                          // cell entropy p / rho^gamma
+    double *ent64;                    // precision form with binary64 switches: the entropy in binary64
     PT *cx, *cy;                      // smoothness indicator along x and y
     PT *sx, *sy;                      // Ducros x pressure sensor (SC only)
     PT *lu, *lv, *lp, *la, *lc, *lE;  // first-order HLLC cell state: velocity, floored
@@ -88,7 +89,7 @@ void launch_fp64_probe(double *out, int iters, cudaStream_t s, int blocks, int t
 
 // Precision form (binary32 face sweep).
 void launch_prep32(const Grid &g, const Eos &e, const Fields &q, const PrepT<float> &p,
-                   const Cells32 &c, int variant, cudaStream_t s);
+                   const Cells32 &c, int variant, bool sw64, cudaStream_t s);
 void launch_faces32(const Grid &g, const Eos &e, int variant, int recon, const Cells32 &c,
                     const PrepT<float> &p, const Face<float> &fh, const Face<float> &gh,
                     const Face<float> &fl, const Face<float> &gl, bool high, bool low,

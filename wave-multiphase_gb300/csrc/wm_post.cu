@@ -111,17 +111,24 @@ __global__ void conv_check_kernel(const unsigned long long *in, long long n, uns
         const bool same64 = __double_as_longlong(c) == __double_as_longlong(d) || (c != c && d != d);
         if (!same32) atomicAdd(&bad[0], 1ull);
         if (!same64) atomicAdd(&bad[1], 1ull);
+        // integer binary64 compares against the hardware ones (pairs of neighbouring inputs)
+        const double z = __longlong_as_double((long long)in[k + 1 < n ? k + 1 : 0]);
+        const bool cmp_ok = wm::dlt(x, z) == (x < z) && wm::dlt(z, x) == (z < x) && wm::dneg(x) == (x < 0.0) &&
+                            __double_as_longlong(wm::wmin(x, z)) == __double_as_longlong(x < z ? x : z) &&
+                            __double_as_longlong(wm::wmax(x, z)) == __double_as_longlong(x > z ? x : z) &&
+                            wm::wsign(x) == (x < 0.0 ? -1.0 : 1.0);
+        if (!cmp_ok) atomicAdd(&bad[2], 1ull);
     }
 }
 
 }  // namespace
 
 extern "C" int wm_check_conversions(const unsigned long long *bits, long long n, long long *bad_f32,
-                                    long long *bad_f64, void *stream)
+                                    long long *bad_f64, long long *bad_cmp, void *stream)
 {
-    if (!bits || n < 0 || !bad_f32 || !bad_f64) return WM_ERR_INVALID;
+    if (!bits || n < 0 || !bad_f32 || !bad_f64 || !bad_cmp) return WM_ERR_INVALID;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    unsigned long long *ctr = nullptr, host[2] = {0, 0};
+    unsigned long long *ctr = nullptr, host[3] = {0, 0, 0};
     cudaError_t e = cudaMalloc(&ctr, sizeof host);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctr, 0, sizeof host, s);
     if (e == cudaSuccess && n > 0) {
@@ -139,6 +146,7 @@ extern "C" int wm_check_conversions(const unsigned long long *bits, long long n,
     }
     *bad_f32 = (long long)host[0];
     *bad_f64 = (long long)host[1];
+    *bad_cmp = (long long)host[2];
     return WM_OK;
 }
 

@@ -129,20 +129,20 @@ final_kernel(Grid g, Eos e, unsigned flags, Fields q, Fields old, Face<FT> fh, F
     }
 }
 
-__global__ void __launch_bounds__(BX *BY) prep32_kernel(Grid g, Eos e, Fields q, PrepT<float> p, Cells32 c)
+__global__ void __launch_bounds__(BX *BY) prep32_kernel(Grid g, Eos e, Fields q, PrepT<float> p, Cells32 c, int sw64)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.nxg || j >= g.nyg) return;
-    prep32_body(g, e, q, p, c, i, j);
+    prep32_body(g, e, q, p, c, sw64 != 0, i, j);
 }
 
-__global__ void __launch_bounds__(BX *BY) sensor32_kernel(Grid g, PrepT<float> p, Cells32 c, int sc)
+__global__ void __launch_bounds__(BX *BY) sensor32_kernel(Grid g, Fields q, PrepT<float> p, Cells32 c, int sc, int sw64)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.nxg || j >= g.nyg) return;
-    sensor32_body(g, p, c, sc, i, j);
+    sensor32_body(g, q, p, c, sc, sw64 != 0, i, j);
 }
 
 __global__ void widen_kernel(const float *src, double *dst, long long n)
@@ -289,10 +289,10 @@ template void launch_final<float>(const Grid &, const Eos &, unsigned, const Fie
                                   double, double, const Counters &, cudaStream_t);
 
 void launch_prep32(const Grid &g, const Eos &e, const Fields &q, const PrepT<float> &p,
-                   const Cells32 &c, int variant, cudaStream_t s)
+                   const Cells32 &c, int variant, bool sw64, cudaStream_t s)
 {
-    prep32_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, e, q, p, c);
-    sensor32_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, p, c, variant == kSC);
+    prep32_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, e, q, p, c, sw64 ? 1 : 0);
+    sensor32_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, q, p, c, variant == kSC, sw64 ? 1 : 0);
 }
 
 void launch_widen(const float *src, double *dst, long long n, cudaStream_t s)

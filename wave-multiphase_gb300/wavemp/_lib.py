@@ -23,7 +23,8 @@ class WmParams(ctypes.Structure):
                 ("gamma2", ctypes.c_double), ("pinf2", ctypes.c_double),
                 ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("cfl", ctypes.c_double),
                 ("variant", ctypes.c_int), ("recon", ctypes.c_int), ("bc", ctypes.c_int * 4),
-                ("emergency_repair", ctypes.c_int), ("precision", ctypes.c_int)]
+                ("emergency_repair", ctypes.c_int), ("precision", ctypes.c_int),
+                ("fp64_switches", ctypes.c_int)]
 
 
 class WmFields(ctypes.Structure):
@@ -45,7 +46,7 @@ class WmSchedule(ctypes.Structure):
 class WmBatchParams(ctypes.Structure):
     _fields_ = [("variant", ctypes.c_int), ("recon", ctypes.c_int), ("precision", ctypes.c_int),
                 ("emergency_repair", ctypes.c_int), ("g", ctypes.c_int), ("cfl", ctypes.c_double),
-                ("tile_shape", ctypes.c_int)]
+                ("tile_shape", ctypes.c_int), ("fp64_switches", ctypes.c_int)]
 
 
 class WmSolveDesc(ctypes.Structure):
@@ -146,7 +147,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.wm_batch_dt_log.argtypes = [vp, i, vp, ctypes.c_longlong, i]
     L.wm_set_prechecks.argtypes = [vp, i]
     L.wm_check_conversions.argtypes = [vp, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong),
-                                       ctypes.POINTER(ctypes.c_longlong), vp]
+                                       ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong), vp]
     L.wm_verify_limiter_precheck.argtypes = [vp, F, d, ctypes.POINTER(ctypes.c_longlong),
                                              ctypes.POINTER(ctypes.c_longlong), vp]
     L.wm_batch_profile_read.argtypes = [vp, ctypes.POINTER(d * len(BATCH_PHASES)), i, vp]

@@ -53,17 +53,18 @@ class SolveSpec:
 
 class Batch:
     def __init__(self, capacity: int, variant="sc", recon="mp5c6", precision="fp64",
-                 emergency_repair=True, cfl=0.4, g=5, tile_shape=-1, device=None):
+                 emergency_repair=True, cfl=0.4, g=5, tile_shape=-1, device=None, fp64_switches=False):
         self.L = _lib.load()
         self.g = g
         self.capacity = capacity
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.scheme = dict(variant=variant, recon=recon, precision=precision,
-                           emergency_repair=emergency_repair, cfl=cfl)
+                           emergency_repair=emergency_repair, cfl=cfl, fp64_switches=fp64_switches)
         p = _lib.WmBatchParams()
         p.variant, p.recon = _lib.VARIANT[variant], _lib.RECON[recon]
         p.precision, p.emergency_repair = _lib.PRECISION[precision], int(bool(emergency_repair))
         p.g, p.cfl, p.tile_shape = g, cfl, tile_shape
+        p.fp64_switches = int(bool(fp64_switches))
         self._p = p
         h = ctypes.c_void_p()
         _lib.check(self.L.wm_batch_create(ctypes.byref(p), capacity, ctypes.byref(h)), "wm_batch_create")
@@ -92,7 +93,7 @@ class Batch:
     def _solver_kw(self):
         s = self.scheme
         return dict(variant=s["variant"], recon=s["recon"], precision=s["precision"],
-                    emergency_repair=s["emergency_repair"], cfl=s["cfl"])
+                    emergency_repair=s["emergency_repair"], cfl=s["cfl"], fp64_switches=s["fp64_switches"])
 
     # -- slots ----------------------------------------------------------------------------------
     def free_slot(self) -> int | None:

@@ -27,6 +27,7 @@ class SolverParams:
     bc: tuple = ("transmissive", "transmissive", "slip", "slip")  # x-lo, x-hi, y-lo, y-hi
     emergency_repair: bool = True
     precision: str = "fp64"
+    fp64_switches: bool = False  # precision form: THINC / Ducros switches from binary64 sensors
 
     def to_c(self) -> _lib.WmParams:
         p = _lib.WmParams()
@@ -43,4 +44,5 @@ class SolverParams:
         if len(self.bc) != 4:
             raise ValueError("bc needs four sides (x-lo, x-hi, y-lo, y-hi)")
         p.emergency_repair = int(bool(self.emergency_repair))
+        p.fp64_switches = int(bool(self.fp64_switches))
         return p
