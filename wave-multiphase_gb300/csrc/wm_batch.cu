@@ -583,7 +583,7 @@ int wm_batch_set(wm_batch *b, int slot, const wm_solve_desc *d, void *workspace,
     SolveDev &S = b->host[slot];
     Grid &G = S.g;
     G.nx = d->nx; G.ny = d->ny; G.g = g; G.nxg = d->nx + 2 * g; G.nyg = nyg; G.pitch = nyg;
-    G.dx = d->dx; G.dy = d->dy; G.inv_dx = 1.0 / d->dx; G.inv_dy = 1.0 / d->dy; G.cfl = b->P.cfl;
+    G.dx = d->dx; G.dy = d->dy; G.inv_dx = 1.0 / d->dx; G.inv_dy = 1.0 / d->dy; G.inv_dxf = float(G.inv_dx); G.inv_dyf = float(G.inv_dy); G.cfl = b->P.cfl;
     S.e = make_eos(d->gamma1, d->pinf1, d->gamma2, d->pinf2);
     for (int k = 0; k < 4; ++k) S.bc[k] = d->bc[k];
     Fields *dst[2] = {&S.q, &S.old};

@@ -258,7 +258,7 @@ __device__ __forceinline__ double theta_body(const Grid &g, const Eos &e, const 
 {
     const CellFaces<FT, NP> cf(g, theta, i, j);
     const long long kf = kf_of(q, i, j), kw = cf.kw, kx = cf.kx, ky = cf.ky;
-    const FT idx = FT(g.inv_dx), idy = FT(g.inv_dy);
+    const FT idx = cst<FT>(g.inv_dx, g.inv_dxf), idy = cst<FT>(g.inv_dy, g.inv_dyf);
     constexpr int C0 = STAGE == 1 ? 5 : 0, C1 = STAGE == 0 ? 2 : 6;
     FT rh[6], rl[6];
 #pragma unroll
@@ -385,7 +385,7 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
         if (interior && (flags & FIN_RK3)) {
             if (dt_dev) dt = *dt_dev;
             const CellFaces<FT, NP> cf(g, theta, i, j);
-            const FT idx = FT(g.inv_dx), idy = FT(g.inv_dy);
+            const FT idx = cst<FT>(g.inv_dx, g.inv_dxf), idy = cst<FT>(g.inv_dy, g.inv_dyf);
             FT ap;
             if constexpr (sizeof(FT) == 4) ap = to_f32(q.f[F_ALP][kf]);
             else ap = q.f[F_ALP][kf];

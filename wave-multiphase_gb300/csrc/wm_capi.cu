@@ -221,7 +221,7 @@ int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t
     h->P = *p;
     Grid &G = h->g;
     G.nx = nx; G.ny = ny; G.g = g; G.nxg = nx + 2 * g; G.nyg = ny + 2 * g; G.pitch = G.nyg;
-    G.dx = p->dx; G.dy = p->dy; G.inv_dx = 1.0 / p->dx; G.inv_dy = 1.0 / p->dy; G.cfl = p->cfl;
+    G.dx = p->dx; G.dy = p->dy; G.inv_dx = 1.0 / p->dx; G.inv_dy = 1.0 / p->dy; G.inv_dxf = float(G.inv_dx); G.inv_dyf = float(G.inv_dy); G.cfl = p->cfl;
     h->e = make_eos(p->gamma1, p->pinf1, p->gamma2, p->pinf2);
 
     if (workspace) {

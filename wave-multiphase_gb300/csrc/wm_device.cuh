@@ -22,7 +22,8 @@ struct Eos {
     double k1, k2;          // g1*p1/(g1-1), g2*p2/(g2-1)
     double thinc_t1;        // tanh(beta/2), beta = 1.8 (computed once on the host)
     double thinc_inv_t1;    // 1/tanh(beta/2)
-    float r1f, r2f, k1f, k2f;  // binary32 copies (the precision form's limiter pre-checks)
+    float r1f, r2f, k1f, k2f;  // binary32 copies (binary32 kernels use these: no conversion on the
+    float thinc_t1f, thinc_inv_t1f;  // device, where it would issue on the narrow binary64 pipe)
 };
 
 // The run's constants of the stiffened-gas mixture (host side).
@@ -35,14 +36,21 @@ inline Eos make_eos(double g1, double p1, double g2, double p2)
     E.thinc_t1 = std::tanh(1.8 * 0.5);
     E.thinc_inv_t1 = 1.0 / E.thinc_t1;
     E.r1f = float(E.r1); E.r2f = float(E.r2); E.k1f = float(E.k1); E.k2f = float(E.k2);
+    E.thinc_t1f = float(E.thinc_t1); E.thinc_inv_t1f = float(E.thinc_inv_t1);
     return E;
 }
+
+// A run-time constant in the arithmetic type T: the binary64 value, or its host-made binary32 copy.
+template <typename T> __device__ __forceinline__ T cst(double d, float f);
+template <> __device__ __forceinline__ double cst<double>(double d, float) { return d; }
+template <> __device__ __forceinline__ float cst<float>(double, float f) { return f; }
 
 struct Grid {
     int nx, ny, g;       // interior size and ghost width
     int nxg, nyg;        // padded size
     long long pitch;     // elements between x rows
     double dx, dy, inv_dx, inv_dy, cfl;
+    float inv_dxf, inv_dyf;  // binary32 copies of 1/dx, 1/dy
 };
 
 // Reference constants (SC:44-70).
@@ -143,8 +151,8 @@ template <typename T>
 __device__ __forceinline__ void mix_gamma_pibig(const Eos &e, T a1, T &gb, T &pb)
 {
     T a2 = T(1) - a1;
-    gb = a1 * T(e.r1) + a2 * T(e.r2);
-    pb = a1 * T(e.k1) + a2 * T(e.k2);
+    gb = a1 * cst<T>(e.r1, e.r1f) + a2 * cst<T>(e.r2, e.r2f);
+    pb = a1 * cst<T>(e.k1, e.k1f) + a2 * cst<T>(e.k2, e.k2f);
 }
 
 // mixture gamma and p_inf: g = 1/Gamma + 1, p_inf = (g-1) Pi / g = Pi / (1 + Gamma), with the two
@@ -395,9 +403,9 @@ template <typename T> __device__ __forceinline__ T thinc_ul(const Eos &e, T vm1,
         T qa = T(0.5) * (v1 + vm1);
         T qd = T(0.5) * (v1 - vm1);
         T feng = (v0 - qa) / qd;
-        T T1 = T(e.thinc_t1);
+        T T1 = cst<T>(e.thinc_t1, e.thinc_t1f);
         T T2 = wtanh(feng * T(1.8) * T(0.5));
-        result = qa + qd * (T1 + T2 * T(e.thinc_inv_t1)) / (T(1) + T2);
+        result = qa + qd * (T1 + T2 * cst<T>(e.thinc_inv_t1, e.thinc_inv_t1f)) / (T(1) + T2);
     }
     return result;
 }
@@ -409,9 +417,9 @@ template <typename T> __device__ __forceinline__ T thinc_ur(const Eos &e, T v0, 
         T qa = T(0.5) * (v2 + v0);
         T qd = T(0.5) * (v2 - v0);
         T feng = (v1 - qa) / qd;
-        T T1 = T(e.thinc_t1);
+        T T1 = cst<T>(e.thinc_t1, e.thinc_t1f);
         T T2 = wtanh(feng * T(1.8) * T(0.5));
-        result = qa - qd * (T1 - T2 * T(e.thinc_inv_t1)) / (T(1) - T2);
+        result = qa - qd * (T1 - T2 * cst<T>(e.thinc_inv_t1, e.thinc_inv_t1f)) / (T(1) - T2);
     }
     return result;
 }
