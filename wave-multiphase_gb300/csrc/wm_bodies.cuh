@@ -693,12 +693,12 @@ __device__ __forceinline__ void face_body(const Grid &g, const Eos &e, const CS 
     // --- sensors (per-cell, computed by sensor_kernel) -------------------------------------------
     const T *ci = DIR == 0 ? p.cx : p.cy;
     const T c_m1 = ci[kw - sw], c_0 = ci[kw], c_p1 = ci[kw + sw], c_p2 = ci[kw + 2 * sw];
-    const bool use_thinc = wmin(wmin(c_m1, c_0), wmin(c_p1, c_p2)) < T(kThincThresh);
+    const bool use_thinc = flt(wmin(wmin(c_m1, c_0), wmin(c_p1, c_p2)), T(kThincThresh));
     bool smooth = false;
     if (VAR == kSC) {
         const T *sg = DIR == 0 ? p.sx : p.sy;
         const T smax = wmax(wmax(sg[kw - sw], sg[kw]), wmax(sg[kw + sw], sg[kw + 2 * sw]));
-        smooth = smax < T(kSigmaSmooth);
+        smooth = flt(smax, T(kSigmaSmooth));
     }
 
     // --- face-averaged state and eigenvector basis (SC:1039-1048) ------------------------------
@@ -778,17 +778,17 @@ __device__ __forceinline__ void face_body(const Grid &g, const Eos &e, const CS 
     for (int s = 0; s < 2; ++s) {
         S6<T> &ph = s == 0 ? phL : phR;
         const S6<T> &pf = s == 0 ? phfL : phfR;
-        if (ph.v[0] < T(0) || wisnan(ph.v[0])) ph.v[0] = pf.v[0];
-        if (ph.v[1] < T(0) || wisnan(ph.v[1])) ph.v[1] = pf.v[1];
-        if (ph.v[5] < T(0) || ph.v[5] > T(1)) ph.v[5] = pf.v[5];
+        if (!fge(ph.v[0], T(0))) ph.v[0] = pf.v[0];  // x < 0 or NaN
+        if (!fge(ph.v[1], T(0))) ph.v[1] = pf.v[1];
+        if (flt(ph.v[5], T(0)) || fgt(ph.v[5], T(1))) ph.v[5] = pf.v[5];
         if (VAR == kM10) {
-            if (rho_ctilde2_sc(e, ph) < T(kPpCtilde) || wisnan(ph.v[4])) ph.v[4] = pf.v[4];
+            if (flt(rho_ctilde2_sc(e, ph), T(kPpCtilde)) || wisnan(ph.v[4])) ph.v[4] = pf.v[4];
             ph = pp_floor_pressure_state(e, ph);
         } else if (wisnan(ph.v[4])) {
             ph.v[4] = pf.v[4];
         }
     }
-    if (ca < T(0) || wisnan(ca)) {
+    if (!fge(ca, T(0))) {  // ca < 0 or NaN
         phL = phfL;
         phR = phfR;
     }

@@ -122,6 +122,32 @@ __device__ __forceinline__ bool dneg(double x)
     return ix < 0 && m != 0 && m <= 0x7ff0000000000000LL;
 }
 
+// IEEE a <= b on binary64 the same way (both zeros map to 0, so -0 <= +0).
+__device__ __forceinline__ bool dle(double a, double b)
+{
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    const long long ma = ia & 0x7fffffffffffffffLL, mb = ib & 0x7fffffffffffffffLL;
+    const long long inf = 0x7ff0000000000000LL;
+    const long long ka = ia < 0 ? -ma : ma, kb = ib < 0 ? -mb : mb;
+    return ma <= inf && mb <= inf && ka <= kb;
+}
+// x > 0 on binary64: sign bit clear, not a zero, not NaN
+__device__ __forceinline__ bool dpos(double x)
+{
+    const long long ix = __double_as_longlong(x);
+    return ix > 0 && ix <= 0x7ff0000000000000LL;
+}
+
+// IEEE comparisons in the arithmetic type T (binary64: the integer forms above, same results).
+template <typename T> __device__ __forceinline__ bool flt(T a, T b) { return a < b; }
+template <typename T> __device__ __forceinline__ bool fle(T a, T b) { return a <= b; }
+template <> __device__ __forceinline__ bool flt<double>(double a, double b) { return dlt(a, b); }
+template <> __device__ __forceinline__ bool fle<double>(double a, double b) { return dle(a, b); }
+template <typename T> __device__ __forceinline__ bool fgt(T a, T b) { return flt(b, a); }
+template <typename T> __device__ __forceinline__ bool fge(T a, T b) { return fle(b, a); }
+template <typename T> __device__ __forceinline__ bool fpos(T x) { return x > T(0); }
+template <> __device__ __forceinline__ bool fpos<double>(double x) { return dpos(x); }
+
 // The reference's wp.min / wp.max / wp.sign: a < b ? a : b, a > b ? a : b, x < 0 ? -1 : 1
 // (binary64: by the integer compares above, the same results).
 template <typename T> __device__ __forceinline__ T wmin(T a, T b) { return a < b ? a : b; }
@@ -132,7 +158,10 @@ template <> __device__ __forceinline__ double wmax(double a, double b) { return 
 template <> __device__ __forceinline__ double wsign(double x) { return dneg(x) ? -1.0 : 1.0; }
 __device__ __forceinline__ double wabs(double x) { return fabs(x); }
 __device__ __forceinline__ float wabs(float x) { return fabsf(x); }
-__device__ __forceinline__ bool wisnan(double x) { return isnan(x); }
+__device__ __forceinline__ bool wisnan(double x)  // by integer compare of the bits
+{
+    return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
 __device__ __forceinline__ bool wisnan(float x) { return isnan(x); }
 __device__ __forceinline__ double wsqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float wsqrt(float x) { return sqrtf(x); }
@@ -175,7 +204,7 @@ __device__ __forceinline__ T sound_speed_r(const Eos &e, T inv_rho, T p, T a1)
     T g, pi;
     mix_gamma_pinf(e, a1, g, pi);
     T val = g * (p + pi) * inv_rho;
-    if (val < T(kTiny)) val = T(kTiny);
+    if (flt(val, T(kTiny))) val = T(kTiny);
     return wsqrt(val);
 }
 
@@ -195,8 +224,8 @@ template <typename T> __device__ __forceinline__ T clamp01_pp(T a1)
 {
     T a = a1;
     if (wisnan(a)) a = T(kPpAlpha);
-    if (a < T(kPpAlpha)) a = T(kPpAlpha);
-    if (a > T(1) - T(kPpAlpha)) a = T(1) - T(kPpAlpha);
+    if (flt(a, T(kPpAlpha))) a = T(kPpAlpha);
+    if (fgt(a, T(1) - T(kPpAlpha))) a = T(1) - T(kPpAlpha);
     return a;
 }
 
@@ -236,7 +265,7 @@ template <typename T> __device__ __forceinline__ S6<T> pp_floor_pressure_state(c
     T a1 = clamp01_pp(s.v[5]);
     T g, pi;
     mix_gamma_pinf(e, a1, g, pi);
-    if (wisnan(s.v[4]) || rho_ctilde2_sc(e, s) < T(kPpCtilde)) s.v[4] = T(kPpCtilde) * (g - T(1)) - pi;
+    if (wisnan(s.v[4]) || flt(rho_ctilde2_sc(e, s), T(kPpCtilde))) s.v[4] = T(kPpCtilde) * (g - T(1)) - pi;
     s.v[5] = a1;
     return s;
 }
@@ -246,11 +275,11 @@ __device__ __forceinline__ S6<T> wong_stage_lower_s6(const S6<T> &base, const S6
                                                      T high_val, T floor_)
 {
     T theta = T(1);
-    if (wisnan(base_val) || wisnan(high_val) || base_val < floor_) {
+    if (wisnan(base_val) || wisnan(high_val) || flt(base_val, floor_)) {
         theta = T(0);
-    } else if (high_val < floor_) {
+    } else if (flt(high_val, floor_)) {
         T denom = base_val - high_val;
-        theta = denom > T(kTiny) ? (base_val - floor_) / denom : T(0);
+        theta = fgt(denom, T(kTiny)) ? (base_val - floor_) / denom : T(0);
     }
     return blend_s6(base, high, theta);
 }
@@ -262,18 +291,18 @@ __device__ __forceinline__ S6<T> pp_limit_reconstructed_state(const Eos &e, cons
 {
     S6<T> b = base;
     b.v[5] = clamp01_pp(b.v[5]);
-    if (b.v[0] < T(kPpRho) || wisnan(b.v[0])) b.v[0] = T(kPpRho);
-    if (b.v[1] < T(kPpRho) || wisnan(b.v[1])) b.v[1] = T(kPpRho);
+    if (flt(b.v[0], T(kPpRho)) || wisnan(b.v[0])) b.v[0] = T(kPpRho);
+    if (flt(b.v[1], T(kPpRho)) || wisnan(b.v[1])) b.v[1] = T(kPpRho);
     S6<T> s = high;
     s = wong_stage_lower_s6(b, s, b.v[0], s.v[0], T(kPpRho));
     s = wong_stage_lower_s6(b, s, b.v[1], s.v[1], T(kPpRho));
     s = wong_stage_lower_s6(b, s, b.v[5], s.v[5], T(kPpAlpha));
     s = wong_stage_lower_s6(b, s, T(1) - b.v[5], T(1) - s.v[5], T(kPpAlpha));
     s = wong_stage_lower_s6(b, s, rho_ctilde2_sc(e, b), rho_ctilde2_sc(e, s), T(kPpCtilde));
-    if (s.v[0] < T(kPpHsRho) || s.v[1] < T(kPpHsRho) || s.v[5] < T(kPpHsAlpha) ||
-        s.v[5] > T(1) - T(kPpHsAlpha))
+    if (flt(s.v[0], T(kPpHsRho)) || flt(s.v[1], T(kPpHsRho)) || flt(s.v[5], T(kPpHsAlpha)) ||
+        fgt(s.v[5], T(1) - T(kPpHsAlpha)))
         s = b;
-    if (rho_ctilde2_sc(e, s) < T(kPpHsCtilde) || wisnan(s.v[4])) s = b;
+    if (flt(rho_ctilde2_sc(e, s), T(kPpHsCtilde)) || wisnan(s.v[4])) s = b;
     return s;
 }
 
@@ -399,7 +428,7 @@ template <typename T> __device__ __forceinline__ T cator2_val(T em2, T em1, T e0
 template <typename T> __device__ __forceinline__ T thinc_ul(const Eos &e, T vm1, T v0, T v1)
 {
     T result = v0;
-    if ((v1 - v0) * (v0 - vm1) > T(0)) {
+    if (fpos((v1 - v0) * (v0 - vm1))) {
         T qa = T(0.5) * (v1 + vm1);
         T qd = T(0.5) * (v1 - vm1);
         T feng = (v0 - qa) / qd;
@@ -413,7 +442,7 @@ template <typename T> __device__ __forceinline__ T thinc_ul(const Eos &e, T vm1,
 template <typename T> __device__ __forceinline__ T thinc_ur(const Eos &e, T v0, T v1, T v2)
 {
     T result = v1;
-    if ((v2 - v1) * (v1 - v0) > T(0)) {
+    if (fpos((v2 - v1) * (v1 - v0))) {
         T qa = T(0.5) * (v2 + v0);
         T qd = T(0.5) * (v2 - v0);
         T feng = (v1 - qa) / qd;
@@ -430,7 +459,7 @@ template <typename T> __device__ __forceinline__ T mp5_ul(T vm2, T vm1, T v0, T 
     T VOR = T(k1o60) * (T(2) * vm2 - T(13) * vm1 + T(47) * v0 + T(27) * vp1 - T(3) * vp2);
     T VMP = v0 + mm2(vp1 - v0, T(kMp5Alpha) * (v0 - vm1));
     T result = VOR;
-    if ((VOR - v0) * (VOR - VMP) >= T(kEpsM)) {
+    if (fge((VOR - v0) * (VOR - VMP), T(kEpsM))) {
         T DJM1 = vm2 - T(2) * vm1 + v0;
         T DJ = vm1 - T(2) * v0 + vp1;
         T DJP1 = v0 - T(2) * vp1 + vp2;
@@ -453,7 +482,7 @@ template <typename T> __device__ __forceinline__ T mp5_ur(T vm1, T v0, T vp1, T 
     T VOR = T(k1o60) * (T(-3) * vm1 + T(27) * v0 + T(47) * vp1 - T(13) * vp2 + T(2) * vp3);
     T VMP = vp1 + mm2(v0 - vp1, T(kMp5Alpha) * (vp1 - vp2));
     T result = VOR;
-    if ((VOR - vp1) * (VOR - VMP) >= T(kEpsM)) {
+    if (fge((VOR - vp1) * (VOR - VMP), T(kEpsM))) {
         T DJM1 = vm1 - T(2) * v0 + vp1;
         T DJ = v0 - T(2) * vp1 + vp2;
         T DJP1 = vp1 - T(2) * vp2 + vp3;
@@ -567,19 +596,19 @@ __device__ __forceinline__ void hllc(const Side<T> &L, const Side<T> &R, T f[6],
     T SL = wmin(L.un - L.c, n_avg - c_avg);
     T SR = wmax(R.un + R.c, n_avg + c_avg);
     T denom = L.rho * (SL - L.un) - R.rho * (SR - R.un);
-    if (wabs(denom) < T(kTiny)) denom = T(kTiny);
+    if (flt(wabs(denom), T(kTiny))) denom = T(kTiny);
     T SP = (R.p - L.p + L.rho * L.un * (SL - L.un) - R.rho * R.un * (SR - R.un)) / denom;
     T ratioL = (SL - L.un) / (SL - SP);
     T ratioR = (SR - R.un) / (SR - SP);
 
-    if (SL > T(0)) {
+    if (fpos(SL)) {
         f[0] = L.ar1 * L.un;
         f[1] = L.ar2 * L.un;
         f[N] = L.rho * L.un * L.un + L.p;
         f[Tc] = L.rho * L.un * L.ut;
         f[4] = (L.E + L.p) * L.un;
         f[5] = L.a * L.un;
-    } else if (SL <= T(0) && T(0) < SP) {
+    } else if (fle(SL, T(0)) && fpos(SP)) {
         T ratio = ratioL;
         T E_star = L.E + (SP - L.un) * (SP * L.rho + L.p / (SL - L.un));
         f[0] = L.ar1 * L.un + SL * (L.ar1 * ratio - L.ar1);
@@ -588,7 +617,7 @@ __device__ __forceinline__ void hllc(const Side<T> &L, const Side<T> &R, T f[6],
         f[Tc] = (L.rho * L.un * L.ut) + SL * (L.rho * L.ut * ratio - L.rho * L.ut);
         f[4] = (L.E + L.p) * L.un + SL * (E_star * ratio - L.E);
         f[5] = L.a * L.un + SL * (L.a * ratio - L.a);
-    } else if (SP <= T(0) && T(0) <= SR) {
+    } else if (fle(SP, T(0)) && fle(T(0), SR)) {
         T ratio = ratioR;
         T E_star = R.E + (SP - R.un) * (SP * R.rho + R.p / (SR - R.un));
         f[0] = R.ar1 * R.un + SR * (R.ar1 * ratio - R.ar1);

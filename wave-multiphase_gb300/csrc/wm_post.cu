@@ -116,7 +116,9 @@ __global__ void conv_check_kernel(const unsigned long long *in, long long n, uns
         const bool cmp_ok = wm::dlt(x, z) == (x < z) && wm::dlt(z, x) == (z < x) && wm::dneg(x) == (x < 0.0) &&
                             __double_as_longlong(wm::wmin(x, z)) == __double_as_longlong(x < z ? x : z) &&
                             __double_as_longlong(wm::wmax(x, z)) == __double_as_longlong(x > z ? x : z) &&
-                            wm::wsign(x) == (x < 0.0 ? -1.0 : 1.0);
+                            wm::wsign(x) == (x < 0.0 ? -1.0 : 1.0) && wm::dle(x, z) == (x <= z) &&
+                            wm::dle(z, x) == (z <= x) && wm::dpos(x) == (x > 0.0) &&
+                            wm::wisnan(x) == (x != x);
         if (!cmp_ok) atomicAdd(&bad[2], 1ull);
     }
 }
