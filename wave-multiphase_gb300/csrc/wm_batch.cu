@@ -214,14 +214,15 @@ __device__ __forceinline__ void run_phase(const BatchDev &B, int phase, int stag
         case PH_FACES: {
             const bool xf = i >= g.g - 1 && i < g.g + g.nx && j >= g.g && j < g.g + g.ny;
             const bool yf = i >= g.g && i < g.g + g.nx && j >= g.g - 1 && j < g.g + g.ny;
+            const long long kw = kw_of(g, i, j);
             if (FP32) {
                 const Src32 cs{S.cells32, g.nyg};
-                if (xf) face_body<0, VAR, REC, float>(g, S.e, cs, S.prep32, S.fh32, S.fl32, true, true, i, j);
-                if (yf) face_body<1, VAR, REC, float>(g, S.e, cs, S.prep32, S.gh32, S.gl32, true, true, i, j);
+                if (xf) face_body<0, VAR, REC, float>(S.e, GlobalView<0, float, Src32>(g, cs, S.prep32, i, j), S.fh32, S.fl32, true, true, kw);
+                if (yf) face_body<1, VAR, REC, float>(S.e, GlobalView<1, float, Src32>(g, cs, S.prep32, i, j), S.gh32, S.gl32, true, true, kw);
             } else {
                 const Src64 cs{S.q};
-                if (xf) face_body<0, VAR, REC, double>(g, S.e, cs, S.prep, S.fh, S.fl, true, true, i, j);
-                if (yf) face_body<1, VAR, REC, double>(g, S.e, cs, S.prep, S.gh, S.gl, true, true, i, j);
+                if (xf) face_body<0, VAR, REC, double>(S.e, GlobalView<0, double, Src64>(g, cs, S.prep, i, j), S.fh, S.fl, true, true, kw);
+                if (yf) face_body<1, VAR, REC, double>(S.e, GlobalView<1, double, Src64>(g, cs, S.prep, i, j), S.gh, S.gl, true, true, kw);
             }
             break;
         }

@@ -655,33 +655,55 @@ struct Src32 {
     }
 };
 
+// Where a face body reads its inputs: the six fields of the cells at offsets -2..3 along the sweep
+// from the face's cell 0, the first-order cell states (normal and tangential velocity, floored
+// pressure, clamped alpha, sound speed, energy) of cells 0 and 1, and the two sensors of cells
+// -1..2. GlobalView reads the arrays; SmemView (wm_faces.cu) reads a block's staged tile. Both give
+// the same values, so a face's result does not depend on the view.
+template <int DIR, typename T, typename CS>
+struct GlobalView {
+    CS cs;
+    PrepT<T> p;
+    long long kf, kw, sf, sw;
+    __device__ __forceinline__ GlobalView(const Grid &g, const CS &cs_, const PrepT<T> &p_, int i, int j)
+        : cs(cs_), p(p_)
+    {
+        sf = DIR == 0 ? cs.pitch() : 1;
+        sw = DIR == 0 ? g.nyg : 1;
+        kf = (long long)i * cs.pitch() + j;
+        kw = (long long)i * g.nyg + j;
+    }
+    __device__ __forceinline__ void cell(int o, T u[6]) const { cs.load(kf + o * sf, u); }
+    __device__ __forceinline__ T un(int o) const { return (DIR == 0 ? p.lu : p.lv)[kw + o * sw]; }
+    __device__ __forceinline__ T ut(int o) const { return (DIR == 0 ? p.lv : p.lu)[kw + o * sw]; }
+    __device__ __forceinline__ T lp(int o) const { return p.lp[kw + o * sw]; }
+    __device__ __forceinline__ T la(int o) const { return p.la[kw + o * sw]; }
+    __device__ __forceinline__ T lc(int o) const { return p.lc[kw + o * sw]; }
+    __device__ __forceinline__ T lE(int o) const { return p.lE[kw + o * sw]; }
+    __device__ __forceinline__ T sens_c(int o) const { return (DIR == 0 ? p.cx : p.cy)[kw + o * sw]; }
+    __device__ __forceinline__ T sens_s(int o) const { return (DIR == 0 ? p.sx : p.sy)[kw + o * sw]; }
+};
+
 // One face of the sweep in direction DIR: the face between cell (i, j) and its neighbour at +1
 // along the sweep. Callers guarantee that the face exists.
-template <int DIR, int VAR, int REC, typename T, typename CS, typename FT>
-__device__ __forceinline__ void face_body(const Grid &g, const Eos &e, const CS &cs, const PrepT<T> &p,
-                                          const Face<FT> &hi, const Face<FT> &lo, bool do_high,
-                                          bool do_low, int i, int j)
+template <int DIR, int VAR, int REC, typename T, typename V, typename FT>
+__device__ __forceinline__ void face_body(const Eos &e, const V &v, const Face<FT> &hi, const Face<FT> &lo,
+                                          bool do_high, bool do_low, long long kw)
 {
     constexpr int N = DIR == 0 ? 2 : 3;   // normal momentum field
     constexpr int TG = DIR == 0 ? 3 : 2;  // tangential momentum field
-    const long long sf = DIR == 0 ? cs.pitch() : 1;  // stride along the sweep, cell arrays
-    const long long sw = DIR == 0 ? g.nyg : 1;       // stride along the sweep, workspace
-    const long long kf = (long long)i * cs.pitch() + j;
-    const long long kw = (long long)i * g.nyg + j;
 
     // Cells 0 and 1 of the face (i and i+1 along the sweep).
     T U0[6], U1[6];
-    cs.load(kf, U0);
-    cs.load(kf + sf, U1);
+    v.cell(0, U0);
+    v.cell(1, U1);
 
     if (do_low) {  // first-order HLLC of the two cell states (fx_low_kernel, SC:1303-1347)
         Side<T> L, R;
-        const T *un = DIR == 0 ? p.lu : p.lv, *ut = DIR == 0 ? p.lv : p.lu;
         L.ar1 = U0[0]; L.ar2 = U0[1]; L.rho = U0[0] + U0[1];
-        L.un = un[kw]; L.ut = ut[kw]; L.p = p.lp[kw]; L.a = p.la[kw]; L.c = p.lc[kw]; L.E = p.lE[kw];
+        L.un = v.un(0); L.ut = v.ut(0); L.p = v.lp(0); L.a = v.la(0); L.c = v.lc(0); L.E = v.lE(0);
         R.ar1 = U1[0]; R.ar2 = U1[1]; R.rho = U1[0] + U1[1];
-        R.un = un[kw + sw]; R.ut = ut[kw + sw]; R.p = p.lp[kw + sw]; R.a = p.la[kw + sw];
-        R.c = p.lc[kw + sw]; R.E = p.lE[kw + sw];
+        R.un = v.un(1); R.ut = v.ut(1); R.p = v.lp(1); R.a = v.la(1); R.c = v.lc(1); R.E = v.lE(1);
         T f[6], us;
         hllc<DIR>(L, R, f, us);
 #pragma unroll
@@ -691,13 +713,11 @@ __device__ __forceinline__ void face_body(const Grid &g, const Eos &e, const CS 
     if (!do_high) return;
 
     // --- sensors (per-cell, computed by sensor_kernel) -------------------------------------------
-    const T *ci = DIR == 0 ? p.cx : p.cy;
-    const T c_m1 = ci[kw - sw], c_0 = ci[kw], c_p1 = ci[kw + sw], c_p2 = ci[kw + 2 * sw];
+    const T c_m1 = v.sens_c(-1), c_0 = v.sens_c(0), c_p1 = v.sens_c(1), c_p2 = v.sens_c(2);
     const bool use_thinc = flt(wmin(wmin(c_m1, c_0), wmin(c_p1, c_p2)), T(kThincThresh));
     bool smooth = false;
     if (VAR == kSC) {
-        const T *sg = DIR == 0 ? p.sx : p.sy;
-        const T smax = wmax(wmax(sg[kw - sw], sg[kw]), wmax(sg[kw + sw], sg[kw + 2 * sw]));
+        const T smax = wmax(wmax(v.sens_s(-1), v.sens_s(0)), wmax(v.sens_s(1), v.sens_s(2)));
         smooth = flt(smax, T(kSigmaSmooth));
     }
 
@@ -737,7 +757,7 @@ __device__ __forceinline__ void face_body(const Grid &g, const Eos &e, const CS 
 #pragma unroll
             for (int f = 0; f < 6; ++f) u[f] = U1[f];
         } else {
-            cs.load(kf + (o - 2) * sf, u);
+            v.cell(o - 2, u);
         }
         S6<T> w = to_char<DIR>(b, u);
 #pragma unroll
