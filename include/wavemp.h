@@ -159,15 +159,17 @@ int wm_init_dt(wm_handle *h, const wm_fields *q, void *stream);
  * place form, the unlimited ones otherwise; the closures always blend in place. */
 int wm_set_limiter_sweeps(wm_handle *h, int in_place);
 
-/* Precision form: binary32 pre-checks that let cells skip binary64 tests whose outcome they prove
- * (the limiter's bound solves, the combine's clamp / floor / NaN / repair tests), on (1, default)
- * or off (0). Results are the same bits either way; off exists to show that. */
+/* Binary32 pre-checks that let cells skip binary64 tests whose outcome they prove -- the limiter's
+ * bound solves (both forms; the plain form's from binary32 roundings of its binary64 state and
+ * fluxes, with a margin covering those roundings) and, in the precision form, the combine's clamp /
+ * floor / NaN / repair tests -- on (1, default) or off (0). Results are the same bits either way;
+ * off exists to show that. */
 int wm_set_prechecks(wm_handle *h, int on);
-/* Diagnostic of the precision form's limiter pre-check (after wm_compute_fluxes and
- * wm_compute_low_fluxes, like wm_limit_fluxes, whose work it does): every bound pass evaluates both
- * the binary32 pre-check that lets cells skip the binary64 bound solve and the solve itself;
- * *decided counts cells the pre-check decided, *disagreed cells where the solve did not return 1
- * for them (0 when the pre-check's margins hold). No counterpart in the reference. */
+/* Diagnostic of the limiter pre-check (after wm_compute_fluxes and wm_compute_low_fluxes, like
+ * wm_limit_fluxes, whose work it does): every bound pass evaluates both the binary32 pre-check that
+ * lets cells skip the binary64 bound solve and the solve itself; *decided counts cells the
+ * pre-check decided, *disagreed cells where the solve did not return 1 for them (0 when the
+ * pre-check's margins hold). No counterpart in the reference. */
 int wm_verify_limiter_precheck(wm_handle *h, const wm_fields *q, double dt, long long *decided,
                                long long *disagreed, void *stream);
 

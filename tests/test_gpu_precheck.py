@@ -1,4 +1,5 @@
-"""The precision form's binary32 limiter pre-check never decides a cell the binary64 bound solve
+"""The binary32 limiter pre-checks (precision form from its binary32 copies, plain form from
+binary32 roundings of its binary64 state and fluxes) never decide a cell the binary64 bound solve
 would limit (wm_verify_limiter_precheck runs both): on the golden fixtures (the near-vacuum stress
 state included), and on seeded states pushed onto every bound's floor -- partial densities near
 1e-10, volume fractions near 1e-10 and 1 - 1e-10, energies near the rho c~^2 floor -- with time
@@ -33,11 +34,12 @@ def verify(s, q, dt):
     return s.verify_limiter_precheck(q, dt)
 
 
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
 @pytest.mark.parametrize("case", pu.CASES)
-def test_precheck_on_fixtures(case):
+def test_precheck_on_fixtures(case, precision):
     d = pu.load_case(case)
     nx, ny = int(d["meta_nx"]), int(d["meta_ny"])
-    s = Solver(pu.params_from(d, precision="fp32"), nx, ny)
+    s = Solver(pu.params_from(d, precision=precision), nx, ny)
     for scale in (1.0, 4.0):
         decided, disagreed = verify(s, load_state(d), scale * float(d["dt0"]))
         assert disagreed == 0, (case, scale, decided)
@@ -74,10 +76,12 @@ def near_floor_state(nx, ny, seed):
     return p, q
 
 
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
 @pytest.mark.parametrize("seed", [1, 2, 3])
-def test_precheck_near_the_floors(seed):
+def test_precheck_near_the_floors(seed, precision):
     nx, ny = 96, 48
     p, q = near_floor_state(nx, ny, seed)
+    p.precision = precision
     s = Solver(p, nx, ny)
     s.initialize(q)
     dt = s.get_dt(q)
@@ -102,12 +106,14 @@ def run_steps(p, q0, nx, ny, prechecks, steps=3):
     return {k: pu.host(v) for k, v in q.items()}, s.status()
 
 
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
 @pytest.mark.parametrize("seed", [4, 5])
-def test_prechecks_do_not_change_bits(seed):
+def test_prechecks_do_not_change_bits(seed, precision):
     """Steps with the binary32 pre-checks (limiter and combine) equal steps without them, bit for
     bit, on states at the floors (repairs and limiting happen) and on the golden fixtures."""
     nx, ny = 96, 48
     p, q0 = near_floor_state(nx, ny, seed)
+    p.precision = precision
     a, sa = run_steps(p, q0, nx, ny, True)
     b, sb = run_steps(p, q0, nx, ny, False)
     for k in pu.ALL:
@@ -117,7 +123,7 @@ def test_prechecks_do_not_change_bits(seed):
     for case in ("sc_mp5c6_stress", "m10_cfg2", "sc_mp5c6_triple"):
         d = pu.load_case(case)
         nxc, nyc = int(d["meta_nx"]), int(d["meta_ny"])
-        pc = pu.params_from(d, precision="fp32")
+        pc = pu.params_from(d, precision=precision)
         qc = load_state(d)
         a, _ = run_steps(pc, qc, nxc, nyc, True, steps=2)
         b, _ = run_steps(pc, qc, nxc, nyc, False, steps=2)

@@ -183,39 +183,21 @@ struct CellFaces {
 // the test's value, doubled. When this returns true the binary64 bound solve would return 1, so
 // it is skipped; otherwise the caller runs it. The results are the same bits either way.
 template <int STAGE>
-__device__ __forceinline__ bool theta_one_f32(const Eos &e, const Cells32 &c, long long kw, const float *rh,
-                                              const float *rl, float dtf)
+__device__ __forceinline__ bool theta_one_core(const Eos &e, const float *hx, const float *dx, bool lfin)
 {
-    constexpr float kRel = 3.0e-7f;
+    if (!lfin) return false;
     if (STAGE == 0) {
         bool ok = true;
 #pragma unroll
-        for (int k = 0; k < 2; ++k) {
-            const float qv = (k == 0 ? c.ar1 : c.ar2)[kw];
-            const float dh = dtf * rh[k], hf = qv - dh, lf = qv - dtf * rl[k];
-            const float m = kRel * (fabsf(qv) + fabsf(dh));
-            ok = ok && isfinite(lf) && isfinite(hf) && hf >= float(kPpRho) * 1.000001f + m;
-        }
+        for (int k = 0; k < 2; ++k) ok = ok && isfinite(hx[k]) && hx[k] >= float(kPpRho) * 1.000001f + dx[k];
         return ok;
     } else if (STAGE == 1) {
-        const float qv = c.al[kw];
-        const float dh = dtf * rh[5], hf = qv - dh, lf = qv - dtf * rl[5];
-        const float m = kRel * (fabsf(qv) + fabsf(dh));
-        const float lo = float(kPpAlpha) * 1.000001f + m;
-        return isfinite(lf) && isfinite(hf) && hf >= lo && 1.0f - hf >= lo;
+        const float lo = float(kPpAlpha) * 1.000001f + dx[5];
+        return isfinite(hx[5]) && hx[5] >= lo && 1.0f - hx[5] >= lo;
     } else {
-        float hx[6], dx[6];
         bool ok = true;
-        const float *src[6] = {c.ar1, c.ar2, c.ru, c.rv, c.E, c.al};
 #pragma unroll
-        for (int k = 0; k < 6; ++k) {
-            const float qv = src[k][kw];
-            const float dh = dtf * rh[k];
-            hx[k] = qv - dh;
-            dx[k] = kRel * (fabsf(qv) + fabsf(dh));
-            ok = ok && isfinite(hx[k]);
-            if (k >= 2 && k <= 4) ok = ok && isfinite(qv - dtf * rl[k]);
-        }
+        for (int k = 0; k < 6; ++k) ok = ok && isfinite(hx[k]);
         if (!ok) return false;
         // ctilde_surely_above in binary32: V = 2 rho (1+G)(E - floor) - (1+G)(mx^2+my^2) - 2 rho Pi
         float a1 = hx[5];
@@ -241,14 +223,85 @@ __device__ __forceinline__ bool theta_one_f32(const Eos &e, const Cells32 &c, lo
     }
 }
 
+// Precision form: the binary32 states from the stage-start binary32 copies and the binary32
+// residuals the binary64 solve would widen (margin 3e-7 of |Q| + |dt R|).
+template <int STAGE>
+__device__ __forceinline__ bool theta_one_f32(const Eos &e, const Cells32 &c, long long kw, const float *rh,
+                                              const float *rl, float dtf)
+{
+    constexpr float kRel = 3.0e-7f;
+    constexpr int C0 = STAGE == 1 ? 5 : 0, C1 = STAGE == 0 ? 2 : 6;
+    const float *src[6] = {c.ar1, c.ar2, c.ru, c.rv, c.E, c.al};
+    float hx[6], dx[6];
+    bool lfin = true;
+#pragma unroll
+    for (int k = C0; k < C1; ++k) {
+        const float qv = src[k][kw];
+        const float dh = dtf * rh[k];
+        hx[k] = qv - dh;
+        dx[k] = kRel * (fabsf(qv) + fabsf(dh));
+        if (STAGE != 2 || (k >= 2 && k <= 4)) lfin = lfin && isfinite(qv - dtf * rl[k]);
+    }
+    return theta_one_core<STAGE>(e, hx, dx, lfin);
+}
+
+__device__ __forceinline__ bool finite64(double x)
+{
+    return (__double_as_longlong(x) & 0x7ff0000000000000LL) != 0x7ff0000000000000LL;
+}
+
+// Plain form (blends in place): the binary32 states from binary32 roundings of the binary64 state
+// and face fluxes (integer-pipe conversions). Each face value is rounded by 2^-24 of itself, so the
+// residual's error is bounded by its magnitude A = (|F+| + |F-|)/dx + (|G+| + |G-|)/dy (+ the
+// alpha term's), and the state's by about 6 * 2^-24 (|Q| + dt A); the margin is 1e-6 of that.
+// The low-order state of a needed component is finite when its inputs are.
+template <int STAGE>
+__device__ __forceinline__ bool theta_one_f64in(const Grid &g, const Eos &e, const Fields &q, long long kf,
+                                                long long kw, const Face<double> &fh, const Face<double> &gh,
+                                                const Face<double> &fl, const Face<double> &gl, double dt)
+{
+    constexpr int C0 = STAGE == 1 ? 5 : 0, C1 = STAGE == 0 ? 2 : 6;
+    const long long kx = kw - g.nyg, ky = kw - 1;
+    const float dtf = to_f32(dt), idx = g.inv_dxf, idy = g.inv_dyf;
+    float hx[6], dx[6];
+    bool lfin = true;
+#pragma unroll
+    for (int k = C0; k < C1; ++k) {
+        const float xp = to_f32(fh.f[k][kw]), xm = to_f32(fh.f[k][kx]);
+        const float yp = to_f32(gh.f[k][kw]), ym = to_f32(gh.f[k][ky]);
+        float rh = div_sum(xp - xm, idx, yp - ym, idy);
+        float A = (fabsf(xp) + fabsf(xm)) * idx + (fabsf(yp) + fabsf(ym)) * idy;
+        const double qd = q.f[k][kf];
+        bool fin = finite64(qd);
+        if (STAGE != 2 || (k >= 2 && k <= 4))
+            fin = fin && finite64(fl.f[k][kw]) && finite64(fl.f[k][kx]) && finite64(gl.f[k][kw]) &&
+                  finite64(gl.f[k][ky]);
+        if (k == 5) {
+            const float a = to_f32(q.f[F_ALP][kf]);
+            const float sxp = to_f32(fh.f[6][kw]), sxm = to_f32(fh.f[6][kx]);
+            const float syp = to_f32(gh.f[6][kw]), sym = to_f32(gh.f[6][ky]);
+            rh = rh - src_term(a, sxp - sxm, idx) - src_term(a, syp - sym, idy);
+            A += fabsf(a) * ((fabsf(sxp) + fabsf(sxm)) * idx + (fabsf(syp) + fabsf(sym)) * idy);
+            fin = fin && finite64(q.f[F_ALP][kf]) && finite64(fl.f[6][kw]) && finite64(fl.f[6][kx]) &&
+                  finite64(gl.f[6][kw]) && finite64(gl.f[6][ky]);
+        }
+        const float qv = to_f32(qd);
+        hx[k] = qv - dtf * rh;
+        dx[k] = 1.0e-6f * (fabsf(qv) + dtf * A);
+        lfin = lfin && fin && isfinite(A) && isfinite(dx[k]);
+    }
+    return theta_one_core<STAGE>(e, hx, dx, lfin);
+}
+
 // pp_cell_theta_kernel (SC:1397-1476): residuals of the current (partly blended) high-order and of
 // the first-order fluxes, bound solve of this pass. Pass 0 bounds the partial densities, pass 1
 // alpha and 1 - alpha, pass 2 rho c~^2 (theta_cons_stage, SC:268-292); each pass forms only the
 // residual components its bound uses. NP: limiter passes whose blends are deferred (0 when the
 // high-order arrays already hold the blended fluxes, STAGE when they are rebuilt in registers).
-// Precision form: the binary32 pre-check above decides most cells without binary64 arithmetic;
-// VERIFY runs the binary64 solve as well and counts (verify[0]) cells the pre-check decided and
-// (verify[1]) cells where the solve disagreed with it -- a diagnostic of the pre-check's margins.
+// The binary32 pre-checks above decide most cells without the binary64 solve (precision form:
+// theta_one_f32; plain form with blends in place: theta_one_f64in); VERIFY runs the binary64 solve
+// as well and counts (verify[0]) cells the pre-check decided and (verify[1]) cells where the solve
+// disagreed with it -- a diagnostic of the pre-check's margins.
 template <int STAGE, typename FT, int NP = 0, int VERIFY = 0>
 __device__ __forceinline__ double theta_body(const Grid &g, const Eos &e, const Fields &q, const Cells32 &c32,
                                              const Face<FT> &fh, const Face<FT> &gh,
@@ -258,6 +311,11 @@ __device__ __forceinline__ double theta_body(const Grid &g, const Eos &e, const 
 {
     const CellFaces<FT, NP> cf(g, theta, i, j);
     const long long kf = kf_of(q, i, j), kw = cf.kw, kx = cf.kx, ky = cf.ky;
+    bool one = false;
+    if constexpr (sizeof(FT) == 8 && NP == 0) {  // plain form, blends in place
+        one = theta_one_f64in<STAGE>(g, e, q, kf, kw, fh, gh, fl, gl, dt);
+        if (!VERIFY && one && prechecks) return 1.0;
+    }
     const FT idx = cst<FT>(g.inv_dx, g.inv_dxf), idy = cst<FT>(g.inv_dy, g.inv_dyf);
     constexpr int C0 = STAGE == 1 ? 5 : 0, C1 = STAGE == 0 ? 2 : 6;
     FT rh[6], rl[6];
@@ -274,7 +332,6 @@ __device__ __forceinline__ double theta_body(const Grid &g, const Eos &e, const 
             rl[c] = rl[c] - src_term(a, fl.f[6][kw] - fl.f[6][kx], idx) - src_term(a, gl.f[6][kw] - gl.f[6][ky], idy);
         }
     }
-    bool one = false;
     if constexpr (sizeof(FT) == 4) {
         one = theta_one_f32<STAGE>(e, c32, kw, rh, rl, to_f32(dt));
         if (!VERIFY && one && prechecks) return 1.0;

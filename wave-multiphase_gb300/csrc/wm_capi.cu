@@ -418,7 +418,7 @@ int wm_limit_fluxes(wm_handle *h, const wm_fields *q, double dt, void *stream)
                        nullptr, h->cnt, false, as_stream(stream), nullptr, h->prechecks);
     else
         launch_limiter(h->g, h->e, to_fields(q), Cells32{}, h->fh, h->gh, h->fl, h->gl, h->theta, dt, nullptr,
-                       h->cnt, false, as_stream(stream));
+                       h->cnt, false, as_stream(stream), nullptr, h->prechecks);
     return check_launch("wm_limit_fluxes");
 }
 
@@ -523,7 +523,7 @@ static int run_stage(wm_handle *h, const Fields &F, const Fields &O, double dt, 
                            h->cnt, h->defer_limiter, s, nullptr, h->prechecks);
         else
             launch_limiter(h->g, h->e, F, Cells32{}, h->fh, h->gh, h->fl, h->gl, h->theta, dt, dt_dev, h->cnt,
-                           h->defer_limiter, s);
+                           h->defer_limiter, s, nullptr, h->prechecks);
     }
     unsigned flags = final_flags(h, alpha);
     if (!h->prechecks) flags |= FIN_EXACT_CHECKS;
@@ -785,15 +785,18 @@ int wm_verify_limiter_precheck(wm_handle *h, const wm_fields *q, double dt, long
                                long long *disagreed, void *stream)
 {
     if (!h || !fields_ok(h, q) || !std::isfinite(dt) || !decided || !disagreed) return WM_ERR_INVALID;
-    if (!h->fp32) return WM_ERR_INVALID;  // the pre-check belongs to the precision form
     if (!h->fluxes_ready || !h->low_ready) return WM_ERR_STATE;
     unsigned long long *ctr = nullptr, host[2] = {0, 0};
     cudaStream_t s = as_stream(stream);
     cudaError_t err = cudaMalloc(&ctr, sizeof host);
     if (err == cudaSuccess) err = cudaMemsetAsync(ctr, 0, sizeof host, s);
     if (err == cudaSuccess) {
-        launch_limiter(h->g, h->e, to_fields(q), h->cells32, h->fh32, h->gh32, h->fl32, h->gl32, h->theta32, dt,
-                       nullptr, h->cnt, false, s, ctr);
+        if (h->fp32)
+            launch_limiter(h->g, h->e, to_fields(q), h->cells32, h->fh32, h->gh32, h->fl32, h->gl32, h->theta32,
+                           dt, nullptr, h->cnt, false, s, ctr);
+        else
+            launch_limiter(h->g, h->e, to_fields(q), Cells32{}, h->fh, h->gh, h->fl, h->gl, h->theta, dt, nullptr,
+                           h->cnt, false, s, ctr);
         err = cudaGetLastError();
     }
     if (err == cudaSuccess) err = cudaMemcpyAsync(host, ctr, sizeof host, cudaMemcpyDeviceToHost, s);
