@@ -160,10 +160,9 @@ int wm_init_dt(wm_handle *h, const wm_fields *q, void *stream);
 int wm_set_limiter_sweeps(wm_handle *h, int in_place);
 
 /* Binary32 pre-checks that let cells skip binary64 tests whose outcome they prove -- the limiter's
- * bound solves (both forms; the plain form's from binary32 roundings of its binary64 state and
- * fluxes, with a margin covering those roundings) and, in the precision form, the combine's clamp /
- * floor / NaN / repair tests -- on (1, default) or off (0). Results are the same bits either way;
- * off exists to show that. */
+ * bound solves (the plain form's from binary32 roundings of its binary64 state and fluxes, with a
+ * margin covering those roundings) and the combine's clamp / floor / NaN / repair tests -- on (1,
+ * default) or off (0). Results are the same bits either way; off exists to show that. */
 int wm_set_prechecks(wm_handle *h, int on);
 /* Diagnostic of the limiter pre-check (after wm_compute_fluxes and wm_compute_low_fluxes, like
  * wm_limit_fluxes, whose work it does): every bound pass evaluates both the binary32 pre-check that

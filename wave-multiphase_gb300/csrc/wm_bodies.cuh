@@ -388,7 +388,7 @@ __device__ __forceinline__ void blend_body(const Grid &g, const Face<FT> &fh, co
 // cons_to_prim_kernel (SC:840-864) + al_prim copy on every cell, then the dt candidate of
 // timestep_kernel (SC:1686-1705) -- each step selected by `flags`.
 // Returns the bit pattern of the cell's time-step candidate (all ones when it has none).
-// Binary32 pre-check of the combine's admissibility tests (precision form): true only when the
+// Binary32 pre-check of the combine's admissibility tests (both forms): true only when the
 // binary64 state Q certainly has finite components, partial densities at or above the 1e-10 floor,
 // alpha inside [1e-8, 1 - 1e-8] (so neither alpha clamp acts) and no energy repair
 // ((E - kin)(1 + Gamma) - Pi >= 1e-8 (1 + Gamma), enforce_admissible_kernel SC:918-958). Rounding
@@ -468,13 +468,11 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
         // 1/(rho Gamma) of the admissibility check, reused by the primitive recovery when alpha
         // is unchanged by the second clamp
         double rg_a1 = -1.0, rg_rho = 0.0, rg_inv = 0.0, rg_gb = 0.0, rg_pb = 0.0;
-        // Precision form: a binary32 pre-check proves most cells need no clamp, floor, NaN
-        // handling or repair; they skip those binary64 tests (the recovery is unchanged)
+        // A binary32 pre-check proves most cells need no clamp, floor, NaN handling or repair;
+        // they skip those binary64 tests (the recovery is unchanged)
         bool fast = false;
-        if constexpr (sizeof(FT) == 4) {
-            if ((flags & FIN_ADMISSIBLE) && (flags & FIN_PRIM) && !(flags & FIN_EXACT_CHECKS))
-                fast = cell_surely_admissible(e, Q);
-        }
+        if ((flags & FIN_ADMISSIBLE) && (flags & FIN_PRIM) && !(flags & FIN_EXACT_CHECKS))
+            fast = cell_surely_admissible(e, Q);
         if ((flags & FIN_ADMISSIBLE) && fast) {
             const double a1 = Q[F_AL], rho = Q[0] + Q[1];
             double gb, pb;
