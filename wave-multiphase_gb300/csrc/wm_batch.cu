@@ -179,6 +179,10 @@ __device__ __forceinline__ void run_phase(const BatchDev &B, int phase, int stag
     const double alpha = stage == 0 ? 0.0 : (stage == 1 ? 0.75 : 1.0 / 3.0);
     const double beta = stage == 0 ? 1.0 : (stage == 1 ? 0.25 : 2.0 / 3.0);
     const int tid = threadIdx.x;
+    // the face phase sweeps the tile list twice, x faces then y faces (no barrier between them:
+    // they share no data), so that a block runs one face body at a time
+    const int passes = phase == PH_FACES ? 2 : 1;
+    for (int pass = 0; pass < passes; ++pass)
     for (int t = blockIdx.x; t < B.ntiles; t += gridDim.x) {
         const Tile tl = B.tiles[t];
         const SolveDev &S = B.solves[tl.slot];
@@ -212,8 +216,8 @@ __device__ __forceinline__ void run_phase(const BatchDev &B, int phase, int stag
             }
             break;
         case PH_FACES: {
-            const bool xf = i >= g.g - 1 && i < g.g + g.nx && j >= g.g && j < g.g + g.ny;
-            const bool yf = i >= g.g && i < g.g + g.nx && j >= g.g - 1 && j < g.g + g.ny;
+            const bool xf = pass == 0 && i >= g.g - 1 && i < g.g + g.nx && j >= g.g && j < g.g + g.ny;
+            const bool yf = pass == 1 && i >= g.g && i < g.g + g.nx && j >= g.g - 1 && j < g.g + g.ny;
             const long long kw = kw_of(g, i, j);
             if (FP32) {
                 const Src32 cs{S.cells32, g.nyg};
