@@ -87,24 +87,11 @@ template <typename T> __device__ __forceinline__ const T *cell_plane(const Src64
     return cs.q.f[idx[f]];
 }
 
-// Binary32 sweeps: registers capped for 8 resident blocks per SM (no spills; 64 registers instead
-// of 89 lift the warp occupancy from 31 % to 50 % of the latency-bound kernel); binary64: 2.
-// STAGED: the block's tile is staged in shared memory first (binary64: as fast as direct loads, the
-// sweep being bound by the binary64 pipe); otherwise each face reads its stencil directly, through
-// L1 (binary32: 55 ms against 89 ms staged per 10 steps of the triple point -- the staging's
-// barrier serialises loads and compute within a block, and L1 already serves the reuse).
-template <int DIR, int VAR, int REC, typename T, typename CS, typename FT, bool STAGED>
-__global__ void __launch_bounds__(FBX *FBY, sizeof(T) == 4 ? 8 : 2)
-face_kernel(Grid g, Eos e, CS cs, PrepT<T> p, Face<FT> hi, Face<FT> lo, int do_high, int do_low)
+// The staged form of face_kernel: stage the block's tile, then compute its faces from it.
+template <int DIR, int VAR, int REC, typename T, typename CS, typename FT>
+__device__ __forceinline__ void staged_faces(const Grid &g, const Eos &e, const CS &cs, const PrepT<T> &p,
+                                             const Face<FT> &hi, const Face<FT> &lo, int do_high, int do_low)
 {
-    if constexpr (!STAGED) {
-        const int j = blockIdx.x * blockDim.x + threadIdx.x + (DIR == 0 ? g.g : g.g - 1);
-        const int i = blockIdx.y * blockDim.y + threadIdx.y + (DIR == 0 ? g.g - 1 : g.g);
-        if (i >= g.g + g.nx || j >= g.g + g.ny) return;
-        face_body<DIR, VAR, REC, T>(e, GlobalView<DIR, T, CS>(g, cs, p, i, j), hi, lo, do_high != 0, do_low != 0,
-                                    (long long)i * g.nyg + j);
-        return;
-    }
     using S = TileShape<DIR>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sm = reinterpret_cast<T *>(smem_raw);
@@ -146,6 +133,27 @@ face_kernel(Grid g, Eos e, CS cs, PrepT<T> p, Face<FT> hi, Face<FT> lo, int do_h
         v.bs = ti * S::cols(3) + tj + 1;
     }
     face_body<DIR, VAR, REC, T>(e, v, hi, lo, do_high != 0, do_low != 0, (long long)i * g.nyg + j);
+}
+
+// Binary32 sweeps: registers capped for 8 resident blocks per SM (no spills; 64 registers instead
+// of 89 lift the warp occupancy from 31 % to 50 % of the latency-bound kernel); binary64: 2.
+// STAGED: the block's tile is staged in shared memory first (binary64: as fast as direct loads, the
+// sweep being bound by the binary64 pipe); otherwise each face reads its stencil directly, through
+// L1 (binary32: 55 ms against 89 ms staged per 10 steps of the triple point -- the staging's
+// barrier serialises loads and compute within a block, and L1 already serves the reuse).
+template <int DIR, int VAR, int REC, typename T, typename CS, typename FT, bool STAGED>
+__global__ void __launch_bounds__(FBX *FBY, sizeof(T) == 4 ? 8 : 2)
+face_kernel(Grid g, Eos e, CS cs, PrepT<T> p, Face<FT> hi, Face<FT> lo, int do_high, int do_low)
+{
+    if constexpr (!STAGED) {
+        const int j = blockIdx.x * blockDim.x + threadIdx.x + (DIR == 0 ? g.g : g.g - 1);
+        const int i = blockIdx.y * blockDim.y + threadIdx.y + (DIR == 0 ? g.g - 1 : g.g);
+        if (i >= g.g + g.nx || j >= g.g + g.ny) return;
+        face_body<DIR, VAR, REC, T>(e, GlobalView<DIR, T, CS>(g, cs, p, i, j), hi, lo, do_high != 0, do_low != 0,
+                                    (long long)i * g.nyg + j);
+    } else {
+        staged_faces<DIR, VAR, REC, T>(g, e, cs, p, hi, lo, do_high, do_low);
+    }
 }
 
 template <int DIR, int VAR, int REC, typename T, typename CS, typename FT>
