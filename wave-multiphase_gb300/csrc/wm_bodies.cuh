@@ -460,7 +460,8 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
                 double rc;
                 if constexpr (sizeof(FT) == 4) rc = to_f64(res[c]);
                 else rc = res[c];
-                double base = __dmul_rn(beta, __fma_rn(-dt, rc, Q[c]));
+                double base = __fma_rn(-dt, rc, Q[c]);
+                if (beta != 1.0) base = __dmul_rn(beta, base);  // 1 * x is x: stage 1 skips it
                 Q[c] = (flags & FIN_OLD_READ) ? __fma_rn(alpha, old.f[c][ko], base) : base;
             }
             wrote_q = true;
