@@ -161,9 +161,18 @@ int wm_set_limiter_sweeps(wm_handle *h, int in_place);
 
 /* Binary32 pre-checks that let cells skip binary64 tests whose outcome they prove -- the limiter's
  * bound solves (the plain form's from binary32 roundings of its binary64 state and fluxes, with a
- * margin covering those roundings) and the combine's clamp / floor / NaN / repair tests -- on (1,
- * default) or off (0). Results are the same bits either way; off exists to show that. */
+ * margin covering those roundings), the combine's clamp / floor / NaN / repair tests, and the THINC
+ * switch of the binary64 sensors (cator2 of the cell entropies against 0.35, SC:318-325, 1028-1032:
+ * binary32 entropies with an error bound, the binary64 pow only where the bound does not settle
+ * it) -- on (1, default) or off (0). Results are the same bits either way; off exists to show that. */
 int wm_set_prechecks(wm_handle *h, int on);
+/* Diagnostic of the THINC switch pre-check on state q (binary64, any form): for every cell and
+ * direction with a full five-cell stencil, both the binary32 pre-check and the binary64 decision
+ * are evaluated from q. *checked counts the stencils, *decided those the pre-check settled,
+ * *disagreed those it settled differently from the binary64 decision (0 when its error bound
+ * holds). No counterpart in the reference. */
+int wm_verify_switch_precheck(wm_handle *h, const wm_fields *q, long long *checked, long long *decided,
+                              long long *disagreed, void *stream);
 /* Diagnostic of the limiter pre-check (after wm_compute_fluxes and wm_compute_low_fluxes, like
  * wm_limit_fluxes, whose work it does): every bound pass evaluates both the binary32 pre-check that
  * lets cells skip the binary64 bound solve and the solve itself; *decided counts cells the
@@ -315,7 +324,7 @@ int wm_profile_read(wm_handle *h, double ms[WM_PROF_GROUPS], long long launches[
  * device memory from its own pool and does not let libraries call cudaMalloc, or a loop that must
  * never wait on the allocator. Runs the same stage as wm_rhs_stage, without a handle: the
  * workspace is a device array inside the library, sized for grids of at most WM_STATIC_MAX_CELLS
- * padded cells, (nx + 2g) * (ny + 2g) <= 32768 (about 10.5 MiB, held by every GPU that loads the
+ * padded cells, (nx + 2g) * (ny + 2g) <= 32768 (about 10.75 MiB, held by every GPU that loads the
  * library until the process exits). Larger grids are rejected with WM_ERR_INVALID and a message in
  * wm_last_error(). Calls no cudaMalloc or cudaFree. The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress); make that first call before any stream capture.

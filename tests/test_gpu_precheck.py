@@ -129,3 +129,83 @@ def test_prechecks_do_not_change_bits(seed, precision):
         b, _ = run_steps(pc, qc, nxc, nyc, False, steps=2)
         for k in pu.ALL:
             assert np.array_equal(a[k], b[k], equal_nan=True), (case, k)
+
+
+# ---- the THINC switch pre-check (binary32 entropies with an error bound) ----------------------
+@pytest.mark.parametrize("case", pu.CASES)
+def test_switch_precheck_on_fixtures(case):
+    d = pu.load_case(case)
+    nx, ny = int(d["meta_nx"]), int(d["meta_ny"])
+    s = Solver(pu.params_from(d), nx, ny)
+    checked, decided, disagreed = s.verify_switch_precheck(load_state(d))
+    assert disagreed == 0, (case, checked, decided)
+    assert checked > 0
+
+
+def switch_states(seed, nx=128, ny=64):
+    """Seeded states whose entropy stencils put cator2 near its 0.35 threshold: entropies
+    s0 (1 + N(0, sigma)) with sigma spread over decades (the switch turns where the stencil
+    differences reach sqrt(eps) ~ 0.07 of the entropy scale), pressures and densities scaled over
+    1e-6 .. 1e6, both fluids and mixtures."""
+    rng = np.random.default_rng(seed)
+    g = 5
+    shape = (nx + 2 * g, ny + 2 * g)
+    for p_scale in (1e-6, 1e-2, 1.0, 1e2, 1e5, 1e9):
+        for sigma in (1e-4, 3e-3, 3e-2, 0.3):
+            al = np.clip(rng.random(shape), 1e-8, 1 - 1e-8)
+            al[rng.random(shape) < 0.3] = 1 - 1e-8
+            al[rng.random(shape) < 0.3] = 1e-8
+            rho = np.exp(rng.uniform(-2, 2)) * (1.0 + 0.1 * rng.random(shape))
+            p = p_scale * (1.0 + sigma * rng.standard_normal(shape))
+            q = {k: torch.zeros(shape, dtype=torch.float64, device="cuda") for k in pu.ALL}
+            q["ar1"].copy_(torch.from_numpy(al * rho))
+            q["ar2"].copy_(torch.from_numpy((1 - al) * rho))
+            q["al"].copy_(torch.from_numpy(al))
+            q["al_prim"].copy_(torch.from_numpy(al))
+            q["p_p"].copy_(torch.from_numpy(p))
+            yield p_scale, sigma, q
+
+
+@pytest.mark.parametrize("seed", [11, 12])
+def test_switch_precheck_near_the_threshold(seed):
+    nx, ny = 128, 64
+    params = wavemp.SolverParams(dx=1.0 / nx, dy=0.5 / ny, gamma1=4.4, pinf1=6e8, recon="mp5c6")
+    s = Solver(params, nx, ny)
+    undecided = 0
+    for p_scale, sigma, q in switch_states(seed, nx, ny):
+        checked, decided, disagreed = s.verify_switch_precheck(q)
+        assert disagreed == 0, (p_scale, sigma, checked, decided)
+        undecided += checked - decided
+    assert undecided > 0  # the bound is exercised: some stencils are left to binary64
+
+
+def test_switch_precheck_settles_the_triple_point():
+    """On the dimensionless triple point nearly every stencil is settled in binary32."""
+    nx, ny = 448, 192
+    q = ic.triple_point(nx, ny)
+    s = Solver(wavemp.SolverParams(dx=7.0 / nx, dy=3.0 / ny, gamma1=1.5, pinf1=0.0, gamma2=1.4, pinf2=0.0,
+                                   recon="mp5c6", bc=("slip",) * 4), nx, ny)
+    s.initialize(q)
+    old = alloc_state(nx, ny, names=wavemp.FIELDS)
+    s.init_dt(q)
+    for _ in range(20):
+        s.step(q, old, None, sync=False)
+    checked, decided, disagreed = s.verify_switch_precheck(q)
+    assert disagreed == 0
+    assert decided >= 0.99 * checked, (checked, decided)
+
+
+@pytest.mark.parametrize("case", ["sc_mp5c6_triple", "sc_cfg0", "m10_cfg2"])
+def test_switch_precheck_does_not_change_bits(case):
+    """Steps with the switch pre-check equal steps without it, bit for bit, in the plain form and
+    in the precision form with binary64 switches."""
+    d = pu.load_case(case)
+    nxc, nyc = int(d["meta_nx"]), int(d["meta_ny"])
+    for precision, sw in (("fp64", False), ("fp32", True)):
+        pc = pu.params_from(d, precision=precision)
+        pc.fp64_switches = sw
+        qc = load_state(d)
+        a, _ = run_steps(pc, qc, nxc, nyc, True, steps=3)
+        b, _ = run_steps(pc, qc, nxc, nyc, False, steps=3)
+        for k in pu.ALL:
+            assert np.array_equal(a[k], b[k], equal_nan=True), (case, precision, k)

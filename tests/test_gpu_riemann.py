@@ -6,8 +6,11 @@ tests/riemann_cases.py) on 400 cells laid along x and along y, with every scheme
   (max |rho - rho_oracle| <= 1e-9 max rho after 200-640 steps), so the density L1 error against the
   exact solution is the oracle's, below the bound the oracle tests pin;
 * the tube along y gives the tube along x (the y sweeps are the x sweeps with u and v exchanged);
-* the precision form (binary32 reconstruction and fluxes) stays within 1e-5 of the binary64
-  density in L1 and within the same bound against the exact solution;
+* the precision form (binary32 reconstruction and fluxes) stays within the same bound against the
+  exact solution, and its distance to the binary64 density (L1) is below a tenth of the binary64
+  error against the exact solution (measured: 4e-8 .. 5.5e-6, against 7e-4 .. 3.5e-3): binary32
+  moves knife-edge decisions of the scheme (the THINC and MP5 switches) at a few faces, which costs
+  far less than the discretisation does;
 * volume fraction in [1e-8, 1 - 1e-8] and partial densities at or above the floor after the run.
 """
 import numpy as np
@@ -74,11 +77,13 @@ def test_shock_tube_fp64(name, variant, recon):
 def test_shock_tube_precision_form(name, variant, recon):
     case = rc.CASES[name]
     ref = rc.density_line(run_device(case, variant, recon, "x"), N, "x")
+    discretisation = rc.l1_error(case, ref)
     for along in ("x", "y"):
         f = run_device(case, variant, recon, along, precision="fp32")
         rho = rc.density_line(f, N, along)
         assert np.isfinite(rho).all()
         l1 = np.abs(rho - ref).sum() / np.abs(ref).sum()
-        assert l1 <= 1e-5, f"{name} {variant}/{recon} along {along}: fp32 vs fp64 L1 {l1:.3e}"
+        assert l1 <= 0.1 * discretisation, \
+            f"{name} {variant}/{recon} along {along}: fp32 vs fp64 L1 {l1:.3e}, fp64 vs exact {discretisation:.3e}"
         assert rc.l1_error(case, rho) <= BOUND_400[name]
         check_bounds(f, along)

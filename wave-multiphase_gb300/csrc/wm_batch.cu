@@ -202,17 +202,17 @@ __device__ __forceinline__ void run_phase(const BatchDev &B, int phase, int stag
         case PH_PREP:
             if (in) {
                 if (FP32)
-                    prep32_body(g, S.e, S.q, S.prep32, S.cells32, B.sw64 != 0, i, j);
+                    prep32_body(g, S.e, S.q, S.prep32, S.cells32, B.sw64 != 0, true, i, j);
                 else
-                    prep_body(g, S.e, S.q, S.prep, i, j);
+                    prep_body(g, S.e, S.q, S.prep, true, i, j);
             }
             break;
         case PH_SENSOR:
             if (in) {
                 if (FP32)
-                    sensor32_body(g, S.q, S.prep32, S.cells32, VAR == kSC, B.sw64 != 0, i, j);
+                    sensor32_body(g, S.e, S.q, S.prep32, S.cells32, VAR == kSC, B.sw64 != 0, true, i, j);
                 else
-                    sensor_body(g, S.q, S.prep, VAR == kSC, i, j);
+                    sensor_body(g, S.e, S.q, S.prep, VAR == kSC, true, i, j);
             }
             break;
         case PH_FACES: {
@@ -506,7 +506,7 @@ size_t wm_solve_workspace_bytes(const wm_batch_params *p, int nx, int ny)
     const int g = p->g;
     if (p->precision == WM_PREC_FP32)
         return (size_t)(28 + 3 + 11 + 9) * arr_bytes(nx, ny, g, 4) + arr_bytes(nx, ny, g, 8);
-    return (size_t)42 * arr_bytes(nx, ny, g, 8);
+    return (size_t)42 * arr_bytes(nx, ny, g, 8) + arr_bytes(nx, ny, g, 4);
 }
 
 int wm_batch_create(const wm_batch_params *p, int capacity, wm_batch **out)
@@ -623,6 +623,7 @@ int wm_batch_set(wm_batch *b, int slot, const wm_solve_desc *d, void *workspace,
         C.u = f4[45]; C.v = f4[46]; C.E = f4[47];
         for (int k = 0; k < 3; ++k) S.theta32[k] = f4[48 + k];
         P.ent64 = reinterpret_cast<double *>(cur);
+        P.ent32 = P.ent;
     } else {
         size_t a8 = arr_bytes(d->nx, d->ny, g, 8);
         double *f8[42];
@@ -637,6 +638,8 @@ int wm_batch_set(wm_batch *b, int slot, const wm_solve_desc *d, void *workspace,
         Prep &P = S.prep;
         P.sx = f8[31]; P.sy = f8[32]; P.ent = f8[33]; P.cx = f8[34]; P.cy = f8[35]; P.lu = f8[36];
         P.lv = f8[37]; P.lp = f8[38]; P.la = f8[39]; P.lc = f8[40]; P.lE = f8[41];
+        P.ent64 = f8[33];
+        P.ent32 = reinterpret_cast<float *>(cur);  // the binary32 entropy of the switch pre-check
     }
     slot_scalars(b, slot, S);
     // zero the slot's scalars (t, steps, done) and set the CFL accumulator to get_dt's start value

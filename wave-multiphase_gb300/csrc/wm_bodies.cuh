@@ -23,17 +23,143 @@ __device__ __forceinline__ void count_if(unsigned long long *ctr, bool pred)
     if (b && (threadIdx.x & 31) == (__ffs(mask) - 1)) atomicAdd(ctr, (unsigned long long)__popc(b));
 }
 
-// The cell entropy of cell_entropy (SC:308-314), binary64: p / rho^gamma, gamma = gamma(alpha).
+// The cell entropy of cell_entropy (SC:308-314), binary64: p / rho^gamma, gamma = gamma(alpha),
+// with rho clamped below at 1e-20 as the reference clamps it.
+__device__ __forceinline__ double entropy64_r(double ge, double rho_e, double pp) { return pp / pow(rho_e, ge); }
 __device__ __forceinline__ double entropy64(double ge, double ar1, double ar2, double pp)
 {
     double rho_e = ar1 + ar2;
     if (rho_e < kTiny) rho_e = kTiny;
-    return pp / pow(rho_e, ge);
+    return entropy64_r(ge, rho_e, pp);
+}
+
+// A sensor value reduced to its side of the face sweep's threshold: 0 below it, 1 at or above it,
+// NaN for NaN. The map is monotone, so it commutes with the reference's a<b?a:b minimum and maximum
+// over the four cells of a face (NaN included), and (encoded < threshold) holds exactly when
+// (value < threshold) does: the binary32 sweep makes the decisions of the binary64 values.
+__device__ __forceinline__ float side_of(double v, double threshold)
+{
+    return v < threshold ? 0.0f : (isnan(v) ? __int_as_float(0x7fc00000) : 1.0f);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Binary32 pre-check of the THINC switch. The entropies reach the face sweep only through one
+// comparison, cator2_val < 0.35 (SC:318-325, 1028-1032), so the sensor pass first makes it from
+// binary32 entropies with an error bound, and falls back to the binary64 entropies (binary64 pow,
+// as the reference) only where the bound does not settle it. The decision is the binary64 one in
+// every case: the results are the same bits.
+//
+// entropy32: p / rho^gamma as p * 2^(-gamma log2 rho), from integer-pipe roundings of the binary64
+// rho (already clamped), gamma and p. Relative error against p / rho^gamma of those binary64
+// inputs, for |t| = |gamma log2 rho| <= 64 and gamma <= 64: the rounded rho moves log2 rho by
+// 2^-23.47; log2f (1 ulp), the rounded gamma and the product move t by at most
+// gamma 2^-23.47 + |t| 2^-22; exp2f (2 ulp), the rounded p and the final product add 2^-21.4; in
+// all below 2^-21.4 + ln2 (gamma 2^-23.47 + |t| 2^-22) <= 1.6e-5. kEnt32Rel = 2^-14 is four
+// times that (and covers the binary64 pow's few ulp). Outside those limits, or for operands that
+// are not finite and normal (|p| in [2^-60, 2^60], so the result is normal too), it returns NaN:
+// no pre-check with that cell. p = 0 gives the exact 0.
+constexpr float kEnt32Rel = 6.1035156e-05f;  // 2^-14
+// Prep keeps the binary64 entropy of the cells whose binary32 entropy is NaN or above this in
+// magnitude: there the bound (about 4e-4 of the entropies) is too wide to settle smooth stencils,
+// so the sensor pass will need it. Below it the sensor evaluates the rare one it needs itself.
+constexpr float kEnt64Scale = 64.0f;
+
+__device__ __forceinline__ float entropy32(double ge, double rho_e, double pp)
+{
+    if (pp == 0.0) return 0.0f;
+    const float r = to_f32(rho_e), gm = to_f32(ge), pf = to_f32(pp), ap = fabsf(pf);
+    const float nan = __int_as_float(0x7fc00000);
+    if (!(r >= 1.17549435e-38f && r <= 3.0e38f) || !(gm > 0.0f && gm <= 64.0f) ||
+        !(ap >= 8.67361738e-19f && ap <= 1.15292150e18f))
+        return nan;
+    const float t = gm * log2f(r);
+    if (!(fabsf(t) <= 64.0f)) return nan;
+    return pf * exp2f(-t);
+}
+
+// The switch from five binary32 entropies: 0 (cator2 < 0.35) or 1 (>= 0.35) when the bound settles
+// it, -1 when it does not (NaN entropies included). With a = aa and b = bb of cator2_val,
+// cator2 < 0.35  <=>  f = 2ab - 0.35 (a^2 + b^2) + 0.65 eps < 0 (its denominator is positive).
+// Each binary32 entropy is within kEnt32Rel of the binary64 one, so a is within
+// da = (kEnt32Rel + 2^-20) Ma of the binary64 aa, Ma the sum of the magnitudes of aa's terms (2^-20
+// covers the roundings of both evaluations of aa); b likewise. f is bounded over that box by
+// interval arithmetic; a decision needs the whole interval, widened by 2^-19 of the magnitudes for
+// the binary32 roundings of f, on one side of zero.
+__device__ __forceinline__ int thinc_side_pre(float em2, float em1, float e0, float ep1, float ep2)
+{
+    const float k13 = 13.0f / 12.0f;
+    const float a = 0.25f * fabsf(em2 - 4.0f * em1 + 3.0f * e0) + k13 * fabsf(e0 - 2.0f * em1 + em2);
+    const float b = 0.25f * fabsf(3.0f * e0 - 4.0f * ep1 + ep2) + k13 * fabsf(e0 - 2.0f * ep1 + ep2);
+    const float m2 = fabsf(em2), m1 = fabsf(em1), m0 = fabsf(e0), n1 = fabsf(ep1), n2 = fabsf(ep2);
+    const float ma = 0.25f * (m2 + 4.0f * m1 + 3.0f * m0) + k13 * (m0 + 2.0f * m1 + m2);
+    const float mb = 0.25f * (3.0f * m0 + 4.0f * n1 + n2) + k13 * (m0 + 2.0f * n1 + n2);
+    const float rel = kEnt32Rel + 9.53674316e-07f;
+    const float da = rel * ma, db = rel * mb;
+    const float alo = fmaxf(a - da, 0.0f), ahi = a + da, blo = fmaxf(b - db, 0.0f), bhi = b + db;
+    const float c = 0.65f * float(kYuxin);
+    const float flo = 2.0f * alo * blo - 0.35f * (ahi * ahi + bhi * bhi) + c;
+    const float fhi = 2.0f * ahi * bhi - 0.35f * (alo * alo + blo * blo) + c;
+    const float m = 1.90734863e-06f * (2.0f * ahi * bhi + 0.35f * (ahi * ahi + bhi * bhi) + c);
+    if (flo > m) return 1;
+    if (fhi < -m) return 0;
+    return -1;
+}
+
+// The THINC switch of the cell at kw (its state at kf) along one direction -- workspace stride sw,
+// state stride sq -- as side_of's code. With the pre-checks: the binary32 decision where it is
+// settled, else cator2_val of the binary64 entropies, those prep kept (binary32 entropy NaN or
+// above kEnt64Scale in magnitude) read back, the others evaluated here from the cell state exactly
+// as prep evaluates them. Without: the binary64 entropies prep kept for every cell.
+template <typename PT>
+__device__ __forceinline__ float thinc_side(const Eos &e, const Fields &q, const PrepT<PT> &p, long long kw,
+                                            long long kf, long long sw, long long sq, bool prechecks)
+{
+    double v[5];
+    if (prechecks) {
+        float s[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) s[k] = p.ent32[kw + (k - 2) * sw];
+        const int d = thinc_side_pre(s[0], s[1], s[2], s[3], s[4]);
+        if (d >= 0) return float(d);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            if (!(fabsf(s[k]) <= kEnt64Scale)) {
+                v[k] = p.ent64[kw + (k - 2) * sw];
+            } else {
+                const long long c = kf + (k - 2) * sq;
+                double ge, pie;
+                mix_gamma_pinf(e, q.f[F_AL][c], ge, pie);
+                v[k] = entropy64(ge, q.f[F_AR1][c], q.f[F_AR2][c], q.f[F_P][c]);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 5; ++k) v[k] = p.ent64[kw + (k - 2) * sw];
+    }
+    return side_of(cator2_val(v[0], v[1], v[2], v[3], v[4]), kThincThresh);
+}
+
+// The entropy prep leaves for thinc_side: the binary32 one and, where thinc_side will read it,
+// the binary64 one (every cell without the pre-checks).
+template <typename PT>
+__device__ __forceinline__ void store_entropy(const PrepT<PT> &p, long long kw, double ge, double ar1, double ar2,
+                                              double pp, bool prechecks)
+{
+    double rho_e = ar1 + ar2;
+    if (rho_e < kTiny) rho_e = kTiny;
+    if (prechecks) {
+        const float s32 = entropy32(ge, rho_e, pp);
+        p.ent32[kw] = s32;
+        if (!(fabsf(s32) <= kEnt64Scale)) p.ent64[kw] = entropy64_r(ge, rho_e, pp);
+    } else {
+        p.ent64[kw] = entropy64_r(ge, rho_e, pp);
+    }
 }
 
 // Entropy (SC:308-314) and the first-order HLLC cell state of fx_low_kernel (SC:1309-1327), both
 // pure functions of one cell, computed once per cell instead of once per face that reads them.
-__device__ __forceinline__ void prep_body(const Grid &g, const Eos &e, const Fields &q, const Prep &p, int i, int j)
+__device__ __forceinline__ void prep_body(const Grid &g, const Eos &e, const Fields &q, const Prep &p, bool prechecks,
+                                          int i, int j)
 {
     long long kf = kf_of(q, i, j), kw = kw_of(g, i, j);
     double ar1 = q.f[F_AR1][kf], ar2 = q.f[F_AR2][kf], ru = q.f[F_RU][kf], rv = q.f[F_RV][kf];
@@ -41,7 +167,7 @@ __device__ __forceinline__ void prep_body(const Grid &g, const Eos &e, const Fie
 
     double ge, pie;
     mix_gamma_pinf(e, al, ge, pie);
-    p.ent[kw] = entropy64(ge, ar1, ar2, pp);
+    store_entropy(p, kw, ge, ar1, ar2, pp, prechecks);
 
     double rho = ar1 + ar2;
     double ir = 1.0 / rho;
@@ -85,26 +211,15 @@ __device__ __forceinline__ void ducros_xy(const Fields &q, int i, int j, double 
     sy = (aa / (bb + 1.0e-30)) * ducros;
 }
 
-// A sensor value reduced to its side of the face sweep's threshold: 0 below it, 1 at or above it,
-// NaN for NaN. The map is monotone, so it commutes with the reference's a<b?a:b minimum and maximum
-// over the four cells of a face (NaN included), and (encoded < threshold) holds exactly when
-// (value < threshold) does: the binary32 sweep makes the decisions of the binary64 values.
-__device__ __forceinline__ float side_of(double v, double threshold)
+// The THINC switch per cell and direction (cator2_val < 0.35, SC:318-325, 1028-1032) as side_of's
+// code, and the Ducros x pressure sensor (ducros_kernel, SC:875-916).
+__device__ __forceinline__ void sensor_body(const Grid &g, const Eos &e, const Fields &q, const Prep &p, int sc,
+                                            bool prechecks, int i, int j)
 {
-    return v < threshold ? 0.0f : (isnan(v) ? __int_as_float(0x7fc00000) : 1.0f);
-}
-
-// Smoothness indicator per cell and direction (cator2_val, SC:318-325) and the Ducros x pressure
-// sensor (ducros_kernel, SC:875-916).
-__device__ __forceinline__ void sensor_body(const Grid &g, const Fields &q, const Prep &p, int sc, int i, int j)
-{
-    long long kw = kw_of(g, i, j);
+    long long kw = kw_of(g, i, j), kf = kf_of(q, i, j);
     const long long W = g.nyg;
-    const double *en = p.ent;
-    if (i >= 2 && i < g.nxg - 2)
-        p.cx[kw] = cator2_val(en[kw - 2 * W], en[kw - W], en[kw], en[kw + W], en[kw + 2 * W]);
-    if (j >= 2 && j < g.nyg - 2)
-        p.cy[kw] = cator2_val(en[kw - 2], en[kw - 1], en[kw], en[kw + 1], en[kw + 2]);
+    if (i >= 2 && i < g.nxg - 2) p.cx[kw] = thinc_side(e, q, p, kw, kf, W, q.pitch, prechecks);
+    if (j >= 2 && j < g.nyg - 2) p.cy[kw] = thinc_side(e, q, p, kw, kf, 1, 1, prechecks);
     if (!sc) return;
     if (i < 2 || i >= g.nxg - 2 || j < 2 || j >= g.nyg - 2) {
         p.sx[kw] = 1.0;
@@ -575,7 +690,8 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
 // first-order HLLC cell state whose pressure floor and the numerator of its sound speed are
 // recovered in binary64 (the stiffened-gas p + p_inf cancels to round-off of p_inf ~ 6e8 in
 // binary32).
-__device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const Fields &q, const PrepT<float> &p, const Cells32 &c, bool sw64, int i, int j)
+__device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const Fields &q, const PrepT<float> &p, const Cells32 &c, bool sw64,
+                                            bool prechecks, int i, int j)
 {
     long long kf = kf_of(q, i, j), kw = kw_of(g, i, j);
     const double ar1 = q.f[F_AR1][kf], ar2 = q.f[F_AR2][kf], ru = q.f[F_RU][kf], rv = q.f[F_RV][kf];
@@ -592,10 +708,10 @@ __device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const F
     c.v[kw] = to_f32(q.f[F_V][kf]);
     c.E[kw] = to_f32(q.f[F_E][kf]);
 
-    if (sw64) {  // binary64 switches: the entropy of the binary64 form
+    if (sw64) {  // binary64 switches: the entropy of the binary64 form (ent32 is the ent array)
         double ge, pie;
         mix_gamma_pinf(e, al, ge, pie);
-        p.ent64[kw] = entropy64(ge, ar1, ar2, pp);
+        store_entropy(p, kw, ge, ar1, ar2, pp, prechecks);
     } else {
         float ge, pie;
         mix_gamma_pinf(e, alf, ge, pie);
@@ -633,17 +749,15 @@ __device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const F
 }
 
 // Smoothness indicators and Ducros sensor in binary32 (sensor_kernel's arithmetic).
-__device__ __forceinline__ void sensor32_body(const Grid &g, const Fields &q, const PrepT<float> &p, const Cells32 &c, int sc,
-                                              bool sw64, int i, int j)
+__device__ __forceinline__ void sensor32_body(const Grid &g, const Eos &e, const Fields &q, const PrepT<float> &p,
+                                              const Cells32 &c, int sc, bool sw64, bool prechecks, int i, int j)
 {
     long long kw = kw_of(g, i, j);
     const long long W = g.nyg;
     if (sw64) {  // the binary64 sensors, stored as their side of the sweep's thresholds
-        const double *en = p.ent64;
-        if (i >= 2 && i < g.nxg - 2)
-            p.cx[kw] = side_of(cator2_val(en[kw - 2 * W], en[kw - W], en[kw], en[kw + W], en[kw + 2 * W]), kThincThresh);
-        if (j >= 2 && j < g.nyg - 2)
-            p.cy[kw] = side_of(cator2_val(en[kw - 2], en[kw - 1], en[kw], en[kw + 1], en[kw + 2]), kThincThresh);
+        const long long kf = kf_of(q, i, j);
+        if (i >= 2 && i < g.nxg - 2) p.cx[kw] = thinc_side(e, q, p, kw, kf, W, q.pitch, prechecks);
+        if (j >= 2 && j < g.nyg - 2) p.cy[kw] = thinc_side(e, q, p, kw, kf, 1, 1, prechecks);
         if (!sc) return;
         if (i < 2 || i >= g.nxg - 2 || j < 2 || j >= g.nyg - 2) {
             p.sx[kw] = side_of(1.0, kSigmaSmooth);

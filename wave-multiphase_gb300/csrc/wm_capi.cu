@@ -43,7 +43,8 @@ size_t array_bytes(int nx, int ny, int g, size_t elem = sizeof(double))
     return (n + kAlign - 1) / kAlign * kAlign;
 }
 
-// Workspace of the plain form: 42 binary64 arrays. Precision form: 28 binary32 face arrays, 3
+// Workspace of the plain form: 42 binary64 arrays and the binary32 entropy of the switch
+// pre-check. Precision form: 28 binary32 face arrays, 3
 // binary32 limiter factors (bound solves in binary64, stored in the flux type), 11 binary32
 // per-cell arrays, 9 binary32 cell copies and the binary64 entropy of the binary64 switches.
 size_t layout_bytes(int precision, int nx, int ny, int g)
@@ -51,7 +52,7 @@ size_t layout_bytes(int precision, int nx, int ny, int g)
     if (precision == WM_PREC_FP32)
         return (size_t)(kArrays + kCellCopies) * array_bytes(nx, ny, g, sizeof(float)) + array_bytes(nx, ny, g) +
                kTailBytes;
-    return (size_t)kArrays * array_bytes(nx, ny, g) + kTailBytes;
+    return (size_t)kArrays * array_bytes(nx, ny, g) + array_bytes(nx, ny, g, sizeof(float)) + kTailBytes;
 }
 
 bool valid_params(const wm_params *p, int nx, int ny, int g)
@@ -264,7 +265,9 @@ int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t
         P.ent = h->arr[33]; P.cx = h->arr[34]; P.cy = h->arr[35];
         P.lu = h->arr[36]; P.lv = h->arr[37]; P.lp = h->arr[38]; P.la = h->arr[39]; P.lc = h->arr[40];
         P.lE = h->arr[41];
-        tail = base + (size_t)kArrays * ab;
+        P.ent64 = h->arr[33];
+        P.ent32 = reinterpret_cast<float *>(base + (size_t)kArrays * ab);
+        tail = base + (size_t)kArrays * ab + array_bytes(nx, ny, g, sizeof(float));
     } else {
         size_t ab4 = array_bytes(nx, ny, g, sizeof(float));
         char *cur = base;
@@ -298,6 +301,7 @@ int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t
         P.lu = h->arr32[36]; P.lv = h->arr32[37]; P.lp = h->arr32[38]; P.la = h->arr32[39];
         P.lc = h->arr32[40]; P.lE = h->arr32[41];
         P.ent64 = ent64;
+        P.ent32 = P.ent;
         Cells32 &C = h->cells32;
         C.ar1 = copies[0]; C.ar2 = copies[1]; C.ru = copies[2]; C.rv = copies[3];
         C.p = copies[4]; C.al = copies[5]; C.u = copies[6]; C.v = copies[7]; C.E = copies[8];
@@ -379,11 +383,11 @@ int wm_compute_fluxes(wm_handle *h, const wm_fields *q, void *stream)
     Fields F = to_fields(q);
     cudaStream_t s = as_stream(stream);
     if (h->fp32) {
-        launch_prep32(h->g, h->e, F, h->prep32, h->cells32, h->P.variant, h->sw64, s);
+        launch_prep32(h->g, h->e, F, h->prep32, h->cells32, h->P.variant, h->sw64, s, h->prechecks);
         launch_faces32(h->g, h->e, h->P.variant, h->P.recon, h->cells32, h->prep32, h->fh32, h->gh32,
                        h->fl32, h->gl32, true, false, s);
     } else {
-        launch_prep(h->g, h->e, F, h->prep, h->P.variant, s);
+        launch_prep(h->g, h->e, F, h->prep, h->P.variant, s, h->prechecks);
         launch_faces(h->g, h->e, h->P.variant, h->P.recon, F, h->prep, h->fh, h->gh, h->fl, h->gl,
                      true, false, s);
     }
@@ -397,11 +401,11 @@ int wm_compute_low_fluxes(wm_handle *h, const wm_fields *q, void *stream)
     Fields F = to_fields(q);
     cudaStream_t s = as_stream(stream);
     if (h->fp32) {
-        launch_prep32(h->g, h->e, F, h->prep32, h->cells32, h->P.variant, h->sw64, s);
+        launch_prep32(h->g, h->e, F, h->prep32, h->cells32, h->P.variant, h->sw64, s, h->prechecks);
         launch_faces32(h->g, h->e, h->P.variant, h->P.recon, h->cells32, h->prep32, h->fh32, h->gh32,
                        h->fl32, h->gl32, false, true, s);
     } else {
-        launch_prep(h->g, h->e, F, h->prep, h->P.variant, s);
+        launch_prep(h->g, h->e, F, h->prep, h->P.variant, s, h->prechecks);
         launch_faces(h->g, h->e, h->P.variant, h->P.recon, F, h->prep, h->fh, h->gh, h->fl, h->gl,
                      false, true, s);
     }
@@ -503,9 +507,9 @@ static int run_stage(wm_handle *h, const Fields &F, const Fields &O, double dt, 
     {
         ProfScope ps(h, WM_PROF_PREP, 2, s);
         if (h->fp32)
-            launch_prep32(h->g, h->e, F, h->prep32, h->cells32, h->P.variant, h->sw64, s);
+            launch_prep32(h->g, h->e, F, h->prep32, h->cells32, h->P.variant, h->sw64, s, h->prechecks);
         else
-            launch_prep(h->g, h->e, F, h->prep, h->P.variant, s);
+            launch_prep(h->g, h->e, F, h->prep, h->P.variant, s, h->prechecks);
     }
     {
         ProfScope ps(h, WM_PROF_FACES, 2, s);
@@ -808,6 +812,31 @@ int wm_verify_limiter_precheck(wm_handle *h, const wm_fields *q, double dt, long
     }
     *decided = (long long)host[0];
     *disagreed = (long long)host[1];
+    return WM_OK;
+}
+
+int wm_verify_switch_precheck(wm_handle *h, const wm_fields *q, long long *checked, long long *decided,
+                              long long *disagreed, void *stream)
+{
+    if (!h || !fields_ok(h, q) || !checked || !decided || !disagreed) return WM_ERR_INVALID;
+    unsigned long long *ctr = nullptr, host[3] = {0, 0, 0};
+    cudaStream_t s = as_stream(stream);
+    cudaError_t err = cudaMalloc(&ctr, sizeof host);
+    if (err == cudaSuccess) err = cudaMemsetAsync(ctr, 0, sizeof host, s);
+    if (err == cudaSuccess) {
+        launch_verify_switch(h->g, h->e, to_fields(q), ctr, s);
+        err = cudaGetLastError();
+    }
+    if (err == cudaSuccess) err = cudaMemcpyAsync(host, ctr, sizeof host, cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    cudaFree(ctr);
+    if (err != cudaSuccess) {
+        set_error("wm_verify_switch_precheck", err);
+        return WM_ERR_CUDA;
+    }
+    *checked = (long long)host[0];
+    *decided = (long long)host[1];
+    *disagreed = (long long)host[2];
     return WM_OK;
 }
 

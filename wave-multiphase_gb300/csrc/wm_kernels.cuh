@@ -24,7 +24,10 @@ using Face7 = Face<double>;
 // Per-cell data computed once per stage and shared by the faces that use it.
 template <typename PT> struct PrepT {
     PT *ent;                          // cell entropy p / rho^gamma
-    double *ent64;                    // precision form with binary64 switches: the entropy in binary64
+    double *ent64;                    // the entropy in binary64 (plain form; precision form with
+                                      // binary64 switches), kept where the switch pre-check needs it
+    float *ent32;                     // the binary32 entropy of that pre-check (the precision
+                                      // form's ent array, which its binary64 switches leave free)
     PT *cx, *cy;                      // smoothness indicator along x and y
     PT *sx, *sy;                      // Ducros x pressure sensor (SC only)
     PT *lu, *lv, *lp, *la, *lc, *lE;  // first-order HLLC cell state: velocity, floored
@@ -61,7 +64,7 @@ enum : unsigned {
 void launch_bc(const Grid &g, const int bc[4], const Fields &q, const Fields *save_old,
                cudaStream_t s);
 void launch_prep(const Grid &g, const Eos &e, const Fields &q, const Prep &p, int variant,
-                 cudaStream_t s);
+                 cudaStream_t s, bool prechecks = true);
 void launch_faces(const Grid &g, const Eos &e, int variant, int recon, const Fields &q,
                   const Prep &p, const Face7 &fh, const Face7 &gh, const Face7 &fl, const Face7 &gl,
                   bool high, bool low, cudaStream_t s);
@@ -86,10 +89,14 @@ void launch_dt_cell(const Grid &g, const Eos &e, const Fields &q, const Counters
                     cudaStream_t s);
 void launch_dt_finalize(const Grid &g, const Counters &cnt, double *dt_out, cudaStream_t s);
 void launch_fp64_probe(double *out, int iters, cudaStream_t s, int blocks, int threads);
+// The THINC switch pre-check against the binary64 decision on every full stencil of q;
+// verify[0..2]: stencils, decided by the pre-check, decided differently.
+void launch_verify_switch(const Grid &g, const Eos &e, const Fields &q, unsigned long long *verify,
+                          cudaStream_t s);
 
 // Precision form (binary32 face sweep).
 void launch_prep32(const Grid &g, const Eos &e, const Fields &q, const PrepT<float> &p,
-                   const Cells32 &c, int variant, bool sw64, cudaStream_t s);
+                   const Cells32 &c, int variant, bool sw64, cudaStream_t s, bool prechecks = true);
 void launch_faces32(const Grid &g, const Eos &e, int variant, int recon, const Cells32 &c,
                     const PrepT<float> &p, const Face<float> &fh, const Face<float> &gh,
                     const Face<float> &fl, const Face<float> &gl, bool high, bool low,

@@ -67,20 +67,20 @@ __global__ void bc_y_kernel(Grid g, int bb, int bt, Fields q, Fields old, int sa
 
 // ------------------------------------------------------------------------- stage kernels ----
 // Thin launch wrappers over the bodies of wm_bodies.cuh.
-__global__ void __launch_bounds__(BX *BY) prep_kernel(Grid g, Eos e, Fields q, Prep p)
+__global__ void __launch_bounds__(BX *BY) prep_kernel(Grid g, Eos e, Fields q, Prep p, int prechecks)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.nxg || j >= g.nyg) return;
-    prep_body(g, e, q, p, i, j);
+    prep_body(g, e, q, p, prechecks != 0, i, j);
 }
 
-__global__ void __launch_bounds__(BX *BY) sensor_kernel(Grid g, Fields q, Prep p, int sc)
+__global__ void __launch_bounds__(BX *BY) sensor_kernel(Grid g, Eos e, Fields q, Prep p, int sc, int prechecks)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.nxg || j >= g.nyg) return;
-    sensor_body(g, q, p, sc, i, j);
+    sensor_body(g, e, q, p, sc, prechecks != 0, i, j);
 }
 
 // Pass STAGE of the limiter; NP = STAGE rebuilds the blends of the earlier passes in registers
@@ -129,20 +129,55 @@ final_kernel(Grid g, Eos e, unsigned flags, Fields q, Fields old, Face<FT> fh, F
     }
 }
 
-__global__ void __launch_bounds__(BX *BY) prep32_kernel(Grid g, Eos e, Fields q, PrepT<float> p, Cells32 c, int sw64)
+// SW64: binary64 switches (a compile-time choice, so the binary32 sensor keeps its registers)
+template <int SW64>
+__global__ void __launch_bounds__(BX *BY) prep32_kernel(Grid g, Eos e, Fields q, PrepT<float> p, Cells32 c,
+                                                        int prechecks)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.nxg || j >= g.nyg) return;
-    prep32_body(g, e, q, p, c, sw64 != 0, i, j);
+    prep32_body(g, e, q, p, c, SW64 != 0, prechecks != 0, i, j);
 }
 
-__global__ void __launch_bounds__(BX *BY) sensor32_kernel(Grid g, Fields q, PrepT<float> p, Cells32 c, int sc, int sw64)
+template <int SW64>
+__global__ void __launch_bounds__(BX *BY) sensor32_kernel(Grid g, Eos e, Fields q, PrepT<float> p, Cells32 c, int sc,
+                                                          int prechecks)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.nxg || j >= g.nyg) return;
-    sensor32_body(g, q, p, c, sc, sw64 != 0, i, j);
+    sensor32_body(g, e, q, p, c, sc, SW64 != 0, prechecks != 0, i, j);
+}
+
+// The THINC switch pre-check (thinc_side_pre on entropy32) and the binary64 decision (cator2_val of
+// the binary64 entropies), both from the state, for the cell's x and y stencils.
+__global__ void __launch_bounds__(BX *BY) switch_verify_kernel(Grid g, Eos e, Fields q, unsigned long long *verify)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.nxg || j >= g.nyg) return;
+    const long long kf = kf_of(q, i, j);
+    for (int dir = 0; dir < 2; ++dir) {
+        if (dir == 0 ? (i < 2 || i >= g.nxg - 2) : (j < 2 || j >= g.nyg - 2)) continue;
+        const long long sq = dir == 0 ? q.pitch : 1;
+        float s[5];
+        double v[5];
+        for (int k = 0; k < 5; ++k) {
+            const long long c = kf + (k - 2) * sq;
+            double ge, pie;
+            mix_gamma_pinf(e, q.f[F_AL][c], ge, pie);
+            double rho_e = q.f[F_AR1][c] + q.f[F_AR2][c];
+            if (rho_e < kTiny) rho_e = kTiny;
+            s[k] = entropy32(ge, rho_e, q.f[F_P][c]);
+            v[k] = entropy64_r(ge, rho_e, q.f[F_P][c]);
+        }
+        const int d = thinc_side_pre(s[0], s[1], s[2], s[3], s[4]);
+        const float exact = side_of(cator2_val(v[0], v[1], v[2], v[3], v[4]), kThincThresh);
+        count_if(&verify[0], true);
+        count_if(&verify[1], d >= 0);
+        count_if(&verify[2], d >= 0 && !(float(d) == exact));
+    }
 }
 
 __global__ void widen_kernel(const float *src, double *dst, long long n)
@@ -218,10 +253,11 @@ void launch_bc(const Grid &g, const int bc[4], const Fields &q, const Fields *sa
 }
 
 void launch_prep(const Grid &g, const Eos &e, const Fields &q, const Prep &p, int variant,
-                 cudaStream_t s)
+                 cudaStream_t s, bool prechecks)
 {
-    prep_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, e, q, p);
-    sensor_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, q, p, variant == kSC);
+    const int pc = prechecks ? 1 : 0;
+    prep_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, e, q, p, pc);
+    sensor_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, e, q, p, variant == kSC, pc);
 }
 
 template <typename FT>
@@ -289,10 +325,23 @@ template void launch_final<float>(const Grid &, const Eos &, unsigned, const Fie
                                   double, double, const Counters &, cudaStream_t);
 
 void launch_prep32(const Grid &g, const Eos &e, const Fields &q, const PrepT<float> &p,
-                   const Cells32 &c, int variant, bool sw64, cudaStream_t s)
+                   const Cells32 &c, int variant, bool sw64, cudaStream_t s, bool prechecks)
 {
-    prep32_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, e, q, p, c, sw64 ? 1 : 0);
-    sensor32_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, q, p, c, variant == kSC, sw64 ? 1 : 0);
+    const int pc = prechecks ? 1 : 0;
+    const dim3 grid = grid2(g.nyg, g.nxg), block(BX, BY);
+    if (sw64) {
+        prep32_kernel<1><<<grid, block, 0, s>>>(g, e, q, p, c, pc);
+        sensor32_kernel<1><<<grid, block, 0, s>>>(g, e, q, p, c, variant == kSC, pc);
+    } else {
+        prep32_kernel<0><<<grid, block, 0, s>>>(g, e, q, p, c, pc);
+        sensor32_kernel<0><<<grid, block, 0, s>>>(g, e, q, p, c, variant == kSC, pc);
+    }
+}
+
+void launch_verify_switch(const Grid &g, const Eos &e, const Fields &q, unsigned long long *verify,
+                          cudaStream_t s)
+{
+    switch_verify_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, e, q, verify);
 }
 
 void launch_widen(const float *src, double *dst, long long n, cudaStream_t s)

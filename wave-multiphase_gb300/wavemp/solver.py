@@ -216,9 +216,20 @@ class Solver:
                    "verify_limiter_precheck")
         return a.value, b.value
 
+    def verify_switch_precheck(self, q) -> tuple[int, int, int]:
+        """Diagnostic of the THINC switch pre-check on state q: (stencils checked, settled by the
+        binary32 pre-check, settled differently from the binary64 decision -- 0 when its error
+        bound holds)."""
+        a, b, c = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        _lib.check(self.L.wm_verify_switch_precheck(self._h, ctypes.byref(self._fields(q, need_prims=True)),
+                                                    ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                                    _stream()), "verify_switch_precheck")
+        return a.value, b.value, c.value
+
     def set_prechecks(self, on: bool):
-        """Precision form: binary32 pre-checks that skip binary64 tests they decide (default on;
-        the results are the same bits either way)."""
+        """Binary32 pre-checks that skip binary64 tests they decide -- the limiter's bound solves,
+        the combine's admissibility tests, the THINC switch of binary64 sensors (default on; the
+        results are the same bits either way)."""
         _lib.check(self.L.wm_set_prechecks(self._h, int(bool(on))), "set_prechecks")
 
     def set_limiter_sweeps(self, in_place: bool):
