@@ -106,13 +106,14 @@ __device__ __forceinline__ int thinc_side_pre(float em2, float em1, float e0, fl
 }
 
 // The THINC switch of the cell at kw (its state at kf) along one direction -- workspace stride sw,
-// state stride sq -- as side_of's code. With the pre-checks: the binary32 decision where it is
+// state stride sq. With the pre-checks, as side_of's code: the binary32 decision where it is
 // settled, else cator2_val of the binary64 entropies, those prep kept (binary32 entropy NaN or
 // above kEnt64Scale in magnitude) read back, the others evaluated here from the cell state exactly
-// as prep evaluates them. Without: the binary64 entropies prep kept for every cell.
+// as prep evaluates them. Without: cator2_val of the binary64 entropies prep kept for every cell --
+// the value itself in binary64 arrays (the reference's array), its code in binary32 ones.
 template <typename PT>
-__device__ __forceinline__ float thinc_side(const Eos &e, const Fields &q, const PrepT<PT> &p, long long kw,
-                                            long long kf, long long sw, long long sq, bool prechecks)
+__device__ __forceinline__ double thinc_side(const Eos &e, const Fields &q, const PrepT<PT> &p, long long kw,
+                                             long long kf, long long sw, long long sq, bool prechecks)
 {
     double v[5];
     if (prechecks) {
@@ -135,6 +136,7 @@ __device__ __forceinline__ float thinc_side(const Eos &e, const Fields &q, const
     } else {
 #pragma unroll
         for (int k = 0; k < 5; ++k) v[k] = p.ent64[kw + (k - 2) * sw];
+        if constexpr (sizeof(PT) == 8) return cator2_val(v[0], v[1], v[2], v[3], v[4]);
     }
     return side_of(cator2_val(v[0], v[1], v[2], v[3], v[4]), kThincThresh);
 }
@@ -156,6 +158,26 @@ __device__ __forceinline__ void store_entropy(const PrepT<PT> &p, long long kw, 
     }
 }
 
+// (x / d < c) as the reference evaluates it, x / d rounded, for d > 0 and c > 0: settled from the
+// product c d when x is more than 2^-50 of it away (the quotient's and the product's roundings are
+// 2^-53 each), else by the division itself. NaN x takes the division (false).
+__device__ __forceinline__ bool floor_quotient_below(double x, double d, double c)
+{
+    const double cd = c * d;
+    if (x < cd * (1.0 - 8.8817841970012523e-16)) return true;
+    if (x > cd * (1.0 + 8.8817841970012523e-16)) return false;
+    return x / d < c;
+}
+
+// sound_speed_r's value for the mixture (g, pi) the caller already holds: sqrt(max(g (p + pi) / rho,
+// 1e-20)) with 1/rho supplied, the same operations in the same order.
+__device__ __forceinline__ double sound_speed_gp(double g, double pi, double inv_rho, double p)
+{
+    double val = g * (p + pi) * inv_rho;
+    if (flt(val, kTiny)) val = kTiny;
+    return wsqrt(val);
+}
+
 // Entropy (SC:308-314) and the first-order HLLC cell state of fx_low_kernel (SC:1309-1327), both
 // pure functions of one cell, computed once per cell instead of once per face that reads them.
 __device__ __forceinline__ void prep_body(const Grid &g, const Eos &e, const Fields &q, const Prep &p, bool prechecks,
@@ -175,18 +197,22 @@ __device__ __forceinline__ void prep_body(const Grid &g, const Eos &e, const Fie
     double gg = ge, pi = pie;
     if (!(a == al)) mix_gamma_pinf(e, a, gg, pi);
     double pl = pp;
-    if (isnan(pl) || (pl + pi) / (gg - 1.0) < kPpCtilde) pl = kPpCtilde * (gg - 1.0) - pi;
+    if (isnan(pl) || floor_quotient_below(pl + pi, gg - 1.0, kPpCtilde)) pl = kPpCtilde * (gg - 1.0) - pi;
     double u = ru * ir, v = rv * ir;
     p.lu[kw] = u;
     p.lv[kw] = v;
     p.lp[kw] = pl;
     p.la[kw] = a;
-    p.lc[kw] = sound_speed_r(e, ir, pl, a);
+    p.lc[kw] = sound_speed_gp(gg, pi, ir, pl);  // = sound_speed_r(e, ir, pl, a): (gg, pi) is its mixture
     p.lE[kw] = prim_to_energy(e, rho, u, v, pl, a);
 }
 
-// Ducros x pressure sensor of an interior cell (ducros_kernel, SC:875-916), binary64.
-__device__ __forceinline__ void ducros_xy(const Fields &q, int i, int j, double &sx, double &sy)
+// The terms of the Ducros sensor of an interior cell (ducros_kernel, SC:875-916), binary64:
+// sigma_x = (ax / (bx + 1e-30)) * (d2 / den), sigma_y likewise, d2 = div^2, den = d2 + curl^2 + 1e-30.
+struct DucrosTerms {
+    double ax, bx, ay, by, d2, den;
+};
+__device__ __forceinline__ DucrosTerms ducros_terms(const Fields &q, int i, int j)
 {
     const double *U = q.f[F_U], *V = q.f[F_V], *P = q.f[F_P];
     long long kf = kf_of(q, i, j), Q = q.pitch;
@@ -196,23 +222,57 @@ __device__ __forceinline__ void ducros_xy(const Fields &q, int i, int j, double 
     double der_vy = 0.5 * (-V[kf - 1] + V[kf + 1]);
     double div_u = der_ux + der_vy;
     double curl_u = der_vx - der_uy;
-    double ducros = div_u * div_u / (div_u * div_u + curl_u * curl_u + 1.0e-30);
+    DucrosTerms t;
+    t.d2 = div_u * div_u;
+    t.den = t.d2 + curl_u * curl_u + 1.0e-30;
     double p0 = P[kf];
     double pm2 = P[kf - 2 * Q], pm1 = P[kf - Q], pp1 = P[kf + Q], pp2 = P[kf + 2 * Q];
-    double aa = fabs(-pm2 + 16.0 * pm1 - 30.0 * p0 + 16.0 * pp1 - pp2);
-    double bb = fabs(pm2 + 16.0 * pm1 + 30.0 * p0 + 16.0 * pp1 + pp2);
-    sx = (aa / (bb + 1.0e-30)) * ducros;
+    t.ax = fabs(-pm2 + 16.0 * pm1 - 30.0 * p0 + 16.0 * pp1 - pp2);
+    t.bx = fabs(pm2 + 16.0 * pm1 + 30.0 * p0 + 16.0 * pp1 + pp2);
     pm2 = P[kf - 2];
     pm1 = P[kf - 1];
     pp1 = P[kf + 1];
     pp2 = P[kf + 2];
-    aa = fabs(-pm2 + 16.0 * pm1 - 30.0 * p0 + 16.0 * pp1 - pp2);
-    bb = fabs(pm2 + 16.0 * pm1 + 30.0 * p0 + 16.0 * pp1 + pp2);
-    sy = (aa / (bb + 1.0e-30)) * ducros;
+    t.ay = fabs(-pm2 + 16.0 * pm1 - 30.0 * p0 + 16.0 * pp1 - pp2);
+    t.by = fabs(pm2 + 16.0 * pm1 + 30.0 * p0 + 16.0 * pp1 + pp2);
+    return t;
 }
 
-// The THINC switch per cell and direction (cator2_val < 0.35, SC:318-325, 1028-1032) as side_of's
-// code, and the Ducros x pressure sensor (ducros_kernel, SC:875-916).
+// The two Ducros sensors as the reference evaluates them.
+__device__ __forceinline__ void ducros_xy(const Fields &q, int i, int j, double &sx, double &sy)
+{
+    const DucrosTerms t = ducros_terms(q, i, j);
+    const double ducros = t.d2 / t.den;
+    sx = (t.ax / (t.bx + 1.0e-30)) * ducros;
+    sy = (t.ay / (t.by + 1.0e-30)) * ducros;
+}
+
+// The Ducros sensor's side of kSigmaSmooth, the only use the face sweep makes of it (the maximum
+// over a face's four cells against 0.01). sigma = (a / (b + 1e-30)) (d2 / den) with every term
+// non-negative, so sigma < 0.01 <=> a d2 < 0.01 (b + 1e-30) den up to the roundings of the two
+// evaluations (three each from the shared b + 1e-30 and den on, 2^-53 apiece, no cancellation):
+// where the products differ by more than 2^-45 the code is settled without the three divisions,
+// elsewhere (and for NaN or overflow) sigma is evaluated as ducros_xy evaluates it.
+__device__ __forceinline__ float sigma_side(double a, double b, double d2, double den)
+{
+    const double den_b = b + 1.0e-30;
+    const double num = a * d2, thr = 0.01 * (den_b * den);
+    if (num < thr * (1.0 - 2.8421709430404007e-14)) return 0.0f;
+    if (num > thr * (1.0 + 2.8421709430404007e-14)) return 1.0f;
+    return side_of((a / den_b) * (d2 / den), kSigmaSmooth);
+}
+
+// Both Ducros sensors of an interior cell as sigma_side codes.
+__device__ __forceinline__ void ducros_sides(const Fields &q, int i, int j, float &cx, float &cy)
+{
+    const DucrosTerms t = ducros_terms(q, i, j);
+    cx = sigma_side(t.ax, t.bx, t.d2, t.den);
+    cy = sigma_side(t.ay, t.by, t.d2, t.den);
+}
+
+// The THINC switch per cell and direction (cator2_val < 0.35, SC:318-325, 1028-1032) and the
+// Ducros x pressure sensor (ducros_kernel, SC:875-916): as side_of's codes with the pre-checks,
+// the reference's values without.
 __device__ __forceinline__ void sensor_body(const Grid &g, const Eos &e, const Fields &q, const Prep &p, int sc,
                                             bool prechecks, int i, int j)
 {
@@ -226,7 +286,14 @@ __device__ __forceinline__ void sensor_body(const Grid &g, const Eos &e, const F
         p.sy[kw] = 1.0;
         return;
     }
-    ducros_xy(q, i, j, p.sx[kw], p.sy[kw]);
+    if (prechecks) {
+        float cx, cy;
+        ducros_sides(q, i, j, cx, cy);
+        p.sx[kw] = cx;
+        p.sy[kw] = cy;
+    } else {
+        ducros_xy(q, i, j, p.sx[kw], p.sy[kw]);
+    }
 }
 
 // Face limiter factors of pass p (pp_blend_x/y_flux_kernel, SC:1479-1548): the x face between
@@ -764,10 +831,14 @@ __device__ __forceinline__ void sensor32_body(const Grid &g, const Eos &e, const
             p.sy[kw] = side_of(1.0, kSigmaSmooth);
             return;
         }
-        double sx, sy;
-        ducros_xy(q, i, j, sx, sy);
-        p.sx[kw] = side_of(sx, kSigmaSmooth);
-        p.sy[kw] = side_of(sy, kSigmaSmooth);
+        if (prechecks) {
+            ducros_sides(q, i, j, p.sx[kw], p.sy[kw]);
+        } else {
+            double sx, sy;
+            ducros_xy(q, i, j, sx, sy);
+            p.sx[kw] = side_of(sx, kSigmaSmooth);
+            p.sy[kw] = side_of(sy, kSigmaSmooth);
+        }
         return;
     }
     const float *en = p.ent;
