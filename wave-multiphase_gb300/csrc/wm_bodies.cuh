@@ -595,6 +595,29 @@ __device__ __forceinline__ bool cell_surely_admissible(const Eos &e, const doubl
     return v > 4.0e-6f * mag;
 }
 
+// 1 / (rho Gamma) of the primitive recovery. Plain form: the binary64 quotient. Precision form: the
+// Newton-Raphson reciprocal iteration y <- y + y (1 - x y) in binary64 (residual and update each
+// one fused multiply-add; e.g. Muller et al., Handbook of Floating-Point Arithmetic, ch. 5), seeded
+// with the binary32 reciprocal of x rounded to binary32 (relative error below 2^-23). Two steps
+// square that to below 2^-92 before their own roundings, so the result is within about one unit in
+// the last place of the quotient -- binary64 accuracy for the accumulation, without the division's
+// longer binary64 sequence. Outside binary32's normal range it divides.
+template <typename FT>
+__device__ __forceinline__ double recovery_recip(double x)
+{
+    if constexpr (sizeof(FT) == 8) {
+        return 1.0 / x;
+    } else {
+        const float xf = to_f32(x), af = fabsf(xf);
+        if (!(af >= 1.0e-37f && af <= 1.0e37f)) return 1.0 / x;
+        double y = to_f64(__frcp_rn(xf));
+        double r = __fma_rn(-x, y, 1.0);
+        y = __fma_rn(y, r, y);
+        r = __fma_rn(-x, y, 1.0);
+        return __fma_rn(y, r, y);
+    }
+}
+
 // NP: limiter passes whose blends are deferred (3 in the fused stage: the limited fluxes are rebuilt
 // from fh/gh, fl/gl and the three theta arrays; 0 when fh/gh already hold them).
 template <typename FT, int NP = 0>
@@ -660,7 +683,7 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
             const double a1 = Q[F_AL], rho = Q[0] + Q[1];
             double gb, pb;
             mix_gamma_pibig(e, a1, gb, pb);
-            rg_a1 = a1; rg_rho = rho; rg_inv = 1.0 / (rho * gb); rg_gb = gb; rg_pb = pb;
+            rg_a1 = a1; rg_rho = rho; rg_inv = recovery_recip<FT>(rho * gb); rg_gb = gb; rg_pb = pb;
             wrote_q = true;
         } else if (flags & FIN_ADMISSIBLE) {
             double a1 = clamp01_pp(Q[F_AL]);
@@ -673,7 +696,7 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
             double rho = m1 + m2;
             double gb, pb;
             mix_gamma_pibig(e, a1, gb, pb);
-            const double inv = 1.0 / (rho * gb);
+            const double inv = recovery_recip<FT>(rho * gb);
             const double ir = gb * inv;
             double uu = mx * ir, vv = my * ir;
             double kin = 0.5 * rho * (uu * uu + vv * vv);
@@ -713,7 +736,7 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
                 gb = rg_gb; pb = rg_pb; inv = rg_inv;
             } else {
                 mix_gamma_pibig(e, a1, gb, pb);
-                inv = 1.0 / (rho * gb);
+                inv = recovery_recip<FT>(rho * gb);
             }
             double ir = gb * inv;
             double uu = Q[2] * ir, vv = Q[3] * ir;
