@@ -484,20 +484,17 @@ __device__ __forceinline__ bool theta_one_f64in(const Grid &g, const Eos &e, con
 // theta_one_f32; plain form with blends in place: theta_one_f64in); VERIFY runs the binary64 solve
 // as well and counts (verify[0]) cells the pre-check decided and (verify[1]) cells where the solve
 // disagreed with it -- a diagnostic of the pre-check's margins.
-template <int STAGE, typename FT, int NP = 0, int VERIFY = 0>
-__device__ __forceinline__ double theta_body(const Grid &g, const Eos &e, const Fields &q, const Cells32 &c32,
-                                             const Face<FT> &fh, const Face<FT> &gh,
-                                             const Face<FT> &fl, const Face<FT> &gl, double dt,
-                                             FT *const theta[3], int i, int j,
-                                             unsigned long long *verify = nullptr, bool prechecks = true)
+// The binary64 bound solve of one cell (after any binary32 pre-check), binary32 pre-check of the
+// precision form included.
+template <int STAGE, typename FT, int NP, int VERIFY>
+__device__ __forceinline__ double theta_solve_inline(const Grid &g, const Eos &e, const Fields &q, const Cells32 &c32,
+                                                     const Face<FT> &fh, const Face<FT> &gh,
+                                                     const Face<FT> &fl, const Face<FT> &gl, double dt,
+                                                     FT *const theta[3], int i, int j,
+                                                     unsigned long long *verify, bool prechecks, bool one = false)
 {
     const CellFaces<FT, NP> cf(g, theta, i, j);
     const long long kf = kf_of(q, i, j), kw = cf.kw, kx = cf.kx, ky = cf.ky;
-    bool one = false;
-    if constexpr (sizeof(FT) == 8 && NP == 0) {  // plain form, blends in place
-        one = theta_one_f64in<STAGE>(g, e, q, kf, kw, fh, gh, fl, gl, dt);
-        if (!VERIFY && one && prechecks) return 1.0;
-    }
     const FT idx = cst<FT>(g.inv_dx, g.inv_dxf), idy = cst<FT>(g.inv_dy, g.inv_dyf);
     constexpr int C0 = STAGE == 1 ? 5 : 0, C1 = STAGE == 0 ? 2 : 6;
     FT rh[6], rl[6];
@@ -544,6 +541,37 @@ __device__ __forceinline__ double theta_body(const Grid &g, const Eos &e, const 
         count_if(&verify[1], one && th != 1.0);
     }
     return th;
+}
+
+template <int STAGE, int VERIFY>
+__device__ __noinline__ double theta_solve(const Grid &g, const Eos &e, const Fields &q, const Face<double> fh,
+                                           const Face<double> gh, const Face<double> fl, const Face<double> gl,
+                                           double dt, int i, int j, unsigned long long *verify, bool one)
+{
+    double *const none[3] = {nullptr, nullptr, nullptr};
+    return theta_solve_inline<STAGE, double, 0, VERIFY>(g, e, q, Cells32{}, fh, gh, fl, gl, dt, none, i, j, verify,
+                                                         false, one);
+}
+
+template <int STAGE, typename FT, int NP = 0, int VERIFY = 0>
+__device__ __forceinline__ double theta_body(const Grid &g, const Eos &e, const Fields &q, const Cells32 &c32,
+                                             const Face<FT> &fh, const Face<FT> &gh,
+                                             const Face<FT> &fl, const Face<FT> &gl, double dt,
+                                             FT *const theta[3], int i, int j,
+                                             unsigned long long *verify = nullptr, bool prechecks = true)
+{
+    bool one = false;
+    if constexpr (sizeof(FT) == 8 && NP == 0) {  // plain form, blends in place
+        const long long kf = kf_of(q, i, j), kw = kw_of(g, i, j);
+        one = theta_one_f64in<STAGE>(g, e, q, kf, kw, fh, gh, fl, gl, dt);
+        if (!VERIFY && one && prechecks) return 1.0;
+        // the rare cells the pre-check leaves: out of line, so its registers do not hold down the
+        // occupancy of the pass
+        return theta_solve<STAGE, VERIFY>(g, e, q, fh, gh, fl, gl, dt, i, j, verify, one);
+    } else {
+        return theta_solve_inline<STAGE, FT, NP, VERIFY>(g, e, q, c32, fh, gh, fl, gl, dt, theta, i, j, verify,
+                                                         prechecks);
+    }
 }
 
 // pp_blend_x_flux_kernel + pp_blend_y_flux_kernel (SC:1479-1548) in one launch: the thread at
