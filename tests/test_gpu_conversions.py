@@ -64,3 +64,51 @@ def test_compares_on_special_pairs():
     sp = np.concatenate([sp, nan_payload])
     pairs = [np.array([a, b]) for a in sp for b in sp]
     assert check(np.concatenate(pairs).view(np.uint64)) == (0, 0, 0)
+
+
+def check_arith(values_u64: np.ndarray):
+    L = _lib.load()
+    t = torch.from_numpy(values_u64.view(np.int64)).cuda()
+    counts = (ctypes.c_longlong * 8)()
+    _lib.check(L.wm_check_sweep_arith(ctypes.c_void_p(t.data_ptr()), t.numel(), counts, _stream()),
+               "wm_check_sweep_arith")
+    return list(counts)
+
+
+def test_sweep_arithmetic_within_one_ulp():
+    """The face sweep's binary64 reciprocal, quotient and square root (binary32 seed refined by fused
+    multiply-adds) are within one unit in the last place of IEEE 1/y, x/y and sqrt(x) on random
+    bit patterns, on values of every magnitude the fast path takes, and at the edges of its operand
+    ranges; special values (zeros, subnormals, infinities, NaN, out-of-range operands) give the
+    IEEE results bit for bit."""
+    rng = np.random.default_rng(2)
+    bits = rng.integers(0, 2**63, size=2_000_000, dtype=np.uint64) * np.uint64(2)
+    bits |= rng.integers(0, 2, size=bits.size, dtype=np.uint64)
+    vals = rng.standard_normal(2_000_000) * 10.0 ** rng.uniform(-40, 40, 2_000_000)
+    edges = []
+    for k in (-126, -125, -124, 124, 125, 126, -897, -896, -895, 896, 897, 898):
+        for m in (1.0, 1.0 - 2.0 ** -53, 1.0 + 2.0 ** -52, 1.5, 1.9999999999999998):
+            edges += [m * 2.0 ** k, -m * 2.0 ** k]
+    special = [0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324, -5e-324, 2.2250738585072014e-308,
+               1.7976931348623157e308, 1.0, -1.0, 3.0, 6e8, 1e-20, 1.0 + 2.0 ** -52]
+    # significands just below and above a binary32 truncation boundary (the seed's 20 fraction bits)
+    base = (rng.standard_normal(200_000).view(np.uint64) & ~np.uint64(0xFFFFFFFF))
+    trunc = np.concatenate([base | np.uint64(0xFFFFFFFF), base, base | np.uint64(1)])
+    allv = np.concatenate([bits, vals.view(np.uint64), np.array(edges + special).view(np.uint64), trunc])
+    c = check_arith(allv)
+    assert c[:3] == [0, 0, 0], c
+    # the refinement is not a different rounding rule: most results are the IEEE ones exactly
+    assert max(c[3:6]) < 0.05 * allv.size, c
+    assert c[6:] == [0, 0], c
+
+
+def test_minmods_equal_the_sign_sum_products():
+    """mm2 / mm4 on the integer pipe equal 0.5 (sign x + sign y) min|.| and
+    0.125 s |(sa + sc)(sa + sd)| min|.| on the hardware operations bit for bit: every sign pattern of
+    zeros of both signs, infinities, NaN and finite values, in all orders."""
+    sp = np.array([0.0, -0.0, 1.0, -1.0, 2.5, -2.5, np.inf, -np.inf, np.nan, 5e-324, -5e-324, 1e300])
+    quads = np.array(np.meshgrid(sp, sp, sp, sp)).reshape(4, -1).T.copy()
+    rng = np.random.default_rng(3)
+    rnd = rng.standard_normal(400_000) * 10.0 ** rng.uniform(-5, 5, 400_000)
+    c = check_arith(np.concatenate([quads.ravel(), rnd]).view(np.uint64))
+    assert c[6:] == [0, 0], c

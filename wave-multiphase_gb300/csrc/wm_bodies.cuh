@@ -1019,13 +1019,13 @@ __device__ __forceinline__ void face_body(const Eos &e, const V &v, const Face<F
     const T a1a = T(0.5) * (U0[5] + U1[5]);
     const T pa = T(0.5) * (U0[4] + U1[4]);
     const T rhoa = ar1a + ar2a;
-    const T irhoa = T(1) / rhoa;
+    const T irhoa = sw_rcp(rhoa);
     FaceBasis<T> b;
     b.u = T(0.5) * (U0[2] + U1[2]) * irhoa;
     b.v = T(0.5) * (U0[3] + U1[3]) * irhoa;
-    const T ca = sound_speed_r(e, irhoa, pa, a1a);
+    const T ca = sound_speed_r<T, true>(e, irhoa, pa, a1a);
     {
-        const T ic = T(1) / ca;
+        const T ic = sw_rcp(ca);
         b.c = ca;
         b.c2 = ca * ca;
         b.inv2c = T(0.5) * ic;
@@ -1081,28 +1081,45 @@ __device__ __forceinline__ void face_body(const Eos &e, const V &v, const Face<F
 
     // --- back-projection and positivity fallback (SC:1095-1115; M10:1000-1025) ----------------
     S6<T> phL = to_phys<DIR>(b, wL), phR = to_phys<DIR>(b, wR);
-    const S6<T> phfL = to_phys<DIR>(b, W[2]), phfR = to_phys<DIR>(b, W[3]);
     if (VAR == kM10) {
+        const S6<T> phfL = to_phys<DIR>(b, W[2]), phfR = to_phys<DIR>(b, W[3]);
         phL = pp_limit_reconstructed_state(e, phL, phfL);
         phR = pp_limit_reconstructed_state(e, phR, phfR);
-    }
 #pragma unroll
-    for (int s = 0; s < 2; ++s) {
-        S6<T> &ph = s == 0 ? phL : phR;
-        const S6<T> &pf = s == 0 ? phfL : phfR;
-        if (!fge(ph.v[0], T(0))) ph.v[0] = pf.v[0];  // x < 0 or NaN
-        if (!fge(ph.v[1], T(0))) ph.v[1] = pf.v[1];
-        if (flt(ph.v[5], T(0)) || fgt(ph.v[5], T(1))) ph.v[5] = pf.v[5];
-        if (VAR == kM10) {
+        for (int s = 0; s < 2; ++s) {
+            S6<T> &ph = s == 0 ? phL : phR;
+            const S6<T> &pf = s == 0 ? phfL : phfR;
+            if (!fge(ph.v[0], T(0))) ph.v[0] = pf.v[0];  // x < 0 or NaN
+            if (!fge(ph.v[1], T(0))) ph.v[1] = pf.v[1];
+            if (flt(ph.v[5], T(0)) || fgt(ph.v[5], T(1))) ph.v[5] = pf.v[5];
             if (flt(rho_ctilde2_sc(e, ph), T(kPpCtilde)) || wisnan(ph.v[4])) ph.v[4] = pf.v[4];
             ph = pp_floor_pressure_state(e, ph);
-        } else if (wisnan(ph.v[4])) {
-            ph.v[4] = pf.v[4];
         }
-    }
-    if (!fge(ca, T(0))) {  // ca < 0 or NaN
-        phL = phfL;
-        phR = phfR;
+        if (!fge(ca, T(0))) {  // ca < 0 or NaN
+            phL = phfL;
+            phR = phfR;
+        }
+    } else {
+        // The same fallbacks; the first-order state (the back-projection of cell 0 or 1) is formed
+        // only for a side that needs one of its components.
+        const bool bad_ca = !fge(ca, T(0));  // ca < 0 or NaN: both sides take it whole
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            S6<T> &ph = s == 0 ? phL : phR;
+            const bool b0 = !fge(ph.v[0], T(0)), b1 = !fge(ph.v[1], T(0));  // x < 0 or NaN
+            const bool b5 = flt(ph.v[5], T(0)) || fgt(ph.v[5], T(1)), b4 = wisnan(ph.v[4]);
+            if (bad_ca || b0 || b1 || b4 || b5) {
+                const S6<T> pf = to_phys<DIR>(b, s == 0 ? W[2] : W[3]);
+                if (bad_ca) {
+                    ph = pf;
+                } else {
+                    if (b0) ph.v[0] = pf.v[0];
+                    if (b1) ph.v[1] = pf.v[1];
+                    if (b5) ph.v[5] = pf.v[5];
+                    if (b4) ph.v[4] = pf.v[4];
+                }
+            }
+        }
     }
 
     // --- HLLC on the reconstructed states (SC:1118-1133) ---------------------------------------
@@ -1114,12 +1131,12 @@ __device__ __forceinline__ void face_body(const Eos &e, const V &v, const Face<F
         d.ar1 = ph.v[0];
         d.ar2 = ph.v[1];
         d.rho = ph.v[0] + ph.v[1];
-        const T ir = T(1) / d.rho;
+        const T ir = sw_rcp(d.rho);
         d.un = ph.v[N] * ir;
         d.ut = ph.v[TG] * ir;
         d.p = ph.v[4];
         d.a = ph.v[5];
-        d.c = sound_speed_r(e, ir, d.p, d.a);
+        d.c = sound_speed_r<T, true>(e, ir, d.p, d.a);
         d.E = prim_to_energy(e, d.rho, d.un, d.ut, d.p, d.a);
     }
     T f[6], us;

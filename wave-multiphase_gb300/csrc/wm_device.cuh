@@ -148,6 +148,83 @@ template <typename T> __device__ __forceinline__ bool fge(T a, T b) { return fle
 template <typename T> __device__ __forceinline__ bool fpos(T x) { return x > T(0); }
 template <> __device__ __forceinline__ bool fpos<double>(double x) { return dpos(x); }
 
+// ------------------------------------------------------------------------------------------------
+// Reciprocal, quotient and square root of the binary64 face sweep. GB300 issues binary64
+// arithmetic on a narrow pipe (about two operations per SM per clock), where an IEEE division or
+// square root is a chain of several dependent operations; the sweep is bound by that pipe. These
+// forms take a binary32 seed from the integer pipe and the multi-function unit and refine it in
+// binary64 with fused multiply-adds (Newton-Raphson and series refinement, and Markstein's
+// residual correction of the quotient; e.g. Muller et al., Handbook of Floating-Point Arithmetic,
+// ch. 5):
+//   seed  s ~ 1/y: y truncated to 20 fraction bits (relative error < 2^-20), rcp.approx.f32
+//         (<= 1 ulp), widened exactly, so e = 1 - y s has |e| < 2^-19.8;
+//   rcp   s (1 + e + e^2) = 1/y (1 - e^3 / (1 - e)): relative error < 2^-59 before its own
+//         roundings -- within one unit in the last place of 1/y (3 operations);
+//   div   q0 = x s1, r = x - y q0 (one rounding), q = q0 + r s1: within about half a unit of x/y
+//         (6 operations);
+//   sqrt  h ~ 1/sqrt(x) from rsqrt.approx.f32 of x truncated (relative error < 2^-20.5),
+//         z = x h, then twice z += (x - z^2) h/2 (the error goes 2^-20.5 -> 2^-40 -> < 2^-59):
+//         within one unit of sqrt(x) (5 operations).
+// Operands where the seed would not be a normal binary32 number or a product could leave the
+// normal range -- zeros, subnormals, infinities, NaN, negative square-root operands, |y| (and the
+// square-root operand) outside [2^-125, 2^125), |x| outside [2^-896, 2^897) -- take the IEEE
+// operation, so special values give exactly what division and sqrt give. Elsewhere the results
+// may differ from the correctly rounded ones by one unit in the last place (wm_check_sweep_arith
+// counts any larger difference on random and boundary operands).
+__device__ __forceinline__ double widen_normal(float f)  // exact, for a normal binary32 f
+{
+    const unsigned b = __float_as_uint(f);
+    const unsigned hi = (b & 0x80000000u) | ((((b >> 23) & 0xffu) + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)(b << 29));
+}
+// y truncated to binary32 from its high word (sign, biased exponent ey in [898, 1147], 20 bits)
+__device__ __forceinline__ float trunc_f32(unsigned hy, unsigned ey)
+{
+    return __uint_as_float((hy & 0x80000000u) | ((ey - 896u) << 23) | ((hy & 0xfffffu) << 3));
+}
+__device__ __forceinline__ unsigned exp_bits(unsigned hi) { return (hi >> 20) & 0x7ffu; }
+__device__ __forceinline__ double rcp_refine(double y, unsigned hy, unsigned ey)
+{
+    float sf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(sf) : "f"(trunc_f32(hy, ey)));
+    const double s = widen_normal(sf);
+    const double e = __fma_rn(-y, s, 1.0);
+    return __fma_rn(s, __fma_rn(e, e, e), s);
+}
+__device__ __forceinline__ double rcp_nr(double y)
+{
+    const unsigned hy = (unsigned)__double2hiint(y), ey = exp_bits(hy);
+    if (ey - 898u > 249u) return 1.0 / y;
+    return rcp_refine(y, hy, ey);
+}
+__device__ __forceinline__ double div_nr(double x, double y)
+{
+    const unsigned hy = (unsigned)__double2hiint(y), ey = exp_bits(hy);
+    const unsigned ex = exp_bits((unsigned)__double2hiint(x));
+    if (ey - 898u > 249u || ex - 127u > 1792u) return x / y;
+    const double s = rcp_refine(y, hy, ey);
+    const double q0 = __dmul_rn(x, s);
+    return __fma_rn(__fma_rn(-y, q0, x), s, q0);
+}
+__device__ __forceinline__ double sqrt_nr(double x)
+{
+    const unsigned hx = (unsigned)__double2hiint(x), ex = exp_bits(hx);
+    if ((hx >> 31) || ex - 898u > 249u) return sqrt(x);
+    float hf;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(hf) : "f"(trunc_f32(hx, ex)));
+    const double hh = widen_normal(0.5f * hf);  // h / 2, halved exactly in binary32
+    double z = __dmul_rn(x, widen_normal(hf));
+    z = __fma_rn(__fma_rn(-z, z, x), hh, z);
+    return __fma_rn(__fma_rn(-z, z, x), hh, z);
+}
+// The face sweep's forms in the arithmetic type T: binary32 keeps the hardware operations.
+template <typename T> __device__ __forceinline__ T sw_rcp(T y) { return T(1) / y; }
+template <typename T> __device__ __forceinline__ T sw_div(T x, T y) { return x / y; }
+template <typename T> __device__ __forceinline__ T sw_sqrt(T x) { return sqrtf(x); }
+template <> __device__ __forceinline__ double sw_rcp(double y) { return rcp_nr(y); }
+template <> __device__ __forceinline__ double sw_div(double x, double y) { return div_nr(x, y); }
+template <> __device__ __forceinline__ double sw_sqrt(double x) { return sqrt_nr(x); }
+
 // The reference's wp.min / wp.max / wp.sign: a < b ? a : b, a > b ? a : b, x < 0 ? -1 : 1
 // (binary64: by the integer compares above, the same results).
 template <typename T> __device__ __forceinline__ T wmin(T a, T b) { return a < b ? a : b; }
@@ -185,27 +262,27 @@ __device__ __forceinline__ void mix_gamma_pibig(const Eos &e, T a1, T &gb, T &pb
 }
 
 // mixture gamma and p_inf: g = 1/Gamma + 1, p_inf = (g-1) Pi / g = Pi / (1 + Gamma), with the two
-// reciprocals taken from one division 1 / (Gamma (1 + Gamma)).
-template <typename T>
+// reciprocals taken from one division 1 / (Gamma (1 + Gamma)). SW: the face sweep's reciprocal.
+template <typename T, bool SW = false>
 __device__ __forceinline__ void mix_gamma_pinf(const Eos &e, T a1, T &g, T &pi)
 {
     T gb, pb;
     mix_gamma_pibig(e, a1, gb, pb);
     const T gp1 = T(1) + gb;
-    const T inv = T(1) / (gb * gp1);
+    const T inv = SW ? sw_rcp(gb * gp1) : T(1) / (gb * gp1);
     g = gp1 * inv + T(1);
     pi = pb * (gb * inv);
 }
 
-// sound_speed(rho, p, a1) with 1/rho supplied
-template <typename T>
+// sound_speed(rho, p, a1) with 1/rho supplied (SW: with the face sweep's reciprocal and root)
+template <typename T, bool SW = false>
 __device__ __forceinline__ T sound_speed_r(const Eos &e, T inv_rho, T p, T a1)
 {
     T g, pi;
-    mix_gamma_pinf(e, a1, g, pi);
+    mix_gamma_pinf<T, SW>(e, a1, g, pi);
     T val = g * (p + pi) * inv_rho;
     if (flt(val, T(kTiny))) val = T(kTiny);
-    return wsqrt(val);
+    return SW ? sw_sqrt(val) : wsqrt(val);
 }
 
 // prim_to_energy (SC:105-110)
@@ -404,6 +481,34 @@ template <typename T> __device__ __forceinline__ T mm4(T a, T b, T c, T d)
            wmin(wmin(wabs(a), wabs(b)), wmin(wabs(c), wabs(d)));
 }
 
+// Binary64 mm2 / mm4 on the integer pipe, the same values as the products above: with the signs
+// of wsign (x < 0 ? -1 : 1) and m the a<b?a:b minimum of the magnitudes, the sign sum and product
+// are +-2 / +-4 when the signs agree (the result is +-m, negated by its sign bit) and 0 otherwise
+// (the result is 0 times m: a zero -- negative for mm4 when a and b are negative, the sign of
+// 0.125 s -- or NaN when m is infinite or NaN).
+__device__ __forceinline__ double with_sign(double m, bool neg)
+{
+    return __longlong_as_double(__double_as_longlong(m) ^ (neg ? (long long)0x8000000000000000ULL : 0LL));
+}
+__device__ __forceinline__ double zero_times(double m, bool neg)
+{
+    const bool finite = (__double_as_longlong(m) & 0x7fffffffffffffffLL) < 0x7ff0000000000000LL;
+    return finite ? with_sign(0.0, neg) : __longlong_as_double(0x7ff8000000000000LL);
+}
+template <> __device__ __forceinline__ double mm2(double x, double y)
+{
+    const double m = wmin(fabs(x), fabs(y));
+    const bool nx = dneg(x);
+    return nx == dneg(y) ? with_sign(m, nx) : zero_times(m, false);
+}
+template <> __device__ __forceinline__ double mm4(double a, double b, double c, double d)
+{
+    const double m = wmin(wmin(fabs(a), fabs(b)), wmin(fabs(c), fabs(d)));
+    const bool na = dneg(a), nb = dneg(b);
+    if (na == nb && na == dneg(c) && na == dneg(d)) return with_sign(m, na);
+    return zero_times(m, na && nb);
+}
+
 // p / rho^gamma(alpha) (SC:308-314)
 template <typename T> __device__ __forceinline__ T cell_entropy(const Eos &e, T ar1, T ar2, T p, T a1)
 {
@@ -431,10 +536,10 @@ template <typename T> __device__ __forceinline__ T thinc_ul(const Eos &e, T vm1,
     if (fpos((v1 - v0) * (v0 - vm1))) {
         T qa = T(0.5) * (v1 + vm1);
         T qd = T(0.5) * (v1 - vm1);
-        T feng = (v0 - qa) / qd;
+        T feng = sw_div(v0 - qa, qd);
         T T1 = cst<T>(e.thinc_t1, e.thinc_t1f);
         T T2 = wtanh(feng * T(1.8) * T(0.5));
-        result = qa + qd * (T1 + T2 * cst<T>(e.thinc_inv_t1, e.thinc_inv_t1f)) / (T(1) + T2);
+        result = qa + sw_div(qd * (T1 + T2 * cst<T>(e.thinc_inv_t1, e.thinc_inv_t1f)), T(1) + T2);
     }
     return result;
 }
@@ -445,10 +550,10 @@ template <typename T> __device__ __forceinline__ T thinc_ur(const Eos &e, T v0, 
     if (fpos((v2 - v1) * (v1 - v0))) {
         T qa = T(0.5) * (v2 + v0);
         T qd = T(0.5) * (v2 - v0);
-        T feng = (v1 - qa) / qd;
+        T feng = sw_div(v1 - qa, qd);
         T T1 = cst<T>(e.thinc_t1, e.thinc_t1f);
         T T2 = wtanh(feng * T(1.8) * T(0.5));
-        result = qa - qd * (T1 - T2 * cst<T>(e.thinc_inv_t1, e.thinc_inv_t1f)) / (T(1) - T2);
+        result = qa - sw_div(qd * (T1 - T2 * cst<T>(e.thinc_inv_t1, e.thinc_inv_t1f)), T(1) - T2);
     }
     return result;
 }
@@ -539,23 +644,43 @@ template <typename T> struct FaceBasis {
 template <int DIR, typename T> __device__ __forceinline__ S6<T> to_char(const FaceBasis<T> &b, const T u[6])
 {
     S6<T> s;
-    if (DIR == 0) {  // to_char_x (SC:480-499)
-        T un = b.u, ut = b.v;
-        s.v[0] = un * b.inv2c * u[0] + un * b.inv2c * u[1] - b.inv2c * u[2] + b.inv2c2 * u[4];
-        s.v[1] = u[0] - b.Y1c2 * u[4];
-        s.v[2] = u[1] - b.Y2c2 * u[4];
-        s.v[3] = -ut * u[0] - ut * u[1] + u[3];
-        s.v[4] = u[5];
-        s.v[5] = -un * b.inv2c * u[0] - un * b.inv2c * u[1] + b.inv2c * u[2] + b.inv2c2 * u[4];
-    } else {  // to_char_y (SC:537-556)
-        T un = b.v, ut_f = -b.u;
-        s.v[0] = un * b.inv2c * u[0] + un * b.inv2c * u[1] - b.inv2c * u[3] + b.inv2c2 * u[4];
-        s.v[1] = u[0] - b.Y1c2 * u[4];
-        s.v[2] = u[1] - b.Y2c2 * u[4];
-        s.v[3] = -ut_f * u[0] - ut_f * u[1] - u[2];
-        s.v[4] = u[5];
-        s.v[5] = -un * b.inv2c * u[0] - un * b.inv2c * u[1] + b.inv2c * u[3] + b.inv2c2 * u[4];
+    if constexpr (sizeof(T) == 4) {  // binary32: the rows as the reference writes them
+        if (DIR == 0) {  // to_char_x (SC:480-499)
+            T un = b.u, ut = b.v;
+            s.v[0] = un * b.inv2c * u[0] + un * b.inv2c * u[1] - b.inv2c * u[2] + b.inv2c2 * u[4];
+            s.v[1] = u[0] - b.Y1c2 * u[4];
+            s.v[2] = u[1] - b.Y2c2 * u[4];
+            s.v[3] = -ut * u[0] - ut * u[1] + u[3];
+            s.v[4] = u[5];
+            s.v[5] = -un * b.inv2c * u[0] - un * b.inv2c * u[1] + b.inv2c * u[2] + b.inv2c2 * u[4];
+        } else {  // to_char_y (SC:537-556)
+            T un = b.v, ut_f = -b.u;
+            s.v[0] = un * b.inv2c * u[0] + un * b.inv2c * u[1] - b.inv2c * u[3] + b.inv2c2 * u[4];
+            s.v[1] = u[0] - b.Y1c2 * u[4];
+            s.v[2] = u[1] - b.Y2c2 * u[4];
+            s.v[3] = -ut_f * u[0] - ut_f * u[1] - u[2];
+            s.v[4] = u[5];
+            s.v[5] = -un * b.inv2c * u[0] - un * b.inv2c * u[1] + b.inv2c * u[3] + b.inv2c2 * u[4];
+        }
+        return s;
     }
+    // Binary64: the same rows with the partial densities' sum and the acoustic rows' common part
+    // formed once: w0 = A + C and w5 = C - A for A = (un (u0 + u1) - m_n) / (2c), C = p / (2c^2),
+    // un the normal velocity, m_n the normal momentum.
+    constexpr int N = DIR == 0 ? 2 : 3;  // normal momentum field
+    const T un = DIR == 0 ? b.u : b.v;
+    const T s01 = u[0] + u[1];
+    const T A = un * b.inv2c * s01 - b.inv2c * u[N];
+    const T C = b.inv2c2 * u[4];
+    s.v[0] = A + C;
+    s.v[1] = u[0] - b.Y1c2 * u[4];
+    s.v[2] = u[1] - b.Y2c2 * u[4];
+    if (DIR == 0)  // to_char_x (SC:480-499): -v (u0 + u1) + u3
+        s.v[3] = u[3] - b.v * s01;
+    else  // to_char_y (SC:537-556): u (u0 + u1) - u2
+        s.v[3] = -(u[2] - b.u * s01);
+    s.v[4] = u[5];
+    s.v[5] = C - A;
     return s;
 }
 
@@ -597,9 +722,9 @@ __device__ __forceinline__ void hllc(const Side<T> &L, const Side<T> &R, T f[6],
     T SR = wmax(R.un + R.c, n_avg + c_avg);
     T denom = L.rho * (SL - L.un) - R.rho * (SR - R.un);
     if (flt(wabs(denom), T(kTiny))) denom = T(kTiny);
-    T SP = (R.p - L.p + L.rho * L.un * (SL - L.un) - R.rho * R.un * (SR - R.un)) / denom;
-    T ratioL = (SL - L.un) / (SL - SP);
-    T ratioR = (SR - R.un) / (SR - SP);
+    T SP = sw_div(R.p - L.p + L.rho * L.un * (SL - L.un) - R.rho * R.un * (SR - R.un), denom);
+    T ratioL = sw_div(SL - L.un, SL - SP);
+    T ratioR = sw_div(SR - R.un, SR - SP);
 
     if (fpos(SL)) {
         f[0] = L.ar1 * L.un;
@@ -610,7 +735,7 @@ __device__ __forceinline__ void hllc(const Side<T> &L, const Side<T> &R, T f[6],
         f[5] = L.a * L.un;
     } else if (fle(SL, T(0)) && fpos(SP)) {
         T ratio = ratioL;
-        T E_star = L.E + (SP - L.un) * (SP * L.rho + L.p / (SL - L.un));
+        T E_star = L.E + (SP - L.un) * (SP * L.rho + sw_div(L.p, SL - L.un));
         f[0] = L.ar1 * L.un + SL * (L.ar1 * ratio - L.ar1);
         f[1] = L.ar2 * L.un + SL * (L.ar2 * ratio - L.ar2);
         f[N] = (L.rho * L.un * L.un + L.p) + SL * (L.rho * SP * ratio - L.rho * L.un);
@@ -619,7 +744,7 @@ __device__ __forceinline__ void hllc(const Side<T> &L, const Side<T> &R, T f[6],
         f[5] = L.a * L.un + SL * (L.a * ratio - L.a);
     } else if (fle(SP, T(0)) && fle(T(0), SR)) {
         T ratio = ratioR;
-        T E_star = R.E + (SP - R.un) * (SP * R.rho + R.p / (SR - R.un));
+        T E_star = R.E + (SP - R.un) * (SP * R.rho + sw_div(R.p, SR - R.un));
         f[0] = R.ar1 * R.un + SR * (R.ar1 * ratio - R.ar1);
         f[1] = R.ar2 * R.un + SR * (R.ar2 * ratio - R.ar2);
         f[N] = (R.rho * R.un * R.un + R.p) + SR * (R.rho * SP * ratio - R.rho * R.un);

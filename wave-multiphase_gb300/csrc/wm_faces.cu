@@ -15,6 +15,8 @@ namespace wm {
 namespace {
 
 constexpr int FBX = 32, FBY = 4;  // faces of a block: FBY rows (x) by FBX columns (y, contiguous)
+// Resident blocks per SM the binary64 sweep is compiled for: 4 fit its registers (128) without spills.
+constexpr int kFace64Blocks = 4;
 
 // A block's tile, staged in shared memory: the six cell fields over the block's faces and the
 // stencil halo along the sweep (cells -2..3 of every face), the six first-order fields (cells 0, 1)
@@ -136,13 +138,13 @@ __device__ __forceinline__ void staged_faces(const Grid &g, const Eos &e, const 
 }
 
 // Binary32 sweeps: registers capped for 8 resident blocks per SM (no spills; 64 registers instead
-// of 89 lift the warp occupancy from 31 % to 50 % of the latency-bound kernel); binary64: 2.
+// of 89 lift the warp occupancy from 31 % to 50 % of the latency-bound kernel); binary64: kFace64Blocks.
 // STAGED: the block's tile is staged in shared memory first (binary64: as fast as direct loads, the
 // sweep being bound by the binary64 pipe); otherwise each face reads its stencil directly, through
 // L1 (binary32: 55 ms against 89 ms staged per 10 steps of the triple point -- the staging's
 // barrier serialises loads and compute within a block, and L1 already serves the reuse).
 template <int DIR, int VAR, int REC, typename T, typename CS, typename FT, bool STAGED>
-__global__ void __launch_bounds__(FBX *FBY, sizeof(T) == 4 ? 8 : 2)
+__global__ void __launch_bounds__(FBX *FBY, sizeof(T) == 4 ? 8 : kFace64Blocks)
 face_kernel(Grid g, Eos e, CS cs, PrepT<T> p, Face<FT> hi, Face<FT> lo, int do_high, int do_low)
 {
     if constexpr (!STAGED) {

@@ -123,7 +123,78 @@ __global__ void conv_check_kernel(const unsigned long long *in, long long n, uns
     }
 }
 
+// One result of the sweep's arithmetic against the IEEE one: 0 same bits, 1 one unit in the last
+// place apart (both finite, normal and of one sign), 2 otherwise (NaN: both NaN counts as same).
+__device__ int ulp_class(double a, double b)
+{
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    if (ia == ib || (a != a && b != b)) return 0;
+    const long long ma = ia & 0x7fffffffffffffffLL, mb = ib & 0x7fffffffffffffffLL;
+    const long long lo = 0x0010000000000000LL, hi = 0x7ff0000000000000LL;  // normal range
+    if ((ia ^ ib) < 0 || ma < lo || mb < lo || ma >= hi || mb >= hi) return 2;
+    return (ma - mb == 1 || mb - ma == 1) ? 1 : 2;
+}
+
+// The reference's minmod products on the hardware binary64 operations (the generic mm2 / mm4).
+__device__ double mm2_hw(double x, double y)
+{
+    const double sx = x < 0.0 ? -1.0 : 1.0, sy = y < 0.0 ? -1.0 : 1.0, ax = fabs(x), ay = fabs(y);
+    return __dmul_rn(__dmul_rn(0.5, __dadd_rn(sx, sy)), ax < ay ? ax : ay);
+}
+__device__ double mm4_hw(double a, double b, double c, double d)
+{
+    const double sa = a < 0.0 ? -1.0 : 1.0, sb = b < 0.0 ? -1.0 : 1.0;
+    const double sc = c < 0.0 ? -1.0 : 1.0, sd = d < 0.0 ? -1.0 : 1.0;
+    const double m1 = fabs(a) < fabs(b) ? fabs(a) : fabs(b), m2 = fabs(c) < fabs(d) ? fabs(c) : fabs(d);
+    const double p = fabs(__dmul_rn(__dadd_rn(sa, sc), __dadd_rn(sa, sd)));
+    return __dmul_rn(__dmul_rn(__dmul_rn(0.125, __dadd_rn(sa, sb)), p), m1 < m2 ? m1 : m2);
+}
+__device__ bool same_bits(double a, double b)
+{
+    return __double_as_longlong(a) == __double_as_longlong(b) || (a != a && b != b);
+}
+
+__global__ void sweep_arith_kernel(const unsigned long long *in, long long n, unsigned long long *cnt)
+{
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const double y = __longlong_as_double((long long)in[k]);
+        const double x = __longlong_as_double((long long)in[(k + 1) % n]);
+        const double z = __longlong_as_double((long long)in[(k + 2) % n]);
+        const double w = __longlong_as_double((long long)in[(k + 3) % n]);
+        const int c[3] = {ulp_class(wm::rcp_nr(y), 1.0 / y), ulp_class(wm::div_nr(x, y), x / y),
+                          ulp_class(wm::sqrt_nr(fabs(y)), sqrt(fabs(y)))};
+        for (int t = 0; t < 3; ++t)
+            if (c[t]) atomicAdd(&cnt[c[t] == 2 ? t : 3 + t], 1ull);
+        if (!same_bits(wm::mm2(y, x), mm2_hw(y, x))) atomicAdd(&cnt[6], 1ull);
+        if (!same_bits(wm::mm4(y, x, z, w), mm4_hw(y, x, z, w))) atomicAdd(&cnt[7], 1ull);
+    }
+}
+
 }  // namespace
+
+extern "C" int wm_check_sweep_arith(const unsigned long long *bits, long long n, long long counts[8], void *stream)
+{
+    if (!bits || n < 0 || !counts) return WM_ERR_INVALID;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    unsigned long long *ctr = nullptr, host[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    cudaError_t e = cudaMalloc(&ctr, sizeof host);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctr, 0, sizeof host, s);
+    if (e == cudaSuccess && n > 0) {
+        sweep_arith_kernel<<<1024, 256, 0, s>>>(bits, n, ctr);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host, ctr, sizeof host, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(ctr);
+    if (e != cudaSuccess) {
+        char msg[200];
+        snprintf(msg, sizeof msg, "wm_check_sweep_arith: %s", cudaGetErrorString(e));
+        wm::set_error_text(msg);
+        return WM_ERR_CUDA;
+    }
+    for (int t = 0; t < 8; ++t) counts[t] = (long long)host[t];
+    return WM_OK;
+}
 
 extern "C" int wm_check_conversions(const unsigned long long *bits, long long n, long long *bad_f32,
                                     long long *bad_f64, long long *bad_cmp, void *stream)

@@ -77,7 +77,8 @@ EXPORTS = ("wm_version", "wm_last_error", "wm_workspace_bytes", "wm_create", "wm
            "wm_batch_tile_shape", "wm_batch_scalars", "wm_batch_info", "wm_batch_profile",
            "wm_batch_profile_read", "wm_schlieren", "wm_run", "wm_run_uses_graph",
            "wm_set_limiter_sweeps", "wm_batch_dt_log", "wm_verify_limiter_precheck",
-           "wm_check_conversions", "wm_set_prechecks", "wm_verify_switch_precheck")
+           "wm_check_conversions", "wm_set_prechecks", "wm_verify_switch_precheck",
+           "wm_check_sweep_arith")
 STATIC_MAX_CELLS = 32768
 PROF_GROUPS = ("bc", "prep", "faces", "limiter", "final")
 BATCH_PHASES = ("bc_x", "bc_y", "prep", "sensor", "faces", "theta0", "theta1", "theta2", "final",
@@ -148,6 +149,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.wm_set_prechecks.argtypes = [vp, i]
     L.wm_check_conversions.argtypes = [vp, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong),
                                        ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong), vp]
+    L.wm_check_sweep_arith.argtypes = [vp, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong), vp]
     L.wm_verify_limiter_precheck.argtypes = [vp, F, d, ctypes.POINTER(ctypes.c_longlong),
                                              ctypes.POINTER(ctypes.c_longlong), vp]
     L.wm_verify_switch_precheck.argtypes = [vp, F, ctypes.POINTER(ctypes.c_longlong),
