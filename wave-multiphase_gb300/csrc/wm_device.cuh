@@ -274,13 +274,23 @@ __device__ __forceinline__ void mix_gamma_pinf(const Eos &e, T a1, T &g, T &pi)
     pi = pb * (gb * inv);
 }
 
-// sound_speed(rho, p, a1) with 1/rho supplied (SW: with the face sweep's reciprocal and root)
+// sound_speed(rho, p, a1) with 1/rho supplied. SW (the face sweep): the square root and, in
+// binary64, c^2 = g (p + p_inf) / rho written with the mixture's Gamma and Pi as
+// ((1 + Gamma) p + Pi) / (Gamma rho) (g = 1 + 1/Gamma, p_inf = Pi / (1 + Gamma)): one reciprocal
+// instead of mix_gamma_pinf's, the same value up to rounding.
 template <typename T, bool SW = false>
 __device__ __forceinline__ T sound_speed_r(const Eos &e, T inv_rho, T p, T a1)
 {
-    T g, pi;
-    mix_gamma_pinf<T, SW>(e, a1, g, pi);
-    T val = g * (p + pi) * inv_rho;
+    T val;
+    if constexpr (SW && sizeof(T) == 8) {
+        T gb, pb;
+        mix_gamma_pibig(e, a1, gb, pb);
+        val = ((T(1) + gb) * p + pb) * inv_rho * sw_rcp(gb);
+    } else {
+        T g, pi;
+        mix_gamma_pinf<T, SW>(e, a1, g, pi);
+        val = g * (p + pi) * inv_rho;
+    }
     if (flt(val, T(kTiny))) val = T(kTiny);
     return SW ? sw_sqrt(val) : wsqrt(val);
 }
@@ -558,11 +568,35 @@ template <typename T> __device__ __forceinline__ T thinc_ur(const Eos &e, T v0, 
     return result;
 }
 
+// MP5's fifth-order value from five cells, (2 a - 13 b + 47 c + 27 d - 3 e) / 60 (SC:355, 381):
+// binary64 with the 1/60 folded into the coefficients (one product fewer on the narrow pipe).
+template <typename T> __device__ __forceinline__ T mp5_vor(T a, T b, T c, T d, T e)
+{
+    if constexpr (sizeof(T) == 8)
+        return (2.0 / 60.0) * a - (13.0 / 60.0) * b + (47.0 / 60.0) * c + (27.0 / 60.0) * d - (3.0 / 60.0) * e;
+    else
+        return T(k1o60) * (T(2) * a - T(13) * b + T(47) * c + T(27) * d - T(3) * e);
+}
+// MP5's alpha x slope, alpha = 4: binary64 by adding 2 to the exponent on the integer pipe (the
+// exact product) where the result stays normal and finite; zeros, subnormals, infinities and NaN,
+// and values whose product would overflow, take the multiplication.
+static_assert(kMp5Alpha == 4.0, "mp5_alpha_times assumes alpha = 4");
+template <typename T> __device__ __forceinline__ T mp5_alpha_times(T x)
+{
+    if constexpr (sizeof(T) == 8) {
+        const long long b = __double_as_longlong(x);
+        const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+        return e - 1u < 2044u ? __longlong_as_double(b + (2LL << 52)) : 4.0 * x;
+    } else {
+        return T(kMp5Alpha) * x;
+    }
+}
+
 // Suresh-Huynh MP5, left-biased value at i+1/2 from cells i-2..i+2 (SC:353-377)
 template <typename T> __device__ __forceinline__ T mp5_ul(T vm2, T vm1, T v0, T vp1, T vp2)
 {
-    T VOR = T(k1o60) * (T(2) * vm2 - T(13) * vm1 + T(47) * v0 + T(27) * vp1 - T(3) * vp2);
-    T VMP = v0 + mm2(vp1 - v0, T(kMp5Alpha) * (v0 - vm1));
+    T VOR = mp5_vor(vm2, vm1, v0, vp1, vp2);
+    T VMP = v0 + mm2(vp1 - v0, mp5_alpha_times(v0 - vm1));
     T result = VOR;
     if (fge((VOR - v0) * (VOR - VMP), T(kEpsM))) {
         T DJM1 = vm2 - T(2) * vm1 + v0;
@@ -584,8 +618,12 @@ template <typename T> __device__ __forceinline__ T mp5_ul(T vm2, T vm1, T v0, T 
 // right-biased value at i+1/2 from cells i-1..i+3 (SC:379-405)
 template <typename T> __device__ __forceinline__ T mp5_ur(T vm1, T v0, T vp1, T vp2, T vp3)
 {
-    T VOR = T(k1o60) * (T(-3) * vm1 + T(27) * v0 + T(47) * vp1 - T(13) * vp2 + T(2) * vp3);
-    T VMP = vp1 + mm2(v0 - vp1, T(kMp5Alpha) * (vp1 - vp2));
+    T VOR;
+    if constexpr (sizeof(T) == 8)
+        VOR = mp5_vor(vp3, vp2, vp1, v0, vm1);
+    else
+        VOR = T(k1o60) * (T(-3) * vm1 + T(27) * v0 + T(47) * vp1 - T(13) * vp2 + T(2) * vp3);
+    T VMP = vp1 + mm2(v0 - vp1, mp5_alpha_times(vp1 - vp2));
     T result = VOR;
     if (fge((VOR - vp1) * (VOR - VMP), T(kEpsM))) {
         T DJM1 = vm1 - T(2) * v0 + vp1;
@@ -605,11 +643,17 @@ template <typename T> __device__ __forceinline__ T mp5_ur(T vm1, T v0, T vp1, T 
 }
 
 // sixth-order central face value (SC:407-412)
+// binary64: the mean of the two five-point values as one six-point combination,
+// (2 vm2 - 16 vm1 + 74 v0 + 74 vp1 - 16 vp2 + 2 vp3) / 120.
 template <typename T> __device__ __forceinline__ T central6_avg(T vm2, T vm1, T v0, T vp1, T vp2, T vp3)
 {
-    T left = T(k1o60) * (T(2) * vm2 - T(13) * vm1 + T(47) * v0 + T(27) * vp1 - T(3) * vp2);
-    T right = T(k1o60) * (T(-3) * vm1 + T(27) * v0 + T(47) * vp1 - T(13) * vp2 + T(2) * vp3);
-    return T(0.5) * (left + right);
+    if constexpr (sizeof(T) == 8) {
+        return (1.0 / 60.0) * (vm2 + vp3) - (8.0 / 60.0) * (vm1 + vp2) + (37.0 / 60.0) * (v0 + vp1);
+    } else {
+        T left = T(k1o60) * (T(2) * vm2 - T(13) * vm1 + T(47) * v0 + T(27) * vp1 - T(3) * vp2);
+        T right = T(k1o60) * (T(-3) * vm1 + T(27) * v0 + T(47) * vp1 - T(13) * vp2 + T(2) * vp3);
+        return T(0.5) * (left + right);
+    }
 }
 
 // fourth-order central face value (SC:1076-1082)
