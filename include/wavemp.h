@@ -292,14 +292,15 @@ int wm_schlieren(const wm_fields *q, int nx, int ny, int g, const double *xh, co
 int wm_check_conversions(const unsigned long long *bits, long long n, long long *bad_f32,
                          long long *bad_f64, long long *bad_cmp, void *stream);
 /* The binary64 face sweep's reciprocal, quotient and square root (a binary32 seed refined by fused
- * multiply-adds) against IEEE 1/y, x/y and sqrt(x), and its integer-pipe minmods against the
- * reference's sign-sum products on the hardware operations, on n device bit patterns (y: each
- * pattern, x, z, w: the next three, sqrt of |y|, mm2(y, x), mm4(y, x, z, w)). counts[0..2]:
- * results of rcp, div, sqrt that differ from IEEE by more than one unit in the last place, or that
- * are not bit-identical where either result is zero, infinite, subnormal or NaN (0 expected);
- * counts[3..5]: results one unit away; counts[6..7]: mm2, mm4 results that are not bit-identical
- * (NaN equal to NaN; 0 expected). No counterpart in the reference. */
-int wm_check_sweep_arith(const unsigned long long *bits, long long n, long long counts[8], void *stream);
+ * multiply-adds) against IEEE 1/y, x/y and sqrt(x), and its integer-pipe minmods, halving and
+ * sign selection against the reference's products on the hardware operations, on n device bit
+ * patterns (y: each pattern, x, z, w: the next three; sqrt of |y|, mm2(y, x), mm4(y, x, z, w),
+ * y / 2, 0.5 (1 + s) y + 0.5 (1 - s) x for s = +-1). counts[0..2]: results of rcp, div, sqrt
+ * that differ from IEEE by more than one unit in the last place, or that are not bit-identical
+ * where either result is zero, infinite, subnormal or NaN (0 expected); counts[3..5]: results one
+ * unit away; counts[6..9]: mm2, mm4, halving, selection results that are not bit-identical (NaN
+ * equal to NaN; 0 expected). No counterpart in the reference. */
+int wm_check_sweep_arith(const unsigned long long *bits, long long n, long long counts[10], void *stream);
 /* Copy workspace array `which` (WM_WS_*) of the padded grid into the caller's device buffer dst
  * (same padded shape, contiguous rows of ny + 2g). */
 #define WM_WS_FX 0      /* 7 arrays: high-order x fluxes 0..5 and srcx (after limit_fluxes: blended) */

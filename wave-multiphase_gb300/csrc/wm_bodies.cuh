@@ -1014,22 +1014,22 @@ __device__ __forceinline__ void face_body(const Eos &e, const V &v, const Face<F
     }
 
     // --- face-averaged state and eigenvector basis (SC:1039-1048) ------------------------------
-    const T ar1a = T(0.5) * (U0[0] + U1[0]);
-    const T ar2a = T(0.5) * (U0[1] + U1[1]);
-    const T a1a = T(0.5) * (U0[5] + U1[5]);
-    const T pa = T(0.5) * (U0[4] + U1[4]);
+    const T ar1a = half_of(U0[0] + U1[0]);
+    const T ar2a = half_of(U0[1] + U1[1]);
+    const T a1a = half_of(U0[5] + U1[5]);
+    const T pa = half_of(U0[4] + U1[4]);
     const T rhoa = ar1a + ar2a;
     const T irhoa = sw_rcp(rhoa);
     FaceBasis<T> b;
-    b.u = T(0.5) * (U0[2] + U1[2]) * irhoa;
-    b.v = T(0.5) * (U0[3] + U1[3]) * irhoa;
+    b.u = half_of(U0[2] + U1[2]) * irhoa;
+    b.v = half_of(U0[3] + U1[3]) * irhoa;
     const T ca = sound_speed_r<T, true>(e, irhoa, pa, a1a);
     {
         const T ic = sw_rcp(ca);
         b.c = ca;
         b.c2 = ca * ca;
-        b.inv2c = T(0.5) * ic;
-        b.inv2c2 = T(0.5) * (ic * ic);
+        b.inv2c = half_of(ic);
+        b.inv2c2 = half_of(ic * ic);
         b.Y1 = ar1a * irhoa;
         b.Y2 = ar2a * irhoa;
         b.Y1c2 = b.Y1 * (ic * ic);

@@ -519,6 +519,31 @@ template <> __device__ __forceinline__ double mm4(double a, double b, double c, 
     return zero_times(m, na && nb);
 }
 
+// x / 2: binary64 by subtracting 1 from the exponent on the integer pipe (the exact product) where
+// the result stays normal; zeros, subnormals, the smallest normals, infinities and NaN multiply.
+template <typename T> __device__ __forceinline__ T half_of(T x) { return T(0.5) * x; }
+template <> __device__ __forceinline__ double half_of(double x)
+{
+    const long long b = __double_as_longlong(x);
+    const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+    return e - 2u < 2045u ? __longlong_as_double(b - (1LL << 52)) : 0.5 * x;
+}
+
+// 0.5 (1 + s) a + 0.5 (1 - s) b for s = wsign(.) = +-1 (the interface velocity of hllc_x_src,
+// SC:760-768): one coefficient is 1 and the other 0, so the value is the chosen term plus 0 times
+// the other (a zero of the other's sign, or NaN when it is infinite or NaN). Binary64: that sum
+// on the integer pipe and one addition; binary32: the products.
+template <typename T> __device__ __forceinline__ T sign_select(T s, T a, T b)
+{
+    return T(0.5) * (T(1) + s) * a + T(0.5) * (T(1) - s) * b;
+}
+template <> __device__ __forceinline__ double sign_select(double s, double a, double b)
+{
+    const bool pick_a = !dneg(s);
+    const double other = pick_a ? b : a;  // (+0) other: a zero with other's sign bit, or NaN
+    return (pick_a ? a : b) + zero_times(other, __double_as_longlong(other) < 0);
+}
+
 // p / rho^gamma(alpha) (SC:308-314)
 template <typename T> __device__ __forceinline__ T cell_entropy(const Eos &e, T ar1, T ar2, T p, T a1)
 {
@@ -760,8 +785,8 @@ __device__ __forceinline__ void hllc(const Side<T> &L, const Side<T> &R, T f[6],
 {
     constexpr int N = DIR == 0 ? 2 : 3;  // normal momentum component
     constexpr int Tc = DIR == 0 ? 3 : 2; // tangential momentum component
-    T n_avg = T(0.5) * (L.un + R.un);
-    T c_avg = T(0.5) * (L.c + R.c);
+    T n_avg = half_of(L.un + R.un);
+    T c_avg = half_of(L.c + R.c);
     T SL = wmin(L.un - L.c, n_avg - c_avg);
     T SR = wmax(R.un + R.c, n_avg + c_avg);
     T denom = L.rho * (SL - L.un) - R.rho * (SR - R.un);
@@ -806,7 +831,7 @@ __device__ __forceinline__ void hllc(const Side<T> &L, const Side<T> &R, T f[6],
     T left_part = L.un + wmin(T(0), SL) * (ratioL - T(1));
     T right_part = R.un + wmax(T(0), SR) * (ratioR - T(1));
     T sp_sign = wsign(SP);
-    ustar = T(0.5) * (T(1) + sp_sign) * left_part + T(0.5) * (T(1) - sp_sign) * right_part;
+    ustar = sign_select(sp_sign, left_part, right_part);
 }
 
 // Blend of a high-order face value toward the first-order one (pp_blend_*_flux_kernel body,

@@ -167,16 +167,20 @@ __global__ void sweep_arith_kernel(const unsigned long long *in, long long n, un
             if (c[t]) atomicAdd(&cnt[c[t] == 2 ? t : 3 + t], 1ull);
         if (!same_bits(wm::mm2(y, x), mm2_hw(y, x))) atomicAdd(&cnt[6], 1ull);
         if (!same_bits(wm::mm4(y, x, z, w), mm4_hw(y, x, z, w))) atomicAdd(&cnt[7], 1ull);
+        if (!same_bits(wm::half_of(y), __dmul_rn(0.5, y))) atomicAdd(&cnt[8], 1ull);
+        const double s = (k & 1) ? -1.0 : 1.0;
+        const double sel = __fma_rn(__dmul_rn(0.5, __dadd_rn(1.0, s)), y, __dmul_rn(__dmul_rn(0.5, __dadd_rn(1.0, -s)), x));
+        if (!same_bits(wm::sign_select(s, y, x), sel)) atomicAdd(&cnt[9], 1ull);
     }
 }
 
 }  // namespace
 
-extern "C" int wm_check_sweep_arith(const unsigned long long *bits, long long n, long long counts[8], void *stream)
+extern "C" int wm_check_sweep_arith(const unsigned long long *bits, long long n, long long counts[10], void *stream)
 {
     if (!bits || n < 0 || !counts) return WM_ERR_INVALID;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    unsigned long long *ctr = nullptr, host[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    unsigned long long *ctr = nullptr, host[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     cudaError_t e = cudaMalloc(&ctr, sizeof host);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctr, 0, sizeof host, s);
     if (e == cudaSuccess && n > 0) {
@@ -192,7 +196,7 @@ extern "C" int wm_check_sweep_arith(const unsigned long long *bits, long long n,
         wm::set_error_text(msg);
         return WM_ERR_CUDA;
     }
-    for (int t = 0; t < 8; ++t) counts[t] = (long long)host[t];
+    for (int t = 0; t < 10; ++t) counts[t] = (long long)host[t];
     return WM_OK;
 }
 
