@@ -104,3 +104,27 @@ def test_restart_from_checkpoint_continues_the_run(tmp_path):
     sc = pu.natural_scales({k: pu.host(v) for k, v in q1.items()}, 4.4, 6e8, 1.4, 0.0)
     pu.assert_cells({k: pu.host(v) for k, v in q2.items()}, {k: pu.host(v) for k, v in q1.items()},
                     pu.FIELDS, sc, "restarted run", rtol=1e-9)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_step_from_conserved_state_alone(precision):
+    """A caller that keeps only the six conserved arrays (bench.py's end-to-end loop) copies them
+    in, rebuilds the primitives with update_prims and steps: the same bits as stepping the
+    device-resident state, whose primitives the previous step left."""
+    p, s, q, old = make(precision)
+    dt = s.get_dt(q)
+    s.step(q, old, dt)  # primitives now those the step leaves
+    q2 = alloc_state(NX, NY)
+    for k in wavemp.FIELDS:
+        q2[k].copy_(q[k])
+    for k in ("u_p", "v_p", "p_p", "al_prim"):
+        q2[k].fill_(float("nan"))
+    s2 = Solver(p, NX, NY)
+    old2 = alloc_state(NX, NY, names=wavemp.FIELDS)
+    s2.update_prims(q2)
+    for k in wavemp.ALL:
+        assert torch.equal(q2[k], q[k]), k
+    s.step(q, old, dt)
+    s2.step(q2, old2, dt)
+    for k in wavemp.ALL:
+        assert torch.equal(q2[k], q[k]), k
