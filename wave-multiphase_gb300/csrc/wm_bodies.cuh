@@ -582,15 +582,27 @@ __device__ __forceinline__ void blend_body(const Grid &g, const Face<FT> &fh, co
                                            const FT *theta, int i, int j)
 {
     long long kw = kw_of(g, i, j);
+    // Binary64: a face at theta = 1 whose low-order values are all finite keeps its high-order
+    // values (face_blend's value there): only its low-order values are read, nothing is written.
     if (j >= g.g) {  // x face between (i, j) and (i+1, j)
         const FT t = face_theta_x(g, theta, kw, i);
+        bool keep = sizeof(FT) == 8 && is_one(t);
 #pragma unroll
-        for (int c = 0; c < 7; ++c) fh.f[c][kw] = face_blend(fl.f[c][kw], fh.f[c][kw], t);
+        for (int c = 0; c < 7; ++c) keep = keep && finite_bits(fl.f[c][kw]);
+        if (!keep) {
+#pragma unroll
+            for (int c = 0; c < 7; ++c) fh.f[c][kw] = face_blend(fl.f[c][kw], fh.f[c][kw], t);
+        }
     }
     if (i >= g.g) {  // y face between (i, j) and (i, j+1)
         const FT t = face_theta_y(g, theta, kw, j);
+        bool keep = sizeof(FT) == 8 && is_one(t);
 #pragma unroll
-        for (int c = 0; c < 7; ++c) gh.f[c][kw] = face_blend(gl.f[c][kw], gh.f[c][kw], t);
+        for (int c = 0; c < 7; ++c) keep = keep && finite_bits(gl.f[c][kw]);
+        if (!keep) {
+#pragma unroll
+            for (int c = 0; c < 7; ++c) gh.f[c][kw] = face_blend(gl.f[c][kw], gh.f[c][kw], t);
+        }
     }
 }
 

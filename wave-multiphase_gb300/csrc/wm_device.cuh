@@ -834,12 +834,25 @@ __device__ __forceinline__ void hllc(const Side<T> &L, const Side<T> &R, T f[6],
     ustar = sign_select(sp_sign, left_part, right_part);
 }
 
-// Blend of a high-order face value toward the first-order one (pp_blend_*_flux_kernel body,
-// SC:1506-1512). Shared by the in-place limiter and the fused stage so both round alike.
+// Blend of a high-order face value toward the first-order one, low + theta (high - low)
+// (pp_blend_*_flux_kernel body, SC:1506-1512), with one deliberate difference in binary64: at
+// theta = 1 with a finite low value it is the high value itself -- the blend's exact value, where the reference's
+// low + (high - low) can round one unit away -- so a face the limiter leaves alone keeps its
+// high-order flux and the in-place blend need not rewrite it. A non-finite low, high or theta
+// takes the formula (NaN propagates as in the reference). Shared by the in-place limiter and the
+// fused stage so both give the same bits. The tests are integer compares of the bit patterns.
+__device__ __forceinline__ bool is_one(double t) { return __double_as_longlong(t) == 0x3ff0000000000000LL; }
+__device__ __forceinline__ bool is_one(float t) { return __float_as_uint(t) == 0x3f800000u; }
+__device__ __forceinline__ bool finite_bits(double x)
+{
+    return (__double_as_longlong(x) & 0x7fffffffffffffffLL) < 0x7ff0000000000000LL;
+}
+__device__ __forceinline__ bool finite_bits(float x) { return (__float_as_uint(x) & 0x7fffffffu) < 0x7f800000u; }
 __device__ __forceinline__ double face_blend(double low, double high, double theta)
 {
-    return __fma_rn(theta, high - low, low);
+    return is_one(theta) && finite_bits(low) ? high : __fma_rn(theta, high - low, low);
 }
+// Binary32 (the precision form's rebuilt blends, which have no in-place sweep to skip): the formula.
 __device__ __forceinline__ float face_blend(float low, float high, float theta)
 {
     return __fmaf_rn(theta, high - low, low);
