@@ -47,7 +47,7 @@ SAMPLE_NX, SAMPLE_NY = 3584, 1536    # CPU sample: a quarter of the cells of the
 # summarised in profiles/ (None until measured).
 FP64_FLOP_PER_FACE = 814.0  # DFMA x 2 + DADD + DMUL, profiles/face_kernel_triple_point_2048x1024_fp64.md
 DRAM_BYTES_PER_CELL_STAGE_FP32 = 1265.0
-DRAM_BYTES_PER_CELL_STAGE = 2140.0  # profiles/dram_traffic_triple_point_2048x1024.md
+DRAM_BYTES_PER_CELL_STAGE = 1673.0  # profiles/dram_traffic_triple_point_2048x1024.md
 
 
 def params(nx=None, ny=None, precision="fp64"):

@@ -170,12 +170,13 @@ __device__ __forceinline__ bool floor_quotient_below(double x, double d, double 
 }
 
 // sound_speed_r's value for the mixture (g, pi) the caller already holds: sqrt(max(g (p + pi) / rho,
-// 1e-20)) with 1/rho supplied, the same operations in the same order.
+// 1e-20)) with 1/rho supplied, the same operations in the same order, the root refined from a
+// binary32 seed (sqrt_nr).
 __device__ __forceinline__ double sound_speed_gp(double g, double pi, double inv_rho, double p)
 {
     double val = g * (p + pi) * inv_rho;
     if (flt(val, kTiny)) val = kTiny;
-    return wsqrt(val);
+    return sqrt_nr(val);
 }
 
 // Entropy (SC:308-314) and the first-order HLLC cell state of fx_low_kernel (SC:1309-1327), both
@@ -192,7 +193,7 @@ __device__ __forceinline__ void prep_body(const Grid &g, const Eos &e, const Fie
     store_entropy(p, kw, ge, ar1, ar2, pp, prechecks);
 
     double rho = ar1 + ar2;
-    double ir = 1.0 / rho;
+    double ir = rcp_nr(rho);  // 1 / rho (the face sweep's refined reciprocal)
     double a = clamp01_pp(al);
     double gg = ge, pi = pie;
     if (!(a == al)) mix_gamma_pinf(e, a, gg, pi);
@@ -203,7 +204,7 @@ __device__ __forceinline__ void prep_body(const Grid &g, const Eos &e, const Fie
     p.lv[kw] = v;
     p.lp[kw] = pl;
     p.la[kw] = a;
-    p.lc[kw] = sound_speed_gp(gg, pi, ir, pl);  // = sound_speed_r(e, ir, pl, a): (gg, pi) is its mixture
+    p.lc[kw] = sound_speed_gp(gg, pi, ir, pl);  // sound_speed_r(e, ir, pl, a): (gg, pi) is its mixture
     p.lE[kw] = prim_to_energy(e, rho, u, v, pl, a);
 }
 
@@ -635,27 +636,23 @@ __device__ __forceinline__ bool cell_surely_admissible(const Eos &e, const doubl
     return v > 4.0e-6f * mag;
 }
 
-// 1 / (rho Gamma) of the primitive recovery. Plain form: the binary64 quotient. Precision form: the
-// Newton-Raphson reciprocal iteration y <- y + y (1 - x y) in binary64 (residual and update each
-// one fused multiply-add; e.g. Muller et al., Handbook of Floating-Point Arithmetic, ch. 5), seeded
-// with the binary32 reciprocal of x rounded to binary32 (relative error below 2^-23). Two steps
-// square that to below 2^-92 before their own roundings, so the result is within about one unit in
-// the last place of the quotient -- binary64 accuracy for the accumulation, without the division's
-// longer binary64 sequence. Outside binary32's normal range it divides.
-template <typename FT>
+// 1 / (rho Gamma) of the primitive recovery, both forms: the Newton-Raphson reciprocal iteration
+// y <- y + y (1 - x y) in binary64 (residual and update each one fused multiply-add; e.g. Muller et
+// al., Handbook of Floating-Point Arithmetic, ch. 5), seeded with the binary32 reciprocal of x
+// rounded to binary32 (relative error below 2^-23). Two steps square that to below 2^-92 before
+// their own roundings, so the result is within about one unit in the last place of the quotient --
+// binary64 accuracy for the accumulation, without the division's longer binary64 sequence. Outside
+// binary32's normal range it divides. One form for every instantiation of the combine, so the
+// closures (which run the binary64 one for both forms) and the fused stage give the same bits.
 __device__ __forceinline__ double recovery_recip(double x)
 {
-    if constexpr (sizeof(FT) == 8) {
-        return 1.0 / x;
-    } else {
-        const float xf = to_f32(x), af = fabsf(xf);
-        if (!(af >= 1.0e-37f && af <= 1.0e37f)) return 1.0 / x;
-        double y = to_f64(__frcp_rn(xf));
-        double r = __fma_rn(-x, y, 1.0);
-        y = __fma_rn(y, r, y);
-        r = __fma_rn(-x, y, 1.0);
-        return __fma_rn(y, r, y);
-    }
+    const float xf = to_f32(x), af = fabsf(xf);
+    if (!(af >= 1.0e-37f && af <= 1.0e37f)) return 1.0 / x;
+    double y = to_f64(__frcp_rn(xf));
+    double r = __fma_rn(-x, y, 1.0);
+    y = __fma_rn(y, r, y);
+    r = __fma_rn(-x, y, 1.0);
+    return __fma_rn(y, r, y);
 }
 
 // NP: limiter passes whose blends are deferred (3 in the fused stage: the limited fluxes are rebuilt
@@ -723,7 +720,7 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
             const double a1 = Q[F_AL], rho = Q[0] + Q[1];
             double gb, pb;
             mix_gamma_pibig(e, a1, gb, pb);
-            rg_a1 = a1; rg_rho = rho; rg_inv = recovery_recip<FT>(rho * gb); rg_gb = gb; rg_pb = pb;
+            rg_a1 = a1; rg_rho = rho; rg_inv = recovery_recip(rho * gb); rg_gb = gb; rg_pb = pb;
             wrote_q = true;
         } else if (flags & FIN_ADMISSIBLE) {
             double a1 = clamp01_pp(Q[F_AL]);
@@ -736,7 +733,7 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
             double rho = m1 + m2;
             double gb, pb;
             mix_gamma_pibig(e, a1, gb, pb);
-            const double inv = recovery_recip<FT>(rho * gb);
+            const double inv = recovery_recip(rho * gb);
             const double ir = gb * inv;
             double uu = mx * ir, vv = my * ir;
             double kin = 0.5 * rho * (uu * uu + vv * vv);
@@ -776,7 +773,7 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
                 gb = rg_gb; pb = rg_pb; inv = rg_inv;
             } else {
                 mix_gamma_pibig(e, a1, gb, pb);
-                inv = recovery_recip<FT>(rho * gb);
+                inv = recovery_recip(rho * gb);
             }
             double ir = gb * inv;
             double uu = Q[2] * ir, vv = Q[3] * ir;
@@ -800,10 +797,11 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
                     const double d = to_f64((dxf * dyf) / (dyf * a + dxf * b));
                     dt_bits = (unsigned long long)__double_as_longlong(d);
                 } else {
-                    double c = sound_speed_r(e, ir, pp, a1);
-                    double sx = g.dx / (fabs(uu) + c);
-                    double sy = g.dy / (fabs(vv) + c);
-                    double d = sx * sy / (sx + sy);
+                    // timestep_kernel's sx sy / (sx + sy), sx = dx / (|u| + c), sy = dy / (|v| + c)
+                    // (SC:1686-1705), as one quotient dx dy / (dy (|u| + c) + dx (|v| + c)), with
+                    // the face sweep's sound speed and quotient
+                    const double c = sound_speed_r<double, true>(e, ir, pp, a1);
+                    const double d = div_nr(g.dx * g.dy, g.dy * (fabs(uu) + c) + g.dx * (fabs(vv) + c));
                     dt_bits = (unsigned long long)__double_as_longlong(d);
                 }
             }

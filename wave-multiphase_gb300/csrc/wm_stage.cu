@@ -205,10 +205,10 @@ __global__ void dt_cell_kernel(Grid g, Eos e, Fields q, unsigned long long *dt_b
     if (i < g.g + g.nx && j < g.g + g.ny) {
         long long kf = kf_of(q, i, j);
         double rho = q.f[F_AR1][kf] + q.f[F_AR2][kf];
-        double c = sound_speed_r(e, 1.0 / rho, q.f[F_P][kf], q.f[F_AL][kf]);
-        double sx = g.dx / (fabs(q.f[F_U][kf]) + c);
-        double sy = g.dy / (fabs(q.f[F_V][kf]) + c);
-        bits = (unsigned long long)__double_as_longlong(sx * sy / (sx + sy));
+        // sx sy / (sx + sy) as one quotient, as the fused combine evaluates it (final_body)
+        const double c = sound_speed_r<double, true>(e, rcp_nr(rho), q.f[F_P][kf], q.f[F_AL][kf]);
+        const double d = div_nr(g.dx * g.dy, g.dy * (fabs(q.f[F_U][kf]) + c) + g.dx * (fabs(q.f[F_V][kf]) + c));
+        bits = (unsigned long long)__double_as_longlong(d);
     }
     for (int o = 16; o > 0; o >>= 1) {
         unsigned long long other = __shfl_down_sync(0xffffffffu, bits, o);
