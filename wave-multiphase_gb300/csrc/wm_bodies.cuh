@@ -1081,8 +1081,15 @@ __device__ __forceinline__ void face_body(const Eos &e, const V &v, const Face<F
             wL[f] = iph;
             wR[f] = iph;
         } else if (REC == kMp5) {
-            wL[f] = mp5_ul(W[0][f], W[1][f], W[2][f], W[3][f], W[4][f]);
-            wR[f] = mp5_ur(W[1][f], W[2][f], W[3][f], W[4][f], W[5][f]);
+            if constexpr (sizeof(T) == 8) {  // difference form, the differences shared by both values
+                const T d0 = W[1][f] - W[0][f], d1 = W[2][f] - W[1][f], d2 = W[3][f] - W[2][f];
+                const T d3 = W[4][f] - W[3][f], d4 = W[5][f] - W[4][f];
+                wL[f] = mp5_diff(W[2][f], W[3][f], d0, d1, d2, d3);
+                wR[f] = mp5_diff(W[3][f], W[2][f], -d4, -d3, -d2, -d1);
+            } else {
+                wL[f] = mp5_ul(W[0][f], W[1][f], W[2][f], W[3][f], W[4][f]);
+                wR[f] = mp5_ur(W[1][f], W[2][f], W[3][f], W[4][f], W[5][f]);
+            }
         } else {
             wL[f] = muscl_char_ul(W[1][f], W[2][f], W[3][f]);
             wR[f] = muscl_char_ur(W[2][f], W[3][f], W[4][f]);

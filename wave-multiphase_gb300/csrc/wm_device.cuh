@@ -640,6 +640,36 @@ template <typename T> __device__ __forceinline__ T mp5_ul(T vm2, T vm1, T v0, T 
     return result;
 }
 
+// MP5 in difference form (binary64 sweep): the value at the face from the stencil's centre c, the
+// neighbour across the face p1 = v(+1), and the differences dm2 = v(-1) - v(-2), dm1 = c - v(-1),
+// d0 = p1 - c, d1 = v(+2) - p1, the
+// left-biased value of mp5_ul with (vm2, vm1, v0, vp1, vp2). The same terms, each from differences:
+// VOR - v0 = (-2 dm2 + 11 dm1 + 24 d0 - 3 d1) / 60 (the five-point weights sum to 1), the test
+// (VOR - v0)(VOR - VMP) >= eps with VMP - v0 = mm2(d0, 4 dm1), the second differences
+// DJM1 = dm1 - dm2, DJ = d0 - dm1, DJP1 = d1 - d0, VUL = v0 + 4 dm1, VAV = v0 + d0 / 2,
+// VLC = v0 + dm1 / 2 + 4/3 DM4JMH. The right-biased value of mp5_ur at the same face is this
+// function of the mirrored stencil: centre vp1, neighbour v0 and differences -(vp3 - vp2),
+// -(vp2 - vp1), -(vp1 - v0), -(v0 - vm1) (every term of mp5_ur maps onto one of mp5_ul). One subtraction per
+// difference, shared by the two values of a field, replaces the stencil sums; values equal the
+// reference's up to rounding.
+__device__ __forceinline__ double mp5_diff(double c, double p1, double dm2, double dm1, double d0, double d1)
+{
+    const double D = (-2.0 / 60.0) * dm2 + (11.0 / 60.0) * dm1 + (24.0 / 60.0) * d0 - (3.0 / 60.0) * d1;
+    const double VOR = c + D;
+    const double m = mm2(d0, mp5_alpha_times(dm1));
+    if (!fge(D * (D - m), kEpsM)) return VOR;
+    const double DJM1 = dm1 - dm2, DJ = d0 - dm1, DJP1 = d1 - d0;
+    const double DM4JPH = mm4(4.0 * DJ - DJP1, 4.0 * DJP1 - DJ, DJ, DJP1);
+    const double DM4JMH = mm4(4.0 * DJ - DJM1, 4.0 * DJM1 - DJ, DJ, DJM1);
+    const double VUL = c + mp5_alpha_times(dm1);
+    const double VAV = c + half_of(d0);
+    const double VMD = VAV - 0.5 * DM4JPH;
+    const double VLC = c + half_of(dm1) + kB2 * DM4JMH;
+    const double VMIN = wmax(wmin(wmin(c, p1), VMD), wmin(wmin(c, VUL), VLC));
+    const double VMAX = wmin(wmax(wmax(c, p1), VMD), wmax(wmax(c, VUL), VLC));
+    return VOR + mm2(VMIN - VOR, VMAX - VOR);
+}
+
 // right-biased value at i+1/2 from cells i-1..i+3 (SC:379-405)
 template <typename T> __device__ __forceinline__ T mp5_ur(T vm1, T v0, T vp1, T vp2, T vp3)
 {
