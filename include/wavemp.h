@@ -299,8 +299,10 @@ int wm_check_conversions(const unsigned long long *bits, long long n, long long 
  * that differ from IEEE by more than one unit in the last place, or that are not bit-identical
  * where either result is zero, infinite, subnormal or NaN (0 expected); counts[3..5]: results one
  * unit away; counts[6..9]: mm2, mm4, halving, selection results that are not bit-identical (NaN
- * equal to NaN; 0 expected). No counterpart in the reference. */
-int wm_check_sweep_arith(const unsigned long long *bits, long long n, long long counts[10], void *stream);
+ * equal to NaN; 0 expected); counts[10]: pairs of quotients x / y, w / z from one shared reciprocal
+ * that are more than four units from IEEE or not bit-identical at special values (0 expected). No
+ * counterpart in the reference. */
+int wm_check_sweep_arith(const unsigned long long *bits, long long n, long long counts[11], void *stream);
 /* Copy workspace array `which` (WM_WS_*) of the padded grid into the caller's device buffer dst
  * (same padded shape, contiguous rows of ny + 2g). */
 #define WM_WS_FX 0      /* 7 arrays: high-order x fluxes 0..5 and srcx (after limit_fluxes: blended) */

@@ -217,6 +217,26 @@ __device__ __forceinline__ double sqrt_nr(double x)
     z = __fma_rn(__fma_rn(-z, z, x), hh, z);
     return __fma_rn(__fma_rn(-z, z, x), hh, z);
 }
+// Two quotients a / b and c / d. Binary64: from one refined reciprocal of the product,
+// a (d r) and c (b r) with r = rcp_nr(b d) -- 8 operations instead of 12, within a few units in the
+// last place -- where b, d and b d lie in rcp_nr's seeded range and a, c in div_nr's (so every
+// product stays normal); else, and in binary32, the two quotients.
+__device__ __forceinline__ void div2_nr(double a, double b, double c, double d, double &q1, double &q2)
+{
+    const double bd = __dmul_rn(b, d);
+    const unsigned e = exp_bits((unsigned)__double2hiint(bd));
+    const unsigned eb = exp_bits((unsigned)__double2hiint(b)), ed = exp_bits((unsigned)__double2hiint(d));
+    const unsigned ea = exp_bits((unsigned)__double2hiint(a)), ec = exp_bits((unsigned)__double2hiint(c));
+    if (e - 898u > 249u || eb - 898u > 249u || ed - 898u > 249u || ea - 127u > 1792u || ec - 127u > 1792u) {
+        q1 = div_nr(a, b);
+        q2 = div_nr(c, d);
+        return;
+    }
+    const double r = rcp_refine(bd, (unsigned)__double2hiint(bd), e);
+    q1 = __dmul_rn(a, __dmul_rn(d, r));
+    q2 = __dmul_rn(c, __dmul_rn(b, r));
+}
+
 // The face sweep's forms in the arithmetic type T: binary32 keeps the hardware operations.
 template <typename T> __device__ __forceinline__ T sw_rcp(T y) { return T(1) / y; }
 template <typename T> __device__ __forceinline__ T sw_div(T x, T y) { return x / y; }
@@ -224,6 +244,15 @@ template <typename T> __device__ __forceinline__ T sw_sqrt(T x) { return sqrtf(x
 template <> __device__ __forceinline__ double sw_rcp(double y) { return rcp_nr(y); }
 template <> __device__ __forceinline__ double sw_div(double x, double y) { return div_nr(x, y); }
 template <> __device__ __forceinline__ double sw_sqrt(double x) { return sqrt_nr(x); }
+template <typename T> __device__ __forceinline__ void sw_div2(T a, T b, T c, T d, T &q1, T &q2)
+{
+    q1 = a / b;
+    q2 = c / d;
+}
+template <> __device__ __forceinline__ void sw_div2(double a, double b, double c, double d, double &q1, double &q2)
+{
+    div2_nr(a, b, c, d, q1, q2);
+}
 
 // The reference's wp.min / wp.max / wp.sign: a < b ? a : b, a > b ? a : b, x < 0 ? -1 : 1
 // (binary64: by the integer compares above, the same results).
@@ -822,8 +851,8 @@ __device__ __forceinline__ void hllc(const Side<T> &L, const Side<T> &R, T f[6],
     T denom = L.rho * (SL - L.un) - R.rho * (SR - R.un);
     if (flt(wabs(denom), T(kTiny))) denom = T(kTiny);
     T SP = sw_div(R.p - L.p + L.rho * L.un * (SL - L.un) - R.rho * R.un * (SR - R.un), denom);
-    T ratioL = sw_div(SL - L.un, SL - SP);
-    T ratioR = sw_div(SR - R.un, SR - SP);
+    T ratioL, ratioR;
+    sw_div2(SL - L.un, SL - SP, SR - R.un, SR - SP, ratioL, ratioR);
 
     if (fpos(SL)) {
         f[0] = L.ar1 * L.un;

@@ -153,6 +153,16 @@ __device__ bool same_bits(double a, double b)
 {
     return __double_as_longlong(a) == __double_as_longlong(b) || (a != a && b != b);
 }
+// a within n units in the last place of b (both finite, normal and of one sign), or the same bits
+__device__ bool within_ulps(double a, double b, long long n)
+{
+    if (same_bits(a, b)) return true;
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    const long long ma = ia & 0x7fffffffffffffffLL, mb = ib & 0x7fffffffffffffffLL;
+    const long long lo = 0x0010000000000000LL, hi = 0x7ff0000000000000LL;
+    if ((ia ^ ib) < 0 || ma < lo || mb < lo || ma >= hi || mb >= hi) return false;
+    return ma - mb <= n && mb - ma <= n;
+}
 
 __global__ void sweep_arith_kernel(const unsigned long long *in, long long n, unsigned long long *cnt)
 {
@@ -171,16 +181,19 @@ __global__ void sweep_arith_kernel(const unsigned long long *in, long long n, un
         const double s = (k & 1) ? -1.0 : 1.0;
         const double sel = __fma_rn(__dmul_rn(0.5, __dadd_rn(1.0, s)), y, __dmul_rn(__dmul_rn(0.5, __dadd_rn(1.0, -s)), x));
         if (!same_bits(wm::sign_select(s, y, x), sel)) atomicAdd(&cnt[9], 1ull);
+        double q1, q2;
+        wm::div2_nr(x, y, w, z, q1, q2);
+        if (!within_ulps(q1, x / y, 4) || !within_ulps(q2, w / z, 4)) atomicAdd(&cnt[10], 1ull);
     }
 }
 
 }  // namespace
 
-extern "C" int wm_check_sweep_arith(const unsigned long long *bits, long long n, long long counts[10], void *stream)
+extern "C" int wm_check_sweep_arith(const unsigned long long *bits, long long n, long long counts[11], void *stream)
 {
     if (!bits || n < 0 || !counts) return WM_ERR_INVALID;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    unsigned long long *ctr = nullptr, host[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    unsigned long long *ctr = nullptr, host[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     cudaError_t e = cudaMalloc(&ctr, sizeof host);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctr, 0, sizeof host, s);
     if (e == cudaSuccess && n > 0) {
@@ -196,7 +209,7 @@ extern "C" int wm_check_sweep_arith(const unsigned long long *bits, long long n,
         wm::set_error_text(msg);
         return WM_ERR_CUDA;
     }
-    for (int t = 0; t < 10; ++t) counts[t] = (long long)host[t];
+    for (int t = 0; t < 11; ++t) counts[t] = (long long)host[t];
     return WM_OK;
 }
 
