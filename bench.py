@@ -45,7 +45,7 @@ ALG_BYTES_PER_CELL_STAGE = 128.0     # read stage state + step-start state, writ
 SAMPLE_NX, SAMPLE_NY = 3584, 1536    # CPU sample: a quarter of the cells of the same problem
 # Face-sweep binary64 work per face (x or y) and traffic per cell-stage, from the ncu captures
 # summarised in profiles/ (None until measured).
-FP64_FLOP_PER_FACE = 814.0  # DFMA x 2 + DADD + DMUL, profiles/face_kernel_triple_point_2048x1024_fp64.md
+FP64_FLOP_PER_FACE = 721.0  # DFMA x 2 + DADD + DMUL, profiles/face_kernel_triple_point_2048x1024_fp64.md
 DRAM_BYTES_PER_CELL_STAGE_FP32 = 1265.0
 DRAM_BYTES_PER_CELL_STAGE = 1673.0  # profiles/dram_traffic_triple_point_2048x1024.md
 
