@@ -671,8 +671,8 @@ template <typename T> __device__ __forceinline__ T mp5_ul(T vm2, T vm1, T v0, T 
 
 // MP5 in difference form (binary64 sweep): the value at the face from the stencil's centre c, the
 // neighbour across the face p1 = v(+1), and the differences dm2 = v(-1) - v(-2), dm1 = c - v(-1),
-// d0 = p1 - c, d1 = v(+2) - p1, the
-// left-biased value of mp5_ul with (vm2, vm1, v0, vp1, vp2). The same terms, each from differences:
+// d0 = p1 - c, d1 = v(+2) - p1 -- the left-biased value of mp5_ul with (vm2, vm1, v0, vp1, vp2).
+// The same terms, each from differences:
 // VOR - v0 = (-2 dm2 + 11 dm1 + 24 d0 - 3 d1) / 60 (the five-point weights sum to 1), the test
 // (VOR - v0)(VOR - VMP) >= eps with VMP - v0 = mm2(d0, 4 dm1), the second differences
 // DJM1 = dm1 - dm2, DJ = d0 - dm1, DJP1 = d1 - d0, VUL = v0 + 4 dm1, VAV = v0 + d0 / 2,
