@@ -622,15 +622,6 @@ template <typename T> __device__ __forceinline__ T thinc_ur(const Eos &e, T v0, 
     return result;
 }
 
-// MP5's fifth-order value from five cells, (2 a - 13 b + 47 c + 27 d - 3 e) / 60 (SC:355, 381):
-// binary64 with the 1/60 folded into the coefficients (one product fewer on the narrow pipe).
-template <typename T> __device__ __forceinline__ T mp5_vor(T a, T b, T c, T d, T e)
-{
-    if constexpr (sizeof(T) == 8)
-        return (2.0 / 60.0) * a - (13.0 / 60.0) * b + (47.0 / 60.0) * c + (27.0 / 60.0) * d - (3.0 / 60.0) * e;
-    else
-        return T(k1o60) * (T(2) * a - T(13) * b + T(47) * c + T(27) * d - T(3) * e);
-}
 // MP5's alpha x slope, alpha = 4: binary64 by adding 2 to the exponent on the integer pipe (the
 // exact product) where the result stays normal and finite; zeros, subnormals, infinities and NaN,
 // and values whose product would overflow, take the multiplication.
@@ -646,10 +637,11 @@ template <typename T> __device__ __forceinline__ T mp5_alpha_times(T x)
     }
 }
 
-// Suresh-Huynh MP5, left-biased value at i+1/2 from cells i-2..i+2 (SC:353-377)
+// Suresh-Huynh MP5, left-biased value at i+1/2 from cells i-2..i+2 (SC:353-377). The binary32
+// sweep's form; the binary64 sweep uses mp5_diff.
 template <typename T> __device__ __forceinline__ T mp5_ul(T vm2, T vm1, T v0, T vp1, T vp2)
 {
-    T VOR = mp5_vor(vm2, vm1, v0, vp1, vp2);
+    T VOR = T(k1o60) * (T(2) * vm2 - T(13) * vm1 + T(47) * v0 + T(27) * vp1 - T(3) * vp2);
     T VMP = v0 + mm2(vp1 - v0, mp5_alpha_times(v0 - vm1));
     T result = VOR;
     if (fge((VOR - v0) * (VOR - VMP), T(kEpsM))) {
@@ -702,11 +694,7 @@ __device__ __forceinline__ double mp5_diff(double c, double p1, double dm2, doub
 // right-biased value at i+1/2 from cells i-1..i+3 (SC:379-405)
 template <typename T> __device__ __forceinline__ T mp5_ur(T vm1, T v0, T vp1, T vp2, T vp3)
 {
-    T VOR;
-    if constexpr (sizeof(T) == 8)
-        VOR = mp5_vor(vp3, vp2, vp1, v0, vm1);
-    else
-        VOR = T(k1o60) * (T(-3) * vm1 + T(27) * v0 + T(47) * vp1 - T(13) * vp2 + T(2) * vp3);
+    T VOR = T(k1o60) * (T(-3) * vm1 + T(27) * v0 + T(47) * vp1 - T(13) * vp2 + T(2) * vp3);
     T VMP = vp1 + mm2(v0 - vp1, mp5_alpha_times(vp1 - vp2));
     T result = VOR;
     if (fge((VOR - vp1) * (VOR - VMP), T(kEpsM))) {
