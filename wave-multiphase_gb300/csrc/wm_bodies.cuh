@@ -1154,10 +1154,15 @@ __device__ __forceinline__ void face_body(const Eos &e, const V &v, const Face<F
         d.p = ph.v[4];
         d.a = ph.v[5];
         d.c = sound_speed_r<T, true>(e, ir, d.p, d.a);
-        d.E = prim_to_energy(e, d.rho, d.un, d.ut, d.p, d.a);
+        if constexpr (sizeof(T) == 8) {  // hllc forms the energy of the side it reads
+            mix_gamma_pibig(e, d.a, d.gb, d.pb);
+            d.E = T(0);
+        } else {
+            d.E = prim_to_energy(e, d.rho, d.un, d.ut, d.p, d.a);
+        }
     }
     T f[6], us;
-    hllc<DIR>(S[0], S[1], f, us);
+    hllc<DIR, sizeof(T) == 8>(S[0], S[1], f, us);
 #pragma unroll
     for (int c = 0; c < 6; ++c) hi.f[c][kw] = FT(f[c]);
     hi.f[6][kw] = FT(us);

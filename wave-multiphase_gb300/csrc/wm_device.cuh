@@ -822,12 +822,16 @@ template <int DIR, typename T> __device__ __forceinline__ S6<T> to_phys(const Fa
 // ------------------------------------------------------------------------------------------------
 template <typename T> struct Side {
     T ar1, ar2, rho, un, ut, p, a, c, E;
+    T gb, pb;  // the mixture's Gamma and Pi (hllc with LAZY_E forms E from them)
 };
 
 // Flux f[0..5] in SC component order and the interface velocity u* for the alpha source.
 // hllc_x/hllc_y and hllc_x_src/hllc_y_src of the reference recompute the same wave speeds; here
 // they are computed once.
-template <int DIR, typename T>
+// LAZY_E: the sides carry Gamma and Pi instead of E, and hllc forms the total energy of the one side
+// its branch reads (L for the left and star-left fluxes, R for the others) by prim_to_energy's
+// expression -- the same value, for one side instead of two.
+template <int DIR, bool LAZY_E = false, typename T>
 __device__ __forceinline__ void hllc(const Side<T> &L, const Side<T> &R, T f[6], T &ustar)
 {
     constexpr int N = DIR == 0 ? 2 : 3;  // normal momentum component
@@ -841,38 +845,45 @@ __device__ __forceinline__ void hllc(const Side<T> &L, const Side<T> &R, T f[6],
     T SP = sw_div(R.p - L.p + L.rho * L.un * (SL - L.un) - R.rho * R.un * (SR - R.un), denom);
     T ratioL, ratioR;
     sw_div2(SL - L.un, SL - SP, SR - R.un, SR - SP, ratioL, ratioR);
+    T EL = L.E, ER = R.E;
+    if constexpr (LAZY_E) {
+        const bool left = fpos(SL) || (fle(SL, T(0)) && fpos(SP));
+        const T rho = left ? L.rho : R.rho, un = left ? L.un : R.un, ut = left ? L.ut : R.ut;
+        const T p = left ? L.p : R.p, gb = left ? L.gb : R.gb, pb = left ? L.pb : R.pb;
+        EL = ER = gb * p + pb + T(0.5) * rho * (un * un + ut * ut);
+    }
 
     if (fpos(SL)) {
         f[0] = L.ar1 * L.un;
         f[1] = L.ar2 * L.un;
         f[N] = L.rho * L.un * L.un + L.p;
         f[Tc] = L.rho * L.un * L.ut;
-        f[4] = (L.E + L.p) * L.un;
+        f[4] = (EL + L.p) * L.un;
         f[5] = L.a * L.un;
     } else if (fle(SL, T(0)) && fpos(SP)) {
         T ratio = ratioL;
-        T E_star = L.E + (SP - L.un) * (SP * L.rho + sw_div(L.p, SL - L.un));
+        T E_star = EL + (SP - L.un) * (SP * L.rho + sw_div(L.p, SL - L.un));
         f[0] = L.ar1 * L.un + SL * (L.ar1 * ratio - L.ar1);
         f[1] = L.ar2 * L.un + SL * (L.ar2 * ratio - L.ar2);
         f[N] = (L.rho * L.un * L.un + L.p) + SL * (L.rho * SP * ratio - L.rho * L.un);
         f[Tc] = (L.rho * L.un * L.ut) + SL * (L.rho * L.ut * ratio - L.rho * L.ut);
-        f[4] = (L.E + L.p) * L.un + SL * (E_star * ratio - L.E);
+        f[4] = (EL + L.p) * L.un + SL * (E_star * ratio - EL);
         f[5] = L.a * L.un + SL * (L.a * ratio - L.a);
     } else if (fle(SP, T(0)) && fle(T(0), SR)) {
         T ratio = ratioR;
-        T E_star = R.E + (SP - R.un) * (SP * R.rho + sw_div(R.p, SR - R.un));
+        T E_star = ER + (SP - R.un) * (SP * R.rho + sw_div(R.p, SR - R.un));
         f[0] = R.ar1 * R.un + SR * (R.ar1 * ratio - R.ar1);
         f[1] = R.ar2 * R.un + SR * (R.ar2 * ratio - R.ar2);
         f[N] = (R.rho * R.un * R.un + R.p) + SR * (R.rho * SP * ratio - R.rho * R.un);
         f[Tc] = (R.rho * R.un * R.ut) + SR * (R.rho * R.ut * ratio - R.rho * R.ut);
-        f[4] = (R.E + R.p) * R.un + SR * (E_star * ratio - R.E);
+        f[4] = (ER + R.p) * R.un + SR * (E_star * ratio - ER);
         f[5] = R.a * R.un + SR * (R.a * ratio - R.a);
     } else {
         f[0] = R.ar1 * R.un;
         f[1] = R.ar2 * R.un;
         f[N] = R.rho * R.un * R.un + R.p;
         f[Tc] = R.rho * R.un * R.ut;
-        f[4] = (R.E + R.p) * R.un;
+        f[4] = (ER + R.p) * R.un;
         f[5] = R.a * R.un;
     }
     T left_part = L.un + wmin(T(0), SL) * (ratioL - T(1));
