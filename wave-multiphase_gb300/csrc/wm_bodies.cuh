@@ -169,9 +169,8 @@ __device__ __forceinline__ bool floor_quotient_below(double x, double d, double 
     return x / d < c;
 }
 
-// sound_speed_r's value for the mixture (g, pi) the caller already holds: sqrt(max(g (p + pi) / rho,
-// 1e-20)) with 1/rho supplied, the same operations in the same order, the root refined from a
-// binary32 seed (sqrt_nr).
+// sound_speed_r's formula for the mixture (g, pi) the caller already holds: sqrt(max(g (p + pi) / rho,
+// 1e-20)) with 1/rho supplied, the root refined from a binary32 seed (sqrt_nr).
 __device__ __forceinline__ double sound_speed_gp(double g, double pi, double inv_rho, double p)
 {
     double val = g * (p + pi) * inv_rho;
@@ -204,7 +203,7 @@ __device__ __forceinline__ void prep_body(const Grid &g, const Eos &e, const Fie
     p.lv[kw] = v;
     p.lp[kw] = pl;
     p.la[kw] = a;
-    p.lc[kw] = sound_speed_gp(gg, pi, ir, pl);  // sound_speed_r(e, ir, pl, a): (gg, pi) is its mixture
+    p.lc[kw] = sound_speed_gp(gg, pi, ir, pl);  // the sound speed of the clamped cell's mixture
     p.lE[kw] = prim_to_energy(e, rho, u, v, pl, a);
 }
 
