@@ -678,6 +678,14 @@ __device__ __forceinline__ double mp5_diff(double c, double p1, double dm2, doub
     const double D = (-2.0 / 60.0) * dm2 + (11.0 / 60.0) * dm1 + (24.0 / 60.0) * d0 - (3.0 / 60.0) * d1;
     const double VOR = c + D;
     const double m = mm2(d0, mp5_alpha_times(dm1));
+    // The test D (D - m) >= eps cannot pass when D is +-0, or when D and m have the same sign bit
+    // and |m| > |D|: D - m is then nonzero with D's opposite sign, so the product is negative (a NaN
+    // or infinite m makes it NaN or negative). Settled on the integer pipe from the bits -- the
+    // same decision -- it skips the binary64 difference and product for nearly every smooth or
+    // flat stencil.
+    const long long bD = __double_as_longlong(D), bm = __double_as_longlong(m);
+    const long long aD = bD & 0x7fffffffffffffffLL, am = bm & 0x7fffffffffffffffLL;
+    if (aD == 0 || ((bD ^ bm) >= 0 && am > aD)) return VOR;
     if (!fge(D * (D - m), kEpsM)) return VOR;
     const double DJM1 = dm1 - dm2, DJ = d0 - dm1, DJP1 = d1 - d0;
     const double DM4JPH = mm4(4.0 * DJ - DJP1, 4.0 * DJP1 - DJ, DJ, DJP1);
