@@ -45,10 +45,11 @@ ALG_BYTES_PER_CELL_STAGE = 128.0     # read stage state + step-start state, writ
 SAMPLE_NX, SAMPLE_NY = 3584, 1536    # CPU sample: a quarter of the cells of the same problem
 # Face-sweep binary64 work per face (x or y) and traffic per cell-stage, from the ncu captures
 # summarised in profiles/ (None until measured).
-# 721: DFMA x 2 + DADD + DMUL measured by ncu (profiles/face_kernel_triple_point_2048x1024_fp64.md)
-# before HLLC formed one side's energy instead of two, which removes about 8 more per face (3 DFMA,
-# 2 DMUL by the source): the FLOP rate below reads at most about 1 % high.
-FP64_FLOP_PER_FACE = 721.0
+# Binary64 FLOP per face: 721 (DFMA x 2 + DADD + DMUL) measured by ncu
+# (profiles/face_kernel_triple_point_2048x1024_fp64.md) before two later changes that remove, by
+# the source, about 8 (HLLC forms one side's energy: 3 DFMA, 2 DMUL) and about 20 (MP5's limiter test
+# settled on the integer pipe: a DADD and a DMUL on nearly all ten evaluations of a face).
+FP64_FLOP_PER_FACE = 693.0
 DRAM_BYTES_PER_CELL_STAGE_FP32 = 1265.0
 DRAM_BYTES_PER_CELL_STAGE = 1673.0  # profiles/dram_traffic_triple_point_2048x1024.md
 
