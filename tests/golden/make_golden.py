@@ -20,7 +20,8 @@ How the reference is executed
   ``limit_fluxes``, ``rk3_update``, ``enforce_admissible``, ``update_prims``; ``get_dt`` after the
   third stage.
 
-Usage: ``python tests/golden/make_golden.py [--ref-dir DIR] [--only CASE ...]``
+Usage: ``python tests/golden/make_golden.py --ref-dir DIR [--only CASE ...]`` (or the environment
+variable ``WAVEMP_REFERENCE_DIR`` in place of ``--ref-dir``)
 """
 from __future__ import annotations
 
@@ -677,7 +678,9 @@ ALL_CASES = ("sc_ref_ic", "m10_ref_ic", "sc_cfg0", "sc_mp5c6_cfg0", "sc_mp5c6_ra
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-dir", default="/root/reference")
+    ap.add_argument("--ref-dir", default=os.environ.get("WAVEMP_REFERENCE_DIR"),
+                    required="WAVEMP_REFERENCE_DIR" not in os.environ,
+                    help="directory holding the reference's two scripts (or set WAVEMP_REFERENCE_DIR)")
     ap.add_argument("--out-dir", default=HERE)
     ap.add_argument("--only", nargs="*", default=None)
     args = ap.parse_args()
