@@ -334,14 +334,17 @@ int wm_profile_read(wm_handle *h, double ms[WM_PROF_GROUPS], long long launches[
 /* ---- no-allocation form (no counterpart in the reference) ------------------------------------
  * For callers that cannot allocate device memory -- e.g. a host application that serves all
  * device memory from its own pool and does not let libraries call cudaMalloc, or a loop that must
- * never wait on the allocator. Runs the same stage as wm_rhs_stage, without a handle: the
- * workspace is a device array inside the library, sized for grids of at most WM_STATIC_MAX_CELLS
- * padded cells, (nx + 2g) * (ny + 2g) <= 32768 (about 10.75 MiB, held by every GPU that loads the
- * library until the process exits). Larger grids are rejected with WM_ERR_INVALID and a message in
- * wm_last_error(). Calls no cudaMalloc or cudaFree. The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress); make that first call before any stream capture.
- * All calls on a device share the array and it keeps the last call's contents; calls that overlap
- * on the GPU (other streams or threads) race on it. */
+ * never wait on the allocator. Runs the same stage as wm_rhs_stage in the plain binary64 form
+ * (same kernels, same arithmetic, so the same bits), without a handle: the workspace is a device
+ * array inside the library, sized for grids of at most WM_STATIC_MAX_CELLS padded cells,
+ * (nx + 2g) * (ny + 2g) <= 32768 (about 10.75 MiB, held by every GPU that loads the library until
+ * the process exits). Larger grids, and the binary32 precision form (p->precision ==
+ * WM_PREC_FP32, whose workspace has another layout), are rejected with WM_ERR_INVALID and a
+ * message in wm_last_error(). Calls no cudaMalloc or cudaFree. The first call on a device (and the
+ * first after a cudaDeviceReset of it) looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture. All calls on a device
+ * share the array and it keeps the last call's contents; calls that overlap on the GPU (other
+ * streams or threads) race on it. */
 #define WM_STATIC_MAX_CELLS 32768
 int wm_rhs_stage_static(const wm_params *p, int nx, int ny, int g, const wm_fields *q,
                         const wm_fields *q_old, double dt, double alpha, double beta, void *stream);

@@ -123,3 +123,28 @@ def test_python_parameters_reject_unknown_values():
             SolverParams(dx=0.1, dy=0.1, **kw).to_c()
     with pytest.raises(ValueError):
         SolverParams(dx=0.1, dy=0.1, bc=("slip",) * 3).to_c()
+
+
+def test_static_stage_refuses_the_precision_form_and_large_grids(lib):
+    """wm_rhs_stage_static (the no-allocation stage) carries only the binary64 form's workspace:
+    a WM_PREC_FP32 parameter set, a grid above WM_STATIC_MAX_CELLS padded cells and invalid
+    parameters are refused with their own messages before any CUDA call (the field pointers below
+    are never read)."""
+    from wavemp import _lib
+
+    empty = _lib.WmFields()
+    p = params(precision="fp32")
+    assert lib.wm_rhs_stage_static(ctypes.byref(p), 16, 16, 5, ctypes.byref(empty), None,
+                                   1e-6, 0.0, 1.0, None) == WM_ERR_INVALID
+    assert b"binary64 form only" in lib.wm_last_error()
+    p = params()
+    assert lib.wm_rhs_stage_static(ctypes.byref(p), 200, 200, 5, ctypes.byref(empty), None,
+                                   1e-6, 0.0, 1.0, None) == WM_ERR_INVALID
+    assert b"exceeds the static scratch limit" in lib.wm_last_error()
+    for what, bad in bad_params():
+        assert lib.wm_rhs_stage_static(ctypes.byref(bad), 16, 16, 5, ctypes.byref(empty), None,
+                                       1e-6, 0.0, 1.0, None) == WM_ERR_INVALID, what
+        assert b"invalid parameters" in lib.wm_last_error(), what
+    assert lib.wm_rhs_stage_static(ctypes.byref(p), 16, 16, 5, ctypes.byref(empty), None,
+                                   1e-6, 0.0, 1.0, None) == WM_ERR_INVALID
+    assert b"invalid field pointers" in lib.wm_last_error()

@@ -11,6 +11,10 @@
 // The array is shared by every call on a device and keeps the previous call's contents. Nothing
 // in it needs to start at zero: each entry a stage reads is written earlier in the same stage.
 // Two calls that overlap on the GPU (different streams, or different host threads) race on it.
+// The stage is the plain binary64 form only (WM_PREC_FP64); a WM_PREC_FP32 parameter set is
+// refused with its own message.
+#include <cuda.h>  // CUcontext only; the two driver calls are reached through the runtime
+
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -34,11 +38,47 @@ constexpr size_t kScratchBytes = (size_t)kArrays * kArrayBytes;
 static __device__ __align__(256) unsigned char wm_stage_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
-void *g_scratch[kMaxDevices] = {nullptr};
+struct ScratchSlot {
+    unsigned long long ctx_id;  // unique id of the context the address belongs to (0: none yet)
+    void *addr;
+};
+ScratchSlot g_scratch[kMaxDevices] = {};
 std::mutex g_scratch_mutex;
 
+// The driver's cuCtxGetCurrent / cuCtxGetId, reached through the runtime (no link to libcuda).
+// A context id is unique for the life of the process: after cudaDeviceReset the device's new
+// primary context has a new id, its module (and so wm_stage_scratch) may sit at a new address,
+// and the address is looked up again.
+typedef int (*CtxGetCurrentFn)(CUcontext *);
+typedef int (*CtxGetIdFn)(CUcontext, unsigned long long *);
+
+unsigned long long current_context_id()
+{
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *a = nullptr, *b = nullptr;
+        cudaDriverEntryPointQueryResult qa = cudaDriverEntryPointSymbolNotFound, qb = qa;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) ==
+                cudaSuccess && qa == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) ==
+                cudaSuccess && qb == cudaDriverEntryPointSuccess) {
+            get_current = reinterpret_cast<CtxGetCurrentFn>(a);
+            get_id = reinterpret_cast<CtxGetIdFn>(b);
+        }
+    });
+    if (!get_current || !get_id) return 0;  // unknown: the caller looks the address up each call
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
+
 // Device address of wm_stage_scratch on the current device. The host-side name of the array is
-// only a stand-in for it, so the address is looked up once per device, with that device current.
+// only a stand-in for it, so the address is looked up with that device current: once per device
+// and context (again after a cudaDeviceReset), or on every call where the context id is not
+// available.
 int scratch_address(void **out)
 {
     int dev = 0;
@@ -48,7 +88,8 @@ int scratch_address(void **out)
         return WM_ERR_CUDA;
     }
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch[dev]) {
+    unsigned long long id = current_context_id();
+    if (id == 0 || g_scratch[dev].ctx_id != id || !g_scratch[dev].addr) {
         void *p = nullptr;
         err = cudaGetSymbolAddress(&p, wm_stage_scratch);
         if (err != cudaSuccess || !p) {
@@ -58,9 +99,13 @@ int scratch_address(void **out)
             set_error_text(msg);
             return WM_ERR_CUDA;
         }
-        g_scratch[dev] = p;
+        // the lookup makes the device's primary context current if it was not yet
+        g_scratch[dev].ctx_id = id ? id : current_context_id();
+        g_scratch[dev].addr = p;
+        *out = p;
+        return WM_OK;
     }
-    *out = g_scratch[dev];
+    *out = g_scratch[dev].addr;
     return WM_OK;
 }
 
@@ -71,7 +116,6 @@ bool params_ok(const wm_params *p, int nx, int ny, int g)
     if (!std::isfinite(p->pinf1) || !std::isfinite(p->pinf2) || !(p->cfl > 0.0)) return false;
     if (p->variant != WM_VARIANT_SC && p->variant != WM_VARIANT_M10) return false;
     if (p->recon != WM_RECON_SHIPPED && p->recon != WM_RECON_MP5C6) return false;
-    if (p->precision != WM_PREC_FP64) return false;
     for (int k = 0; k < 4; ++k)
         if (p->bc[k] != WM_BC_TRANSMISSIVE && p->bc[k] != WM_BC_SLIP) return false;
     return true;
@@ -101,7 +145,14 @@ extern "C" int wm_rhs_stage_static(const wm_params *p, int nx, int ny, int g, co
                                    const wm_fields *q_old, double dt, double alpha, double beta,
                                    void *stream)
 {
-    if (!params_ok(p, nx, ny, g)) {
+    if (p && p->precision == WM_PREC_FP32) {
+        // the precision form's workspace (binary32 copies of the state and fluxes) has a different
+        // layout; this entry point carries only the plain form's
+        set_error_text("wm_rhs_stage_static: the binary64 form only (precision must be WM_PREC_FP64); "
+                       "use wm_create + wm_rhs_stage for WM_PREC_FP32");
+        return WM_ERR_INVALID;
+    }
+    if (!params_ok(p, nx, ny, g) || p->precision != WM_PREC_FP64) {
         set_error_text("wm_rhs_stage_static: invalid parameters");
         return WM_ERR_INVALID;
     }
