@@ -19,7 +19,7 @@ Reported (one JSON line from rank 0):
   fp64         the face-sweep kernels' binary64 throughput against the device's measured FP64
                FMA peak (GB300's FP64 rate bounds the plain form, not HBM).
   cpu_baseline the CPU oracle (C restatement of the reference kernels, OpenMP on every host core)
-               on a bounded sample of the same workload.
+               on the same 7168 x 3072 grid, for a bounded number of steps (about 12 s).
 With --impl reference the script times that CPU implementation alone (the reference's own path is
 NVIDIA Warp, which is not installable here) and prints its line with "impl": "reference".
 """
@@ -42,7 +42,6 @@ for _p in (ROOT, os.path.join(ROOT, "wave-multiphase_gb300")):
 NX, NY, G = 7168, 3072, 5
 WORKLOAD = f"triple_point_{NX}x{NY}"
 ALG_BYTES_PER_CELL_STAGE = 128.0     # read stage state + step-start state, write new state (avg)
-SAMPLE_NX, SAMPLE_NY = 3584, 1536    # CPU sample: a quarter of the cells of the same problem
 # Face-sweep binary64 work per face (x or y) and traffic per cell-stage, from the ncu captures
 # summarised in profiles/ (None until measured).
 # Binary64 FLOP per face: 721 (DFMA x 2 + DADD + DMUL) measured by ncu
@@ -352,64 +351,40 @@ def batched_form(dev, steps, warmup, n=64, sensitivity_eps=0.0):
     return summary, shapes32
 
 
-def served_form(dev, nreq, shapes=None, capacity=16, chunk_steps=10):
+def served_form(dev, nreq, shapes=None, capacity=16, chunk_steps=10, budget_gb=150.0, tight_gb=2.0):
     """Serving form on the serving workload (Poisson arrivals at 20/s, seed 0, grids log-uniform
-    64x32 to 2048x1024, step counts U[50, 2000], binary32 form, 150 GB admission budget): p50/p99
-    latency (arrival to result on the host) and cell-stage/s, beside the same requests served one
-    at a time in arrival order by the plain binary64 per-solve path, whose service time is the
-    measured step time at each request's grid times its step count."""
+    64x32 to 2048x1024, step counts U[50, 2000], binary32 form): p50/p99 latency (arrival to result
+    on the host) and cell-stage/s with the 150 GB admission budget, again with a budget small enough
+    that memory rather than the slots limits admission, and -- measured on the same clock -- the same
+    requests served one at a time in arrival order by the plain binary64 per-solve path."""
     import torch
 
-    import wavemp
-    from wavemp.serve import Server, percentile, poisson_requests, serial_schedule
+    from wavemp.serve import Server, poisson_requests, serve_serial
 
+    out = {"workload": f"{nreq} requests, Poisson 20/s (seed 0), grids 64x32..2048x1024, "
+                       f"steps U[50,2000], binary32 form"}
+    for key, budget in (("served_fp32", budget_gb), ("served_fp32_budget_bound", tight_gb)):
+        reqs = poisson_requests(nreq, rate=20.0, seed=0, device=dev)
+        srv = Server(capacity=capacity, budget_bytes=budget * 1e9, precision="fp32",
+                     chunk_steps=chunk_steps, shapes=shapes, keep_results=False, device=dev)
+        res = srv.run(reqs)
+        res.update({"slots": capacity, "chunk_steps": chunk_steps, "budget_gb": budget,
+                    "peak_admitted_gb": round(srv.admission.peak_bytes / 1e9, 3), "launches": srv.launches,
+                    "rounds_waiting_for_slot": srv.admission.blocked_by_slots,
+                    "rounds_waiting_for_budget": srv.admission.blocked_by_budget})
+        srv.close()
+        torch.cuda.empty_cache()
+        out[key] = res
     reqs = poisson_requests(nreq, rate=20.0, seed=0, device=dev)
-    srv = Server(capacity=capacity, budget_bytes=150e9, precision="fp32", chunk_steps=chunk_steps,
-                 shapes=shapes, keep_results=False, device=dev)
-    served = srv.run(reqs)
-    served.update({"slots": capacity, "chunk_steps": chunk_steps, "budget_gb": 150.0,
-                   "peak_admitted_gb": round(srv.admission.peak_bytes / 1e9, 3), "launches": srv.launches})
-    srv.close()
+    serial = serve_serial(reqs, precision="fp64", device=dev)
+    serial["how"] = "measured: one request at a time through the per-solve plain binary64 path"
     torch.cuda.empty_cache()
-    stream = torch.cuda.current_stream()
-    per_step = {}
-    for r in reqs:
-        key = (r.spec.nx, r.spec.ny)
-        if key in per_step:
-            continue
-        sp = r.spec
-        p = wavemp.SolverParams(dx=sp.dx, dy=sp.dy, gamma1=sp.gamma1, pinf1=sp.pinf1, bc=sp.bc,
-                                recon="mp5c6", variant="sc", cfl=0.4)
-        s = wavemp.Solver(p, sp.nx, sp.ny, device=dev)
-        q = sp.make_state()
-        old = wavemp.alloc_state(sp.nx, sp.ny, names=wavemp.FIELDS, device=dev)
-        s.initialize(q)
-        s.init_dt(q)
-        for _ in range(2):
-            s.step(q, old, None, sync=False)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(5):
-            s.step(q, old, None, sync=False)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        per_step[key] = e0.elapsed_time(e1) / 5 * 1e-3
-        s.close()
-    arrivals = [r.arrival for r in reqs]
-    finish = serial_schedule(arrivals, [per_step[(r.spec.nx, r.spec.ny)] * r.spec.max_steps for r in reqs])
-    lat = [f - a for f, a in zip(finish, arrivals)]
-    work = sum(r.cell_stages for r in reqs)
-    serial = {"p50_s": round(percentile(lat, 50), 4), "p99_s": round(percentile(lat, 99), 4),
-              "makespan_s": round(max(finish) - min(arrivals), 4),
-              "value": round(work / (max(finish) - min(arrivals)) / 1e6, 3), "unit": "Mcell-stage/s",
-              "service_time": "measured plain binary64 step time at the request's grid x its steps"}
-    return {"workload": f"{nreq} requests, Poisson 20/s (seed 0), grids 64x32..2048x1024, "
-                        f"steps U[50,2000], binary32 form",
-            "served_fp32": served, "serial_plain_fp64": serial,
-            "speedup_vs_serial_plain": round(served["value"] / serial["value"], 3),
-            "p50_ratio_serial_over_served": round(serial["p50_s"] / served["p50_s"], 3),
-            "p99_ratio_serial_over_served": round(serial["p99_s"] / served["p99_s"], 3)}
+    served = out["served_fp32"]
+    out["serial_plain_fp64"] = serial
+    out["speedup_vs_serial_plain"] = round(served["value"] / serial["value"], 3)
+    out["p50_ratio_serial_over_served"] = round(serial["p50_s"] / served["p50_s"], 3)
+    out["p99_ratio_serial_over_served"] = round(serial["p99_s"] / served["p99_s"], 3)
+    return out
 
 
 def measured_peaks():
@@ -488,8 +463,10 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------------- CPU oracle -------
-def cpu_oracle_rate(nx, ny, steps=None, seconds=12.0):
-    """Mcell-stage/s of the CPU oracle (all host cores) on the same problem at nx x ny."""
+def cpu_oracle_rate(nx, ny, steps=None, seconds=12.0, warmup=1):
+    """Mcell-stage/s of the CPU oracle (all host cores) on the same problem at nx x ny: `warmup`
+    untimed steps (page-in, thread start), then `steps` timed steps, or as many as fit in
+    `seconds` when steps is None."""
     import numpy as np
 
     import wavemp
@@ -501,9 +478,11 @@ def cpu_oracle_rate(nx, ny, steps=None, seconds=12.0):
     o = orc.PackedOracle(nx, ny, P)
     for c, k in enumerate(orc.ALL10):
         o.fields[c][...] = st[k].numpy()
+    del st
     o.init_sequence()
     dt = o.get_dt()
-    dt = o.steps(1, dt)  # warm-up step (page-in, thread start)
+    for _ in range(max(warmup, 1)):
+        dt = o.steps(1, dt)
     done, t0 = 0, time.perf_counter()
     while True:
         dt = o.steps(1, dt)
@@ -516,6 +495,9 @@ def cpu_oracle_rate(nx, ny, steps=None, seconds=12.0):
 
 
 def run_reference(args):
+    """The reference arm: the CPU implementation of the path (the oracle, a C restatement of the
+    reference's kernels pinned bit-exact to their source) on the benchmark's own 7168 x 3072 grid,
+    every host core, W untimed then K timed SSP-RK3 steps."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
@@ -524,16 +506,15 @@ def run_reference(args):
     orc.build()
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    rate_w, _, _ = cpu_oracle_rate(SAMPLE_NX, SAMPLE_NY, steps=max(args.warmup, 1))
-    rate, steps, el = cpu_oracle_rate(SAMPLE_NX, SAMPLE_NY, steps=args.steps)
-    sample = (f"{SAMPLE_NX}x{SAMPLE_NY} cells of the same problem (a quarter of the cells), "
-              f"{steps} SSP-RK3 steps after {max(args.warmup, 1)} warm-up")
+    warm = max(args.warmup, 1)
+    rate, steps, el = cpu_oracle_rate(NX, NY, steps=args.steps, warmup=warm)
+    sample = f"the whole {NX}x{NY} grid, {steps} SSP-RK3 steps after {warm} warm-up"
     line = {
         "impl": "reference", "metric": "Mcell-stage/s", "value": round(rate, 3),
         "unit": "Mcell-stage/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(el / steps * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "sampled_as": f"{SAMPLE_NX}x{SAMPLE_NY}",
+        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY,
                    "scheme": "SC, MP5 + THINC + central-6", "form": "plain binary64",
                    "step": "one SSP-RK3 step (3 RHS stages)"},
         "cpu_baseline": {"value": round(rate, 3), "unit": "Mcell-stage/s", "cores": int(os.environ["OMP_NUM_THREADS"]),
@@ -727,11 +708,11 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-        rate, steps, el = cpu_oracle_rate(SAMPLE_NX, SAMPLE_NY, seconds=12.0)
+        rate, steps, el = cpu_oracle_rate(NX, NY, seconds=12.0)
         line["cpu_baseline"] = {"value": round(rate, 3), "unit": "Mcell-stage/s",
                                 "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
-                                "sample": f"{SAMPLE_NX}x{SAMPLE_NY} cells of the same problem, "
-                                          f"{steps} SSP-RK3 steps in {el:.1f} s"}
+                                "sample": f"the whole {NX}x{NY} grid, {steps} SSP-RK3 steps in "
+                                          f"{el:.1f} s after one warm-up step"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -224,6 +224,8 @@ typedef struct wm_batch_params {
     int tile_shape; /* -1: per grid-size class (wm_batch_tile_shape; 32-wide tiles by default),
                        0..3: every grid in tiles of 1x128, 2x64, 4x32 or 8x16 cells */
     int fp64_switches; /* as in wm_params */
+    long long spin_limit; /* waits (64 ns naps) a block spends at a grid barrier before the run gives
+                             up and sets the batch's error flag; <= 0: 2^26 (about 4 s) */
 } wm_batch_params;
 typedef struct wm_solve_desc {
     int nx, ny;
@@ -250,8 +252,12 @@ int wm_batch_clear(wm_batch *b, int slot);
 int wm_batch_init_dt(wm_batch *b, int slot, void *stream);
 int wm_batch_run(wm_batch *b, int nsteps, void *stream);
 /* Waits for the stream and copies every slot's status (capacity entries); WM_ERR_STATE if a grid
- * barrier of an earlier run timed out. */
+ * barrier of a run since the last query timed out. Such a run stopped its solves part-way through a
+ * phase; the query clears the flag and the barrier counters, so the batch runs again once the
+ * caller has put its solves back in a known state (e.g. restored their arrays and scalars). */
 int wm_batch_query(wm_batch *b, wm_solve_status *out, void *stream);
+/* Barrier wait limit of later runs (as wm_batch_params.spin_limit; <= 0: the default). */
+int wm_batch_spin_limit(wm_batch *b, long long limit);
 /* Tile shape (0..3) for the grids whose cell count has floor(log2(nx*ny)) == size_class. */
 int wm_batch_tile_shape(wm_batch *b, int size_class, int shape);
 /* Copy the per-slot scalars (dt accumulator, dt, t, steps, done; 40 bytes per slot) to (write=0)

@@ -152,3 +152,34 @@ def test_dt_record_and_replay():
                                           equal_nan=True)
             else:
                 compare(rep.slots[k]["q"], rec.slots[k]["q"], f"replayed fp32 slot {k}", "fp32")
+
+
+def test_barrier_timeout_is_reported_and_the_batch_runs_again():
+    """A grid-barrier wait that runs out stops the run without hanging: with a wait limit of one
+    nap, blocks that reach a barrier before the last one give up, set the batch's error flag and
+    return. status() then reports it (WM_ERR_STATE) once and clears it. With the default limit
+    back and the solves' arrays and scalars restored, the same batch gives the results of a batch
+    that never timed out, bit for bit."""
+    steps = 2
+    specs = [spec(nx, ny, max_steps=steps) for nx, ny in SIZES[:4]]
+    ref = Batch(len(specs))
+    for sp in specs:
+        ref.add(sp)
+    ref.run(steps)
+    ref.status()
+    b = Batch(len(specs), spin_limit=1)
+    for sp in specs:
+        b.add(sp)
+    snap = b._snapshot()
+    b.run(steps)
+    with pytest.raises(wavemp.WavempError, match="timed out"):
+        b.status()
+    b.status()  # reported once: the flag is clear now
+    b.set_spin_limit(0)
+    b._restore(snap)
+    b.run(steps)
+    st = b.status()
+    for k in range(len(specs)):
+        assert st[k]["done"] and st[k]["steps"] == steps
+        for name in wavemp.ALL:
+            assert torch.equal(b.slots[k]["q"][name], ref.slots[k]["q"][name]), (k, name)

@@ -36,7 +36,7 @@ constexpr int kThreads = 128;
 constexpr int kShapes = 4;
 constexpr int kShapeTI[kShapes] = {1, 2, 4, 8};  // tile rows (x) x columns (y) = 128 cells
 constexpr int kShapeTJ[kShapes] = {128, 64, 32, 16};
-constexpr unsigned long long kSpinLimit = 1ull << 26;
+constexpr unsigned long long kSpinLimit = 1ull << 26;  // default wait limit (about 4 s of 64 ns naps)
 constexpr int kPhaseSlots = 10;  // the 9 phases of a stage, then the end-of-step phase
 
 struct SolveDev {
@@ -75,6 +75,7 @@ struct BatchDev {
     int ntiles;
     unsigned *bar_count, *bar_gen;
     int *err;
+    const unsigned long long *spin_limit;  // waits a block may spin at a grid barrier before failing
     int repair;
     int sw64;                  // binary32 form: binary64 switches
     unsigned long long *prof;  // per-phase nanoseconds (block 0's view), or null
@@ -99,9 +100,10 @@ __device__ bool grid_barrier(const BatchDev &B)
             __threadfence();
             atomicAdd(B.bar_gen, 1u);
         } else {
+            const unsigned long long limit = *(volatile const unsigned long long *)B.spin_limit;
             unsigned long long spins = 0;
             while (*gen == g0) {
-                if (++spins > kSpinLimit) {
+                if (++spins > limit) {
                     atomicExch(B.err, 1);
                     break;
                 }
@@ -402,6 +404,7 @@ struct wm_batch {
     bool graph_ok = true;
     unsigned *bar_count = nullptr, *bar_gen = nullptr;
     int *err = nullptr;
+    unsigned long long *spin_limit = nullptr;  // in d_small's tail
     unsigned long long *prof = nullptr;  // kPhaseSlots counters in d_small's tail
     bool prof_on = false;
 };
@@ -483,6 +486,7 @@ int launch(wm_batch *b, int nsteps, cudaStream_t s)
     B.bar_count = b->bar_count;
     B.bar_gen = b->bar_gen;
     B.err = b->err;
+    B.spin_limit = b->spin_limit;
     B.repair = b->P.emergency_repair;
     B.sw64 = b->P.fp64_switches;
     B.prof = b->prof_on ? b->prof : nullptr;
@@ -540,7 +544,19 @@ int wm_batch_create(const wm_batch_params *p, int capacity, wm_batch **out)
     b->bar_count = reinterpret_cast<unsigned *>(tail);
     b->bar_gen = reinterpret_cast<unsigned *>(tail + 4);
     b->err = reinterpret_cast<int *>(tail + 8);
+    b->spin_limit = reinterpret_cast<unsigned long long *>(tail + 16);
     b->prof = reinterpret_cast<unsigned long long *>(tail + 64);  // kPhaseSlots x 8 bytes, within the 256
+    {
+        const unsigned long long limit = p->spin_limit > 0 ? (unsigned long long)p->spin_limit : kSpinLimit;
+        e = cudaMemcpy(b->spin_limit, &limit, sizeof limit, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            set_err("wm_batch_create", e);
+            cudaFree(b->d_small);
+            cudaFree(b->d_solves);
+            delete b;
+            return WM_ERR_CUDA;
+        }
+    }
     for (int s = 0; s < capacity; ++s) {
         slot_scalars(b, s, b->host[s]);
         b->host[s].done = nullptr;  // empty slot: no done flag, skipped by the kernel's step end
@@ -760,7 +776,14 @@ int wm_batch_query(wm_batch *b, wm_solve_status *out, void *stream)
     }
     int errflag = (int)(raw[(size_t)b->capacity * kSlotScalars + 1] & 0xffffffffu);
     if (errflag) {
-        set_error_text("wm_batch: a grid barrier timed out (not all blocks resident)");
+        // Report once, then clear the flag and the barrier counters (blocks that gave up left the
+        // arrival count part-way), so that the batch runs again once the caller has put its solves
+        // back in a known state: a run that timed out stopped its solves part-way through a phase.
+        e = cudaMemsetAsync(b->bar_count, 0, 12, s);  // count, generation, error flag
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        set_error_text(e == cudaSuccess
+                           ? "wm_batch: a grid barrier timed out; the solves stopped part-way (flag cleared)"
+                           : "wm_batch: a grid barrier timed out and the flag could not be cleared");
         return WM_ERR_STATE;
     }
     return WM_OK;
@@ -771,6 +794,18 @@ int wm_batch_tile_shape(wm_batch *b, int size_class_, int shape)
     if (!b || shape < 0 || shape >= kShapes || size_class_ < 0) return WM_ERR_INVALID;
     b->shape_of_class[size_class_] = shape;
     b->dirty = true;
+    return WM_OK;
+}
+
+int wm_batch_spin_limit(wm_batch *b, long long limit)
+{
+    if (!b) return WM_ERR_INVALID;
+    const unsigned long long v = limit > 0 ? (unsigned long long)limit : kSpinLimit;
+    cudaError_t e = cudaMemcpy(b->spin_limit, &v, sizeof v, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        set_err("wm_batch_spin_limit", e);
+        return WM_ERR_CUDA;
+    }
     return WM_OK;
 }
 

@@ -46,7 +46,8 @@ class WmSchedule(ctypes.Structure):
 class WmBatchParams(ctypes.Structure):
     _fields_ = [("variant", ctypes.c_int), ("recon", ctypes.c_int), ("precision", ctypes.c_int),
                 ("emergency_repair", ctypes.c_int), ("g", ctypes.c_int), ("cfl", ctypes.c_double),
-                ("tile_shape", ctypes.c_int), ("fp64_switches", ctypes.c_int)]
+                ("tile_shape", ctypes.c_int), ("fp64_switches", ctypes.c_int),
+                ("spin_limit", ctypes.c_longlong)]
 
 
 class WmSolveDesc(ctypes.Structure):
@@ -78,7 +79,7 @@ EXPORTS = ("wm_version", "wm_last_error", "wm_workspace_bytes", "wm_create", "wm
            "wm_batch_profile_read", "wm_schlieren", "wm_run", "wm_run_uses_graph",
            "wm_set_limiter_sweeps", "wm_batch_dt_log", "wm_verify_limiter_precheck",
            "wm_check_conversions", "wm_set_prechecks", "wm_verify_switch_precheck",
-           "wm_check_sweep_arith")
+           "wm_check_sweep_arith", "wm_batch_spin_limit")
 STATIC_MAX_CELLS = 32768
 PROF_GROUPS = ("bc", "prep", "faces", "limiter", "final")
 BATCH_PHASES = ("bc_x", "bc_y", "prep", "sensor", "faces", "theta0", "theta1", "theta2", "final",
@@ -139,6 +140,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.wm_batch_query.argtypes = [vp, ctypes.POINTER(WmSolveStatus), vp]
     L.wm_batch_tile_shape.argtypes = [vp, i, i]
     L.wm_batch_scalars.argtypes = [vp, vp, i, vp]
+    L.wm_batch_spin_limit.argtypes = [vp, ctypes.c_longlong]
     L.wm_batch_info.argtypes = [vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)]
     L.wm_batch_profile.argtypes = [vp, i]
     L.wm_schlieren.argtypes = [F, i, i, i, vp, vp, d, d, vp, vp, vp, vp]

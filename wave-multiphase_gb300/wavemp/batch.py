@@ -53,7 +53,8 @@ class SolveSpec:
 
 class Batch:
     def __init__(self, capacity: int, variant="sc", recon="mp5c6", precision="fp64",
-                 emergency_repair=True, cfl=0.4, g=5, tile_shape=-1, device=None, fp64_switches=False):
+                 emergency_repair=True, cfl=0.4, g=5, tile_shape=-1, device=None, fp64_switches=False,
+                 spin_limit: int = 0):
         self.L = _lib.load()
         self.g = g
         self.capacity = capacity
@@ -65,6 +66,7 @@ class Batch:
         p.precision, p.emergency_repair = _lib.PRECISION[precision], int(bool(emergency_repair))
         p.g, p.cfl, p.tile_shape = g, cfl, tile_shape
         p.fp64_switches = int(bool(fp64_switches))
+        p.spin_limit = int(spin_limit)  # grid-barrier wait limit (0: the library's default)
         self._p = p
         h = ctypes.c_void_p()
         _lib.check(self.L.wm_batch_create(ctypes.byref(p), capacity, ctypes.byref(h)), "wm_batch_create")
@@ -175,6 +177,12 @@ class Batch:
         _lib.check(self.L.wm_batch_profile_read(self._h, ctypes.byref(ms), int(reset), _stream()),
                    "wm_batch_profile_read")
         return dict(zip(_lib.BATCH_PHASES, list(ms)))
+
+    def set_spin_limit(self, limit: int = 0):
+        """Grid-barrier wait limit of later runs (0: the library's default). A run whose barrier
+        wait runs out stops part-way; the next status() raises WavempError (WM_ERR_STATE) and
+        clears the condition."""
+        _lib.check(self.L.wm_batch_spin_limit(self._h, int(limit)), "wm_batch_spin_limit")
 
     def set_shape(self, cls: int, shape: int):
         _lib.check(self.L.wm_batch_tile_shape(self._h, int(cls), int(shape)), "wm_batch_tile_shape")

@@ -23,8 +23,11 @@ is the same alone and in the mix.
 multiple of 8), step counts U[50, 2000], droplet and shock parameters drawn as in the batched
 workload (``batch.config3_solves``).
 
-``serial_schedule`` gives the latencies of the same requests served one at a time in arrival order
-from per-request service times, the comparison the serving measurement reports.
+``serve_serial`` serves the same requests one at a time in arrival order through the per-solve
+path (``Solver``, one solve on the device at a time, the plain binary64 form by default): the
+comparison the serving measurement reports, measured on the same clock as the served run.
+``serial_schedule`` gives those latencies from per-request service times instead (a model, for
+the host-side tests).
 """
 from __future__ import annotations
 
@@ -97,6 +100,15 @@ class Admission:
         self.in_use = 0
         self.bytes = 0
         self.peak_bytes = 0
+        self.blocked_by_slots = 0   # launch rounds in which the head of the queue waited for a slot
+        self.blocked_by_budget = 0  # ... had a free slot but waited for budget
+
+    def note_refusal(self, nbytes: int):
+        """Count why the head of the queue was not admitted (slots take precedence)."""
+        if self.in_use >= self.slots:
+            self.blocked_by_slots += 1
+        elif self.bytes + nbytes > self.budget:
+            self.blocked_by_budget += 1
 
     def fits_at_all(self, nbytes: int) -> bool:
         return nbytes <= self.budget
@@ -165,6 +177,7 @@ class Server:
             while waiting:
                 nbytes = self.batch.bytes_for(waiting[0].spec.nx, waiting[0].spec.ny)
                 if not self.admission.can_admit(nbytes):
+                    self.admission.note_refusal(nbytes)
                     break
                 r = waiting.popleft()
                 slot = self.batch.add(r.spec)
@@ -190,6 +203,47 @@ class Server:
                 self.admission.release(nbytes)
                 del entry
         return summarize(requests, busy)
+
+
+def serve_serial(requests, precision="fp64", keep_results=False, device=None, clock=time.perf_counter,
+                 sleep=time.sleep, variant="sc", recon="mp5c6", cfl=0.4) -> dict:
+    """Serve `requests` one at a time in arrival order through the per-solve path: for each, wait
+    for its arrival if the GPU is idle, allocate a Solver and its state, run the start-up sequence
+    and its step budget with the dt on the device, copy the ten cell arrays to host memory (the
+    request's latency ends there) and free the device memory. Returns the run's summary."""
+    import torch
+
+    from .params import SolverParams
+    from .solver import FIELDS, Solver, alloc_state
+
+    t0 = clock()
+    for r in sorted(requests, key=lambda r: r.arrival):
+        wait = r.arrival - (clock() - t0)
+        if wait > 0:
+            sleep(wait)
+        sp = r.spec
+        p = SolverParams(dx=sp.dx, dy=sp.dy, gamma1=sp.gamma1, pinf1=sp.pinf1, gamma2=sp.gamma2,
+                         pinf2=sp.pinf2, bc=tuple(sp.bc), variant=variant, recon=recon, cfl=cfl,
+                         precision=precision)
+        r.admitted = clock() - t0
+        s = Solver(p, sp.nx, sp.ny, device=device)
+        src = sp.state if sp.state is not None else sp.make_state()
+        q = alloc_state(sp.nx, sp.ny, device=s.device)
+        for k in q:
+            q[k].copy_(src[k])
+        old = alloc_state(sp.nx, sp.ny, device=s.device, names=FIELDS)
+        s.initialize(q)
+        s.init_dt(q)
+        for _ in range(sp.max_steps):
+            s.step(q, old, None, sync=False)
+        host = {k: v.to("cpu") for k, v in q.items()}  # blocking device->host copies
+        r.finished = clock() - t0
+        r.steps_done = sp.max_steps
+        r.result = host if keep_results else None
+        s.close()
+        del s, q, old, src
+    torch.cuda.synchronize()
+    return summarize(requests)
 
 
 def summarize(requests, busy_s=None) -> dict:
