@@ -173,7 +173,29 @@ __device__ __forceinline__ void bcy_cell(const SolveDev &S, bool save, int i, in
 
 // The limiter's blends are rebuilt in registers by the next pass and by the combine (CellFaces),
 // so a stage has no blend phases.
-enum Phase { PH_BCX, PH_BCY, PH_PREP, PH_SENSOR, PH_FACES, PH_THETA0, PH_THETA1, PH_THETA2, PH_FINAL };
+enum Phase { PH_BCX, PH_BCY, PH_PREP, PH_SENSOR, PH_FACES, PH_THETA0, PH_THETA1, PH_THETA2, PH_FINAL,
+             PH_BLEND0, PH_BLEND1, PH_BLEND2 };
+// The phases of a stage. Binary32: the limiter passes rebuild the earlier passes' blends in
+// registers and the combine all three (no blend phases: binary32 blends are cheap, the traffic is
+// what counts). Binary64: each pass is followed by the in-place blend of pp_blend_*_flux_kernel
+// (SC:1479-1548), so the passes and the combine read the blended fluxes as they are -- the
+// per-solve path's form, whose binary64 blend arithmetic is done once per face instead of again in
+// every later pass and in the combine.
+constexpr int kPhases32 = 9, kPhases64 = 12;
+template <int FP32> __device__ __forceinline__ int phase_at(int k)
+{
+    if (FP32 || k < 6) return k;  // BCX .. THETA0, then (binary32) THETA1, THETA2, FINAL
+    switch (k) {
+    case 6: return PH_BLEND0;
+    case 7: return PH_THETA1;
+    case 8: return PH_BLEND1;
+    case 9: return PH_THETA2;
+    case 10: return PH_BLEND2;
+    default: return PH_FINAL;
+    }
+}
+// profile slot of a phase: a blend's time counts with its limiter pass
+__device__ __forceinline__ int prof_slot(int ph) { return ph >= PH_BLEND0 ? PH_THETA0 + (ph - PH_BLEND0) : ph; }
 
 template <int VAR, int REC, int FP32>
 __device__ __forceinline__ void run_phase(const BatchDev &B, int phase, int stage)
@@ -244,14 +266,20 @@ __device__ __forceinline__ void run_phase(const BatchDev &B, int phase, int stag
                        : p == 1 ? theta_body<1, float, 1>(g, S.e, S.q, c, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta32, i, j)
                                 : theta_body<2, float, 2>(g, S.e, S.q, c, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta32, i, j);
                     S.theta32[p][kw_of(g, i, j)] = float(th);
-                } else {
+                } else {  // the earlier passes' blends are in place
                     const Cells32 none32{};
                     th = p == 0 ? theta_body<0, double, 0>(g, S.e, S.q, none32, S.fh, S.gh, S.fl, S.gl, dt, S.theta, i, j)
-                       : p == 1 ? theta_body<1, double, 1>(g, S.e, S.q, none32, S.fh, S.gh, S.fl, S.gl, dt, S.theta, i, j)
-                                : theta_body<2, double, 2>(g, S.e, S.q, none32, S.fh, S.gh, S.fl, S.gl, dt, S.theta, i, j);
+                       : p == 1 ? theta_body<1, double, 0>(g, S.e, S.q, none32, S.fh, S.gh, S.fl, S.gl, dt, S.theta, i, j)
+                                : theta_body<2, double, 0>(g, S.e, S.q, none32, S.fh, S.gh, S.fl, S.gl, dt, S.theta, i, j);
                     S.theta[p][kw_of(g, i, j)] = th;
                 }
             }
+            break;
+        case PH_BLEND0:
+        case PH_BLEND1:
+        case PH_BLEND2:  // binary64 only: the faces of cells g-1 .. g+n-1 (blend_kernel's range)
+            if (!FP32 && i >= g.g - 1 && i < g.g + g.nx && j >= g.g - 1 && j < g.g + g.ny)
+                blend_body<double>(g, S.fh, S.gh, S.fl, S.gl, S.theta[phase - PH_BLEND0], i, j);
             break;
         case PH_FINAL: {
             unsigned flags = FIN_RK3 | FIN_PRIM;
@@ -265,7 +293,7 @@ __device__ __forceinline__ void run_phase(const BatchDev &B, int phase, int stag
                 bits = final_body<float, 3>(g, S.e, flags, S.q, S.old, S.fh32, S.gh32, S.fl32, S.gl32, S.theta32,
                                             dt, nullptr, alpha, beta, none, i, j);
             else
-                bits = final_body<double, 3>(g, S.e, flags, S.q, S.old, S.fh, S.gh, S.fl, S.gl, S.theta, dt,
+                bits = final_body<double, 0>(g, S.e, flags, S.q, S.old, S.fh, S.gh, S.fl, S.gl, S.theta, dt,
                                              nullptr, alpha, beta, none, i, j);
             if (stage == 2) {  // every lane of the warp takes part (tiles are warp multiples)
                 for (int o = 16; o > 0; o >>= 1) {
@@ -280,12 +308,20 @@ __device__ __forceinline__ void run_phase(const BatchDev &B, int phase, int stag
     }
 }
 
-// Binary32 form: registers capped for 6 resident blocks per SM (a few dozen bytes of spills in the
-// face phase, 50 % more warps for the memory- and binary64-bound phases); binary64: uncapped.
+// Resident blocks per SM the persistent kernel is compiled for (its phases share one register
+// allocation, so every phase runs at this occupancy). Binary32 form: 8 (64 registers, a few dozen
+// bytes of spills in the face phase, more warps for the memory- and binary64-bound phases).
+// Binary64 form: 4 (128 registers, under 300 bytes of spills in the face phase). Measured on the 64
+// config-3 droplets with the in-place blend phases: 203 / 249 / 264 Mcell-stage/s at 2 (uncapped,
+// 196 registers) / 3 / 4 blocks, against 235 for the same solves run one after another.
 constexpr int kMinBlocksFp32 = 8;
+#ifndef WM_BATCH64_MIN_BLOCKS
+#define WM_BATCH64_MIN_BLOCKS 4
+#endif
+constexpr int kMinBlocksFp64 = WM_BATCH64_MIN_BLOCKS;
 
 template <int VAR, int REC, int FP32>
-__global__ void __launch_bounds__(kThreads, FP32 ? kMinBlocksFp32 : 1) batch_kernel(BatchDev B, int nsteps)
+__global__ void __launch_bounds__(kThreads, FP32 ? kMinBlocksFp32 : kMinBlocksFp64) batch_kernel(BatchDev B, int nsteps)
 {
     // Phase timing: a phase ends when the grid barrier after it opens, so block 0's clock between
     // successive barrier exits is the phase's duration across the whole grid.
@@ -293,12 +329,14 @@ __global__ void __launch_bounds__(kThreads, FP32 ? kMinBlocksFp32 : 1) batch_ker
     unsigned long long last = timing ? global_ns() : 0;
     for (int step = 0; step < nsteps; ++step) {
         for (int stage = 0; stage < 3; ++stage) {
-            for (int ph = PH_BCX; ph <= PH_FINAL; ++ph) {
+#pragma unroll 1
+            for (int k = 0; k < (FP32 ? kPhases32 : kPhases64); ++k) {
+                const int ph = phase_at<FP32>(k);
                 run_phase<VAR, REC, FP32>(B, ph, stage);
                 if (!grid_barrier(B)) return;
                 if (timing) {
                     const unsigned long long now = global_ns();
-                    B.prof[ph] += now - last;
+                    B.prof[prof_slot(ph)] += now - last;
                     last = now;
                 }
             }

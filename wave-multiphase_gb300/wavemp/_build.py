@@ -14,6 +14,8 @@ LIB = os.path.join(PKG_DIR, "libwavemp.so")
 SOURCES = ("wm_capi.cu", "wm_stage.cu", "wm_faces.cu", "wm_static.cu", "wm_batch.cu", "wm_post.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# extra nvcc flags for a build with other compile-time settings (e.g. "-DWM_BATCH64_MIN_BLOCKS=4")
+EXTRA = os.environ.get("WAVEMP_NVCC_EXTRA", "").split()
 
 
 def nvcc() -> str:
@@ -40,7 +42,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(src):
         obj = os.path.join(BUILD, src.replace(".cu", ".o"))
-        cmd = [cc, *ARCH, *FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [cc, *ARCH, *FLAGS, *EXTRA, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")

@@ -53,7 +53,7 @@ class SolveSpec:
 
 class Batch:
     def __init__(self, capacity: int, variant="sc", recon="mp5c6", precision="fp64",
-                 emergency_repair=True, cfl=0.4, g=5, tile_shape=-1, device=None, fp64_switches=False,
+                 emergency_repair=True, cfl=0.4, g=5, tile_shape=-1, device=None, fp64_switches=True,
                  spin_limit: int = 0):
         self.L = _lib.load()
         self.g = g

@@ -27,7 +27,11 @@ class SolverParams:
     bc: tuple = ("transmissive", "transmissive", "slip", "slip")  # x-lo, x-hi, y-lo, y-hi
     emergency_repair: bool = True
     precision: str = "fp64"
-    fp64_switches: bool = False  # precision form: THINC / Ducros switches from binary64 sensors
+    # precision form: the THINC / Ducros switch decisions from binary64 sensors (default). False
+    # takes them from binary32 sensors -- faster, but the THINC indicator's second differences of
+    # cell entropies (about 8e4 for air at 1 bar in SI units) then cancel below binary32's
+    # resolution, so round-off can move a switch in smooth flow.
+    fp64_switches: bool = True
 
     def to_c(self) -> _lib.WmParams:
         p = _lib.WmParams()
