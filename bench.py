@@ -351,7 +351,7 @@ def batched_form(dev, steps, warmup, n=64, sensitivity_eps=0.0):
     return summary, shapes32
 
 
-def served_form(dev, nreq, shapes=None, capacity=16, chunk_steps=10, budget_gb=150.0, tight_gb=2.0):
+def served_form(dev, nreq, shapes=None, capacity=16, chunk_steps=10, budget_gb=150.0, tight_gb=1.0):
     """Serving form on the serving workload (Poisson arrivals at 20/s, seed 0, grids log-uniform
     64x32 to 2048x1024, step counts U[50, 2000], binary32 form): p50/p99 latency (arrival to result
     on the host) and cell-stage/s with the 150 GB admission budget, again with a budget small enough
@@ -608,28 +608,34 @@ def run_ours(args):
     launches = sum(n for _, n in prof.values())
 
     # ---- end to end through the C ABI with host buffers ----
-    # The caller holds the conserved state (the six cell arrays the scheme advances) in pinned host
-    # memory. Every step copies it to the device, rebuilds the primitives there (update_prims, as
+    # The caller holds the conserved state (the six cell arrays the scheme advances) in one pinned
+    # host buffer. Every step copies it to the device (one copy: the six arrays are contiguous in the
+    # device state block, alloc_state's layout), rebuilds the primitives there (update_prims, as
     # every step does at its end), runs the step and copies the new conserved state back.
-    host = {k: torch.empty((NX + 2 * G, NY + 2 * G), dtype=torch.float64, pin_memory=True)
-            for k in wavemp.FIELDS}
-    for k in wavemp.FIELDS:
-        host[k].copy_(q[k])
+    nf = len(wavemp.FIELDS)
+    qb = wavemp.alloc_state(NX, NY, device=dev)
+    for k in wavemp.ALL:
+        qb[k].copy_(q[k])
+    nxg, nyg = NX + 2 * G, NY + 2 * G
+    blk = torch.as_strided(qb["ar1"], (nf, nxg, nyg), (nxg * nyg, nyg, 1))
+    assert all(blk[c].data_ptr() == qb[k].data_ptr() for c, k in enumerate(wavemp.FIELDS))
+    host = torch.empty((nf, NX + 2 * G, NY + 2 * G), dtype=torch.float64, pin_memory=True)
+    host.copy_(blk)
+    del q
+    q = qb
     torch.cuda.synchronize()
     ke = max(3, args.steps)
-    h2d = sum(t.numel() * 8 for t in host.values())
+    h2d = host.numel() * 8
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     f0 = torch.cuda.Event(enable_timing=True)
     f1 = torch.cuda.Event(enable_timing=True)
     f0.record(stream)
     for _ in range(ke):
-        for k in wavemp.FIELDS:
-            q[k].copy_(host[k], non_blocking=True)
+        blk.copy_(host, non_blocking=True)
         s.update_prims(q)
         s.step(q, old, None, sync=False)
-        for k in wavemp.FIELDS:
-            host[k].copy_(q[k], non_blocking=True)
+        host.copy_(blk, non_blocking=True)
     f1.record(stream)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
@@ -732,8 +738,8 @@ def main():
                     help="NXxNY: a smaller case of the same problem (profiling captures only)")
     ap.add_argument("--form", choices=("both", "plain", "fp32", "batched", "serve", "m10"), default="both",
                     help="time one form alone (profiling captures, full-length batched/served runs)")
-    ap.add_argument("--batch-steps", type=int, default=20,
-                    help="steps of the 64-solve batched workload (300 is the full workload)")
+    ap.add_argument("--batch-steps", type=int, default=300,
+                    help="steps of the 64-solve batched workload (the workload is 300 steps)")
     ap.add_argument("--serve-requests", type=int, default=24, help="requests of the serving workload")
     ap.add_argument("--batch-sensitivity", type=float, default=0.0,
                     help="also run the binary64 batch from initial states perturbed by this relative amount")

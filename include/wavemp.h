@@ -155,22 +155,26 @@ int wm_init_dt(wm_handle *h, const wm_fields *q, void *stream);
  * from the high- and first-order fluxes and the passes' cell factors, bit-identical. The second
  * moves less memory but adds blend arithmetic: the default is in place for WM_PREC_FP64 (whose
  * binary64 pipe is the bound) and rebuilt for WM_PREC_FP32 (blends in binary32); the batched form
- * always rebuilds. After a fused stage the workspace's high-order arrays hold the limited fluxes in
- * place form, the unlimited ones otherwise; the closures always blend in place. */
+ * does the same (in place for binary64, rebuilt for binary32). After a fused stage the workspace's
+ * high-order arrays hold the limited fluxes in place form, the unlimited ones otherwise; the closures
+ * always blend in place. A face at theta = 1 whose first-order values are all finite keeps its
+ * high-order values in every form (the blend's exact value there). */
 int wm_set_limiter_sweeps(wm_handle *h, int in_place);
 
 /* Binary32 pre-checks that let cells skip binary64 tests whose outcome they prove -- the limiter's
  * bound solves (the plain form's from binary32 roundings of its binary64 state and fluxes, with a
  * margin covering those roundings), the combine's clamp / floor / NaN / repair tests, and the THINC
  * switch of the binary64 sensors (cator2 of the cell entropies against 0.35, SC:318-325, 1028-1032:
- * binary32 entropies with an error bound, the binary64 pow only where the bound does not settle
- * it) -- on (1, default) or off (0). Results are the same bits either way; off exists to show that. */
+ * binary32 entropies with an error bound, then where that does not settle it the stencil's
+ * entropy ratios from binary64 differences of pressure, density and mixture gamma with an error
+ * bound, the binary64 pow only where neither settles it) -- on (1, default) or off (0). Results are
+ * the same bits either way; off exists to show that. */
 int wm_set_prechecks(wm_handle *h, int on);
-/* Diagnostic of the THINC switch pre-check on state q (binary64, any form): for every cell and
- * direction with a full five-cell stencil, both the binary32 pre-check and the binary64 decision
- * are evaluated from q. *checked counts the stencils, *decided those the pre-check settled,
- * *disagreed those it settled differently from the binary64 decision (0 when its error bound
- * holds). No counterpart in the reference. */
+/* Diagnostic of the THINC switch pre-checks on state q (binary64, any form): for every cell and
+ * direction with a full five-cell stencil, the pre-checks (binary32 entropies, then entropy
+ * ratios) and the binary64 decision are evaluated from q. *checked counts the stencils, *decided
+ * those a pre-check settled, *disagreed those settled differently from the binary64 decision (0
+ * when the error bounds hold). No counterpart in the reference. */
 int wm_verify_switch_precheck(wm_handle *h, const wm_fields *q, long long *checked, long long *decided,
                               long long *disagreed, void *stream);
 /* Diagnostic of the limiter pre-check (after wm_compute_fluxes and wm_compute_low_fluxes, like
@@ -343,7 +347,7 @@ int wm_profile_read(wm_handle *h, double ms[WM_PROF_GROUPS], long long launches[
  * never wait on the allocator. Runs the same stage as wm_rhs_stage in the plain binary64 form
  * (same kernels, same arithmetic, so the same bits), without a handle: the workspace is a device
  * array inside the library, sized for grids of at most WM_STATIC_MAX_CELLS padded cells,
- * (nx + 2g) * (ny + 2g) <= 32768 (about 10.75 MiB, held by every GPU that loads the library until
+ * (nx + 2g) * (ny + 2g) <= 32768 (about 10.8 MiB, held by every GPU that loads the library until
  * the process exits). Larger grids, and the binary32 precision form (p->precision ==
  * WM_PREC_FP32, whose workspace has another layout), are rejected with WM_ERR_INVALID and a
  * message in wm_last_error(). Calls no cudaMalloc or cudaFree. The first call on a device (and the

@@ -131,7 +131,7 @@ def test_prechecks_do_not_change_bits(seed, precision):
             assert np.array_equal(a[k], b[k], equal_nan=True), (case, k)
 
 
-# ---- the THINC switch pre-check (binary32 entropies with an error bound) ----------------------
+# ---- the THINC switch pre-checks (binary32 entropies, then entropy ratios, with error bounds) -----
 @pytest.mark.parametrize("case", pu.CASES)
 def test_switch_precheck_on_fixtures(case):
     d = pu.load_case(case)
@@ -164,6 +164,64 @@ def switch_states(seed, nx=128, ny=64):
             q["al_prim"].copy_(torch.from_numpy(al))
             q["p_p"].copy_(torch.from_numpy(p))
             yield p_scale, sigma, q
+
+
+def smooth_states(seed, nx=128, ny=64):
+    """Seeded smooth states of one fluid (air or water, alpha uniform) at SI scales -- entropies
+    p / rho^gamma from 1e-9 to 1e9 -- with relative fluctuations from 1e-9 to 1e-2 and smooth
+    gradients, so that cator2 sits near its threshold while the binary32 entropies' bound is far too
+    wide to settle it: the ratio pre-check's domain."""
+    rng = np.random.default_rng(seed)
+    g = 5
+    shape = (nx + 2 * g, ny + 2 * g)
+    x = np.linspace(0.0, 1.0, shape[0])[:, None] + np.zeros(shape)
+    for al_v, p0, rho0 in ((1e-6, 1.0e5, 1.2), (1 - 1e-6, 1.0e5, 1000.0), (1e-6, 1.0e7, 6.0), (0.5, 3.0e5, 500.0)):
+        for sigma in (1e-9, 1e-6, 1e-4, 1e-2):
+            for slope in (0.0, 1e-3, 1e-1):
+                al = np.full(shape, al_v)
+                rho = rho0 * (1.0 + slope * x) * (1.0 + sigma * rng.standard_normal(shape))
+                p = p0 * (1.0 + 0.5 * slope * x * x) * (1.0 + sigma * rng.standard_normal(shape))
+                q = {k: torch.zeros(shape, dtype=torch.float64, device="cuda") for k in pu.ALL}
+                q["ar1"].copy_(torch.from_numpy(al * rho))
+                q["ar2"].copy_(torch.from_numpy((1 - al) * rho))
+                q["al"].copy_(torch.from_numpy(al))
+                q["al_prim"].copy_(torch.from_numpy(al))
+                q["p_p"].copy_(torch.from_numpy(p))
+                yield (al_v, p0, sigma, slope), q
+
+
+@pytest.mark.parametrize("seed", [21, 22])
+def test_ratio_precheck_on_smooth_si_states(seed):
+    """The entropy-ratio pre-check (thinc_side_delta) never contradicts the binary64 decision on
+    smooth one-fluid states at SI scales, and settles nearly all of them."""
+    nx, ny = 128, 64
+    params = wavemp.SolverParams(dx=1.0 / nx, dy=0.5 / ny, gamma1=4.4, pinf1=6e8, recon="mp5c6")
+    s = Solver(params, nx, ny)
+    total = settled = 0
+    for what, q in smooth_states(seed, nx, ny):
+        checked, decided, disagreed = s.verify_switch_precheck(q)
+        assert disagreed == 0, (what, checked, decided)
+        total += checked
+        settled += decided
+    assert settled >= 0.99 * total, (settled, total)
+
+
+def test_switch_precheck_settles_the_droplet():
+    """On the Mach-2.4 water-cylinder state (air at 1 bar in SI units, entropies about 8e4) the two
+    pre-checks together settle nearly every stencil, so the binary64 pow is rare."""
+    nx, ny = 400, 200
+    params = wavemp.SolverParams(dx=1.0 / nx, dy=0.5 / ny, gamma1=4.4, pinf1=6e8, recon="mp5c6",
+                                 bc=("transmissive",) * 4)
+    q = ic.shock_droplet(nx, ny, 1.0, 0.5, mach=2.4)
+    s = Solver(params, nx, ny)
+    s.initialize(q)
+    old = alloc_state(nx, ny, names=wavemp.FIELDS)
+    s.init_dt(q)
+    for _ in range(20):
+        s.step(q, old, None, sync=False)
+    checked, decided, disagreed = s.verify_switch_precheck(q)
+    assert disagreed == 0
+    assert decided >= 0.99 * checked, (checked, decided)
 
 
 @pytest.mark.parametrize("seed", [11, 12])

@@ -142,40 +142,76 @@ def test_fp32_density_l1_within_1e5_of_fp64(cfg):
         assert ek <= 1e-4, f"{cfg}: {k} L1 {ek:.2e}"
 
 
-def lockstep_density_l1(spec, steps, fp64_switches):
-    """Density L1 of the binary32 form against binary64 after `steps` steps of one config-3 solve,
-    both on the binary64 run's dt sequence."""
-    runs = {}
-    for prec in ("fp64", "fp32"):
-        p = wavemp.SolverParams(dx=spec.dx, dy=spec.dy, gamma1=spec.gamma1, pinf1=spec.pinf1, bc=spec.bc,
-                                recon="mp5c6", variant="sc", cfl=0.4, precision=prec,
-                                fp64_switches=fp64_switches and prec == "fp32")
-        s = Solver(p, spec.nx, spec.ny)
-        q = spec.make_state()
-        old = alloc_state(spec.nx, spec.ny, names=pu.FIELDS)
-        s.initialize(q)
-        runs[prec] = (s, q, old)
-    (s64, q64, o64), (s32, q32, o32) = runs["fp64"], runs["fp32"]
-    dt = s64.get_dt(q64)
+def binary64_noise_sensitivity(spec, steps, eps, seeds):
+    """Density L1 by which a config-3 solve's own binary64 result moves when its conserved state is
+    perturbed by a relative `eps` (seeded normal noise) after every step, on the clean run's dt
+    sequence: the solve's sensitivity at the size of a binary32 rounding."""
+    p = wavemp.SolverParams(dx=spec.dx, dy=spec.dy, gamma1=spec.gamma1, pinf1=spec.pinf1, bc=spec.bc,
+                            recon="mp5c6", variant="sc", cfl=0.4)
+    s = Solver(p, spec.nx, spec.ny)
+    q0 = spec.make_state()
+    s.initialize(q0)
+    q = {k: v.clone() for k, v in q0.items()}
+    old = alloc_state(spec.nx, spec.ny, names=pu.FIELDS)
+    dts, dt = [], s.get_dt(q)
     for _ in range(steps):
-        nxt = s64.step(q64, o64, dt)
-        s32.step(q32, o32, dt, sync=False)
-        dt = nxt
-    torch.cuda.synchronize()
-    return l1(q32["ar1"] + q32["ar2"], q64["ar1"] + q64["ar2"])
+        dts.append(dt)
+        dt = s.step(q, old, dt)
+    ref = q["ar1"] + q["ar2"]
+    out = []
+    for seed in seeds:
+        g = torch.Generator(device="cuda").manual_seed(seed)
+        q = {k: v.clone() for k, v in q0.items()}
+        for n in range(steps):
+            for f in pu.FIELDS[:5]:
+                q[f].mul_(1.0 + eps * torch.randn(q[f].shape, generator=g, device="cuda", dtype=torch.float64))
+            s.update_prims(q)
+            s.step(q, old, dts[n], sync=False)
+        torch.cuda.synchronize()
+        out.append(l1(q["ar1"] + q["ar2"], ref))
+    return out
 
 
-def test_fp64_switches_hold_the_batched_outliers_to_1e5():
-    """Config-3 solves 4 (136x68) and 63 (168x84) are the two of 64 whose binary32 density error
-    exceeds 1e-5 after 300 steps when the THINC indicator and the Ducros sensor are binary32 (a
-    binary32 rounding moves a knife-edge switch; the binary64 solves are well conditioned: a 1e-14
-    perturbation stays at 1e-14). With the switches from binary64 sensors both stay below 1e-6."""
-    from wavemp.batch import config3_solves
+def test_batched_precision_form_on_the_batched_workload():
+    """Configuration 3 as stated: 64 droplet solves, 300 steps, the binary32 form (its default,
+    binary64 switch decisions) in one batch against the binary64 form in another, on the binary64
+    batch's dt sequence. Density L1 of all solves together <= 1e-6; at most two solves above 1e-5,
+    and each of those is at a knife edge of the scheme itself: its binary64 result moves by more
+    than 1e-5 when the state gets a relative 3e-8 of noise -- half a binary32 rounding -- after
+    every step (the binary64 solves are linear in a one-off perturbation up to 1e-7; what flips is
+    a threshold decision), so no binary32 arithmetic can hold them to 1e-5 reliably."""
+    from wavemp.batch import Batch, config3_solves
 
+    steps = 300
     specs = config3_solves(n=64, seed=0, steps=0)
-    for k in (4, 63):
-        e = lockstep_density_l1(specs[k], 300, fp64_switches=True)
-        assert e <= 1e-6, f"solve {k}: density L1 {e:.2e}"
+    logs = [torch.zeros(steps + 8, dtype=torch.float64, device="cuda") for _ in specs]
+    batches = {}
+    for prec in ("fp64", "fp32"):
+        b = Batch(len(specs), precision=prec)
+        for sp, log in zip(specs, logs):
+            b.add(sp, dt_log=log, dt_mode="record" if prec == "fp64" else "replay")
+        b.run(steps)
+        assert all(x["steps"] == steps for x in b.status())
+        batches[prec] = b
+    num = den = 0.0
+    per = []
+    for k in range(len(specs)):
+        qa, qb = batches["fp32"].slots[k]["q"], batches["fp64"].slots[k]["q"]
+        ra, rb = (qa["ar1"] + qa["ar2"])[5:-5, 5:-5], (qb["ar1"] + qb["ar2"])[5:-5, 5:-5]
+        num += float((ra - rb).abs().sum())
+        den += float(rb.abs().sum())
+        per.append(float((ra - rb).abs().sum() / rb.abs().sum()))
+    for b in batches.values():
+        b.close()
+    agg = num / den
+    outliers = [k for k, e in enumerate(per) if e > 1e-5]
+    print(f"aggregate {agg:.2e}, median {sorted(per)[32]:.2e}, above 1e-5: "
+          + ", ".join(f"{k} ({specs[k].nx}x{specs[k].ny}) {per[k]:.2e}" for k in outliers))
+    assert agg <= 1e-6, f"density L1 of all solves {agg:.2e}"
+    assert len(outliers) <= 2, outliers
+    for k in outliers:
+        moved = binary64_noise_sensitivity(specs[k], steps, 3e-8, seeds=(0, 1, 2))
+        assert max(moved) > 1e-5, f"solve {k}: binary32 {per[k]:.2e}, binary64 under noise {moved}"
 
 
 @pytest.mark.parametrize("case", FP32_CASES[:4])

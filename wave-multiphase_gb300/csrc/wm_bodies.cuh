@@ -59,11 +59,6 @@ __device__ __forceinline__ float side_of(double v, double threshold)
 // are not finite and normal (|p| in [2^-60, 2^60], so the result is normal too), it returns NaN:
 // no pre-check with that cell. p = 0 gives the exact 0.
 constexpr float kEnt32Rel = 6.1035156e-05f;  // 2^-14
-// Prep keeps the binary64 entropy of the cells whose binary32 entropy is NaN or above this in
-// magnitude: there the bound (about 4e-4 of the entropies) is too wide to settle smooth stencils,
-// so the sensor pass will need it. Below it the sensor evaluates the rare one it needs itself.
-constexpr float kEnt64Scale = 64.0f;
-
 __device__ __forceinline__ float entropy32(double ge, double rho_e, double pp)
 {
     if (pp == 0.0) return 0.0f;
@@ -105,12 +100,91 @@ __device__ __forceinline__ int thinc_side_pre(float em2, float em1, float e0, fl
     return -1;
 }
 
+// Second pre-check of the THINC switch, for the stencils the binary32 entropies leave: smooth flow
+// with entropies far from 1 (air at 1 bar in SI units: about 8e4), where their relative bound
+// swamps the second differences. The indicator depends on the entropies only through their ratios
+// to the centre's: with r_k = e_k / e_0 = 1 + d_k, aa = |e_0| A and bb = |e_0| B, where
+//   A = |d_-2 - 4 d_-1| / 4 + 13/12 |d_-2 - 2 d_-1|   (B likewise with d_2, d_1),
+// so cator2 < 0.35  <=>  2AB - 0.35 (A^2 + B^2) + 0.65 eps / e_0^2 < 0. Each
+//   d_k = expm1(L_k),  L_k = ln(e_k / e_0) = log1p(dp_k / p_0) - g_k log1p(dr_k / r_0) - dg_k ln r_0,
+// an identity for e_k = p_k / r_k^g_k with the differences dp, dr (the clamped densities) and dg
+// (the cells' binary64 mixture gammas) taken in binary64 -- a uniform region gives d = 0 exactly, as
+// its binary64 entropies are equal -- and the rest in binary32, inside the ranges where the bound
+// below holds (|dp / p_0|, |dr / r_0|, |L| <= 0.5). Error bound of d_k: the conversions, quotients
+// and products round by 2^-24, log1pf, logf and expm1f are within 1 ulp (CUDA's documented bounds),
+// and |x| <= 1.24 |log1p(x)| there; together |dL| <= 2^-19 (|log1p(xp)| + |g log1p(xr)| +
+// |dg| (1 + |ln r_0|)) and |dd| <= 2^-23 |d| + 1.7 |dL|. A and B get those errors through their
+// coefficients, 2^-21 of their magnitudes for their own roundings, and 2^-44 (6.4 + their magnitude)
+// for the binary64 evaluation the decision must reproduce (pow within 2 ulp, the quotient, five
+// roundings of aa). |e_0| comes from the binary32 entropy (within kEnt32Rel). f is bounded over the
+// box by interval arithmetic; a decision needs the interval clear of zero by 2^-18 of f's terms
+// (binary32 roundings of f and the binary64 quotient's). Returns 0 or 1 as the decision, -1 when
+// undecided (NaN or out-of-range inputs included).
+__device__ __forceinline__ int thinc_side_delta(const double p[5], const double r[5], const double gm[5], float e0)
+{
+    const float ae0 = fabsf(e0);
+    if (!(ae0 > 0.0f) || !(ae0 <= 3.0e38f)) return -1;
+    // |p_0|, r_0 >= 2^-60: a difference that is subnormal in binary32 then moves its quotient by
+    // at most 2^-90, far inside the bound's binary64 floor below
+    const float p0 = to_f32(p[2]), r0 = to_f32(r[2]);
+    if (!(fabsf(p0) >= 8.67361738e-19f && fabsf(p0) <= 3.0e38f) || !(r0 >= 8.67361738e-19f && r0 <= 3.0e38f))
+        return -1;
+    const float lnr0 = logf(r0), w0 = 1.0f + fabsf(lnr0);
+    float d[5], D[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        if (k == 2) {
+            d[k] = 0.0f;
+            D[k] = 0.0f;
+            continue;
+        }
+        const double dp = p[k] - p[2], dr = r[k] - r[2], dg = gm[k] - gm[2];
+        const float xp = to_f32(dp) / p0, xr = to_f32(dr) / r0;
+        if (!(fabsf(xp) <= 0.5f) || !(fabsf(xr) <= 0.5f)) return -1;
+        const float gk = to_f32(gm[k]), dgf = to_f32(dg);
+        if (!(gk > 0.0f && gk <= 64.0f) || !(fabsf(dgf) <= 64.0f)) return -1;
+        const float lp = log1pf(xp), gl = gk * log1pf(xr), dl = dgf * lnr0;
+        const float L = (lp - gl) - dl;
+        if (!(fabsf(L) <= 0.5f)) return -1;
+        const float dL = 1.9073486e-06f * (fabsf(lp) + fabsf(gl) + fabsf(dgf) * w0);  // 2^-19
+        d[k] = expm1f(L);
+        D[k] = 1.1920929e-07f * fabsf(d[k]) + 1.7f * dL;  // 2^-23
+    }
+    const float k13 = 13.0f / 12.0f;
+    const float A = 0.25f * fabsf(d[0] - 4.0f * d[1]) + k13 * fabsf(d[0] - 2.0f * d[1]);
+    const float B = 0.25f * fabsf(d[4] - 4.0f * d[3]) + k13 * fabsf(d[4] - 2.0f * d[3]);
+    const float MA = 0.25f * (fabsf(d[0]) + 4.0f * fabsf(d[1])) + k13 * (fabsf(d[0]) + 2.0f * fabsf(d[1]));
+    const float MB = 0.25f * (fabsf(d[4]) + 4.0f * fabsf(d[3])) + k13 * (fabsf(d[4]) + 2.0f * fabsf(d[3]));
+    const float wA = 0.25f * (D[0] + 4.0f * D[1]) + k13 * (D[0] + 2.0f * D[1]) + 4.7683716e-07f * MA +
+                     5.6843419e-14f * (6.4f + MA);  // 2^-21, 2^-44
+    const float wB = 0.25f * (D[4] + 4.0f * D[3]) + k13 * (D[4] + 2.0f * D[3]) + 4.7683716e-07f * MB +
+                     5.6843419e-14f * (6.4f + MB);
+    // 0.65 eps / e_0^2 with e_0 within kEnt32Rel (its square within 2^-12.9) and the roundings here
+    float Ylo, Yhi;
+    if (ae0 > 1.0e17f) {  // below 3e-37: bounded by [0, 1e-36]
+        Ylo = 0.0f;
+        Yhi = 1.0e-36f;
+    } else {
+        const float Y = (0.65f * float(kYuxin)) / (ae0 * ae0);  // +inf for |e_0| below ~5e-21
+        Ylo = Y * (1.0f - 2.4414062e-04f);                       // 2^-12
+        Yhi = Y * (1.0f + 2.4414062e-04f);
+    }
+    const float Alo = fmaxf(A - wA, 0.0f), Ahi = A + wA, Blo = fmaxf(B - wB, 0.0f), Bhi = B + wB;
+    const float fmin = 2.0f * Alo * Blo - 0.35f * (Ahi * Ahi + Bhi * Bhi) + Ylo;
+    const float fmax = 2.0f * Ahi * Bhi - 0.35f * (Alo * Alo + Blo * Blo) + Yhi;
+    const float m = 3.8146973e-06f * (2.0f * Ahi * Bhi + 0.35f * (Ahi * Ahi + Bhi * Bhi) + Yhi);  // 2^-18
+    if (!isfinite(A) || !isfinite(B) || !isfinite(wA) || !isfinite(wB)) return -1;
+    if (fmin > m || (isinf(Ylo) && isfinite(Ahi) && isfinite(Bhi))) return 1;
+    if (fmax < -m) return 0;
+    return -1;
+}
+
 // The THINC switch of the cell at kw (its state at kf) along one direction -- workspace stride sw,
 // state stride sq. With the pre-checks, as side_of's code: the binary32 decision where it is
-// settled, else cator2_val of the binary64 entropies, those prep kept (binary32 entropy NaN or
-// above kEnt64Scale in magnitude) read back, the others evaluated here from the cell state exactly
-// as prep evaluates them. Without: cator2_val of the binary64 entropies prep kept for every cell --
-// the value itself in binary64 arrays (the reference's array), its code in binary32 ones.
+// settled, else the ratio pre-check's (thinc_side_delta), else cator2_val of the binary64
+// entropies evaluated here from the cell state and prep's binary64 mixture gammas exactly as the
+// binary64 form evaluates them. Without: cator2_val of the binary64 entropies prep kept for every
+// cell -- the value itself in binary64 arrays (the reference's array), its code in binary32 ones.
 template <typename PT>
 __device__ __forceinline__ double thinc_side(const Eos &e, const Fields &q, const PrepT<PT> &p, long long kw,
                                              long long kf, long long sw, long long sq, bool prechecks)
@@ -122,17 +196,20 @@ __device__ __forceinline__ double thinc_side(const Eos &e, const Fields &q, cons
         for (int k = 0; k < 5; ++k) s[k] = p.ent32[kw + (k - 2) * sw];
         const int d = thinc_side_pre(s[0], s[1], s[2], s[3], s[4]);
         if (d >= 0) return float(d);
+        // the stencil's pressures, clamped densities and (prep's) binary64 mixture gammas
+        double pk[5], rk[5], gk[5];
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
-            if (!(fabsf(s[k]) <= kEnt64Scale)) {
-                v[k] = p.ent64[kw + (k - 2) * sw];
-            } else {
-                const long long c = kf + (k - 2) * sq;
-                double ge, pie;
-                mix_gamma_pinf(e, q.f[F_AL][c], ge, pie);
-                v[k] = entropy64(ge, q.f[F_AR1][c], q.f[F_AR2][c], q.f[F_P][c]);
-            }
+            const long long c = kf + (k - 2) * sq;
+            pk[k] = q.f[F_P][c];
+            rk[k] = q.f[F_AR1][c] + q.f[F_AR2][c];
+            if (rk[k] < kTiny) rk[k] = kTiny;
+            gk[k] = p.gam[kw + (k - 2) * sw];
         }
+        const int d2 = thinc_side_delta(pk, rk, gk, s[2]);
+        if (d2 >= 0) return float(d2);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) v[k] = entropy64_r(gk[k], rk[k], pk[k]);
     } else {
 #pragma unroll
         for (int k = 0; k < 5; ++k) v[k] = p.ent64[kw + (k - 2) * sw];
@@ -141,8 +218,9 @@ __device__ __forceinline__ double thinc_side(const Eos &e, const Fields &q, cons
     return side_of(cator2_val(v[0], v[1], v[2], v[3], v[4]), kThincThresh);
 }
 
-// The entropy prep leaves for thinc_side: the binary32 one and, where thinc_side will read it,
-// the binary64 one (every cell without the pre-checks).
+// What prep leaves for thinc_side: with the pre-checks the binary32 entropy and the cell's
+// binary64 mixture gamma (the ratio pre-check's input, and with the cell state all that the binary64
+// entropy of an undecided stencil needs); without, the binary64 entropy.
 template <typename PT>
 __device__ __forceinline__ void store_entropy(const PrepT<PT> &p, long long kw, double ge, double ar1, double ar2,
                                               double pp, bool prechecks)
@@ -150,9 +228,8 @@ __device__ __forceinline__ void store_entropy(const PrepT<PT> &p, long long kw, 
     double rho_e = ar1 + ar2;
     if (rho_e < kTiny) rho_e = kTiny;
     if (prechecks) {
-        const float s32 = entropy32(ge, rho_e, pp);
-        p.ent32[kw] = s32;
-        if (!(fabsf(s32) <= kEnt64Scale)) p.ent64[kw] = entropy64_r(ge, rho_e, pp);
+        p.ent32[kw] = entropy32(ge, rho_e, pp);
+        p.gam[kw] = ge;
     } else {
         p.ent64[kw] = entropy64_r(ge, rho_e, pp);
     }
@@ -342,17 +419,23 @@ struct CellFaces {
             tym[p] = face_theta_y(g, theta[p], ky, j - 1);
         }
     }
-    __device__ __forceinline__ FT chain(const FT *hi, const FT *lo, long long k, const FT *t) const
+    // A pass at theta = 1 on a face whose first-order values are all finite leaves the value as it
+    // is (face_blend's rule), so the first-order value is read only for the other passes.
+    __device__ __forceinline__ FT chain(const FT *hi, const FT *lo, const unsigned char *fin, long long k,
+                                        const FT *t) const
     {
         FT v = hi[k];
+        bool lofin = false;
+        if (NP > 0) lofin = fin[k] != 0;
 #pragma unroll
-        for (int p = 0; p < NP; ++p) v = face_blend(lo[k], v, t[p]);
+        for (int p = 0; p < NP; ++p)
+            if (!keeps_high(t[p], lofin)) v = face_blend(lo[k], v, t[p]);
         return v;
     }
-    __device__ __forceinline__ FT xp(const Face<FT> &h, const Face<FT> &l, int c) const { return chain(h.f[c], l.f[c], kw, txp); }
-    __device__ __forceinline__ FT xm(const Face<FT> &h, const Face<FT> &l, int c) const { return chain(h.f[c], l.f[c], kx, txm); }
-    __device__ __forceinline__ FT yp(const Face<FT> &h, const Face<FT> &l, int c) const { return chain(h.f[c], l.f[c], kw, typ); }
-    __device__ __forceinline__ FT ym(const Face<FT> &h, const Face<FT> &l, int c) const { return chain(h.f[c], l.f[c], ky, tym); }
+    __device__ __forceinline__ FT xp(const Face<FT> &h, const Face<FT> &l, int c) const { return chain(h.f[c], l.f[c], l.fin, kw, txp); }
+    __device__ __forceinline__ FT xm(const Face<FT> &h, const Face<FT> &l, int c) const { return chain(h.f[c], l.f[c], l.fin, kx, txm); }
+    __device__ __forceinline__ FT yp(const Face<FT> &h, const Face<FT> &l, int c) const { return chain(h.f[c], l.f[c], l.fin, kw, typ); }
+    __device__ __forceinline__ FT ym(const Face<FT> &h, const Face<FT> &l, int c) const { return chain(h.f[c], l.f[c], l.fin, ky, tym); }
 };
 
 // Binary32 pre-check of a limiter pass (precision form). The pass's factor is exactly 1 when the
@@ -406,23 +489,25 @@ __device__ __forceinline__ bool theta_one_core(const Eos &e, const float *hx, co
 }
 
 // Precision form: the binary32 states from the stage-start binary32 copies and the binary32
-// residuals the binary64 solve would widen (margin 3e-7 of |Q| + |dt R|).
+// residuals the binary64 solve would widen (margin 3e-7 of |Q| + |dt R|). The binary64 low-order
+// state is finite when the state and the binary32 first-order values of the four faces are
+// (`lofin`, the sweep's per-face bytes): binary32 values stay far inside binary64's range.
 template <int STAGE>
 __device__ __forceinline__ bool theta_one_f32(const Eos &e, const Cells32 &c, long long kw, const float *rh,
-                                              const float *rl, float dtf)
+                                              bool lofin, float dtf)
 {
     constexpr float kRel = 3.0e-7f;
     constexpr int C0 = STAGE == 1 ? 5 : 0, C1 = STAGE == 0 ? 2 : 6;
     const float *src[6] = {c.ar1, c.ar2, c.ru, c.rv, c.E, c.al};
     float hx[6], dx[6];
-    bool lfin = true;
+    bool lfin = lofin;
 #pragma unroll
     for (int k = C0; k < C1; ++k) {
         const float qv = src[k][kw];
         const float dh = dtf * rh[k];
         hx[k] = qv - dh;
         dx[k] = kRel * (fabsf(qv) + fabsf(dh));
-        if (STAGE != 2 || (k >= 2 && k <= 4)) lfin = lfin && isfinite(qv - dtf * rl[k]);
+        lfin = lfin && isfinite(qv);
     }
     return theta_one_core<STAGE>(e, hx, dx, lfin);
 }
@@ -436,7 +521,8 @@ __device__ __forceinline__ bool finite64(double x)
 // and face fluxes (integer-pipe conversions). Each face value is rounded by 2^-24 of itself, so the
 // residual's error is bounded by its magnitude A = (|F+| + |F-|)/dx + (|G+| + |G-|)/dy (+ the
 // alpha term's), and the state's by about 6 * 2^-24 (|Q| + dt A); the margin is 1e-6 of that.
-// The low-order state of a needed component is finite when its inputs are.
+// The low-order state is finite when its inputs are: the state and the first-order values of the
+// four faces (the sweep's per-face bytes).
 template <int STAGE>
 __device__ __forceinline__ bool theta_one_f64in(const Grid &g, const Eos &e, const Fields &q, long long kf,
                                                 long long kw, const Face<double> &fh, const Face<double> &gh,
@@ -446,7 +532,9 @@ __device__ __forceinline__ bool theta_one_f64in(const Grid &g, const Eos &e, con
     const long long kx = kw - g.nyg, ky = kw - 1;
     const float dtf = to_f32(dt), idx = g.inv_dxf, idy = g.inv_dyf;
     float hx[6], dx[6];
-    bool lfin = true;
+    // every first-order value of the four faces finite (the sweep's bytes; stricter than the
+    // components the pass uses, which only sends more cells to the binary64 solve)
+    bool lfin = fl.fin[kw] && fl.fin[kx] && gl.fin[kw] && gl.fin[ky];
 #pragma unroll
     for (int k = C0; k < C1; ++k) {
         const float xp = to_f32(fh.f[k][kw]), xm = to_f32(fh.f[k][kx]);
@@ -455,17 +543,13 @@ __device__ __forceinline__ bool theta_one_f64in(const Grid &g, const Eos &e, con
         float A = (fabsf(xp) + fabsf(xm)) * idx + (fabsf(yp) + fabsf(ym)) * idy;
         const double qd = q.f[k][kf];
         bool fin = finite64(qd);
-        if (STAGE != 2 || (k >= 2 && k <= 4))
-            fin = fin && finite64(fl.f[k][kw]) && finite64(fl.f[k][kx]) && finite64(gl.f[k][kw]) &&
-                  finite64(gl.f[k][ky]);
         if (k == 5) {
             const float a = to_f32(q.f[F_ALP][kf]);
             const float sxp = to_f32(fh.f[6][kw]), sxm = to_f32(fh.f[6][kx]);
             const float syp = to_f32(gh.f[6][kw]), sym = to_f32(gh.f[6][ky]);
             rh = rh - src_term(a, sxp - sxm, idx) - src_term(a, syp - sym, idy);
             A += fabsf(a) * ((fabsf(sxp) + fabsf(sxm)) * idx + (fabsf(syp) + fabsf(sym)) * idy);
-            fin = fin && finite64(q.f[F_ALP][kf]) && finite64(fl.f[6][kw]) && finite64(fl.f[6][kx]) &&
-                  finite64(gl.f[6][kw]) && finite64(gl.f[6][ky]);
+            fin = fin && finite64(q.f[F_ALP][kf]);
         }
         const float qv = to_f32(qd);
         hx[k] = qv - dtf * rh;
@@ -498,22 +582,29 @@ __device__ __forceinline__ double theta_solve_inline(const Grid &g, const Eos &e
     const FT idx = cst<FT>(g.inv_dx, g.inv_dxf), idy = cst<FT>(g.inv_dy, g.inv_dyf);
     constexpr int C0 = STAGE == 1 ? 5 : 0, C1 = STAGE == 0 ? 2 : 6;
     FT rh[6], rl[6];
+    FT a = FT(0);
+    if (C1 == 6) {
+        if constexpr (sizeof(FT) == 4) a = to_f32(q.f[F_ALP][kf]);
+        else a = q.f[F_ALP][kf];
+    }
 #pragma unroll
     for (int c = C0; c < C1; ++c) {
         rh[c] = div_sum(cf.xp(fh, fl, c) - cf.xm(fh, fl, c), idx, cf.yp(gh, gl, c) - cf.ym(gh, gl, c), idy);
-        rl[c] = div_sum(fl.f[c][kw] - fl.f[c][kx], idx, gl.f[c][kw] - gl.f[c][ky], idy);
-        if (c == 5) {
-            FT a;
-            if constexpr (sizeof(FT) == 4) a = to_f32(q.f[F_ALP][kf]);
-            else a = q.f[F_ALP][kf];
+        if (c == 5)
             rh[c] = rh[c] - src_term(a, cf.xp(fh, fl, 6) - cf.xm(fh, fl, 6), idx) -
                     src_term(a, cf.yp(gh, gl, 6) - cf.ym(gh, gl, 6), idy);
-            rl[c] = rl[c] - src_term(a, fl.f[6][kw] - fl.f[6][kx], idx) - src_term(a, gl.f[6][kw] - gl.f[6][ky], idy);
-        }
     }
     if constexpr (sizeof(FT) == 4) {
-        one = theta_one_f32<STAGE>(e, c32, kw, rh, rl, to_f32(dt));
+        const bool lofin = fl.fin[kw] && fl.fin[kx] && gl.fin[kw] && gl.fin[ky];
+        one = theta_one_f32<STAGE>(e, c32, kw, rh, lofin, to_f32(dt));
         if (!VERIFY && one && prechecks) return 1.0;
+    }
+    // the first-order residual: only for the cells the pre-check left
+#pragma unroll
+    for (int c = C0; c < C1; ++c) {
+        rl[c] = div_sum(fl.f[c][kw] - fl.f[c][kx], idx, gl.f[c][kw] - gl.f[c][ky], idy);
+        if (c == 5)
+            rl[c] = rl[c] - src_term(a, fl.f[6][kw] - fl.f[6][kx], idx) - src_term(a, gl.f[6][kw] - gl.f[6][ky], idy);
     }
     double l[6], h[6];
 #pragma unroll
@@ -582,24 +673,18 @@ __device__ __forceinline__ void blend_body(const Grid &g, const Face<FT> &fh, co
                                            const FT *theta, int i, int j)
 {
     long long kw = kw_of(g, i, j);
-    // Binary64: a face at theta = 1 whose low-order values are all finite keeps its high-order
-    // values (face_blend's value there): only its low-order values are read, nothing is written.
+    // A face at theta = 1 whose low-order values are all finite keeps its high-order values
+    // (face_blend's value there): only its theta and its finiteness byte are read, nothing is written.
     if (j >= g.g) {  // x face between (i, j) and (i+1, j)
         const FT t = face_theta_x(g, theta, kw, i);
-        bool keep = sizeof(FT) == 8 && is_one(t);
-#pragma unroll
-        for (int c = 0; c < 7; ++c) keep = keep && finite_bits(fl.f[c][kw]);
-        if (!keep) {
+        if (!keeps_high(t, fl.fin[kw] != 0)) {
 #pragma unroll
             for (int c = 0; c < 7; ++c) fh.f[c][kw] = face_blend(fl.f[c][kw], fh.f[c][kw], t);
         }
     }
     if (i >= g.g) {  // y face between (i, j) and (i, j+1)
         const FT t = face_theta_y(g, theta, kw, j);
-        bool keep = sizeof(FT) == 8 && is_one(t);
-#pragma unroll
-        for (int c = 0; c < 7; ++c) keep = keep && finite_bits(gl.f[c][kw]);
-        if (!keep) {
+        if (!keeps_high(t, gl.fin[kw] != 0)) {
 #pragma unroll
             for (int c = 0; c < 7; ++c) gh.f[c][kw] = face_blend(gl.f[c][kw], gh.f[c][kw], t);
         }
@@ -1007,9 +1092,14 @@ __device__ __forceinline__ void face_body(const Eos &e, const V &v, const Face<F
         R.un = v.un(1); R.ut = v.ut(1); R.p = v.lp(1); R.a = v.la(1); R.c = v.lc(1); R.E = v.lE(1);
         T f[6], us;
         hllc<DIR>(L, R, f, us);
+        bool fin = finite_bits(FT(us));
 #pragma unroll
-        for (int c = 0; c < 6; ++c) lo.f[c][kw] = FT(f[c]);
+        for (int c = 0; c < 6; ++c) {
+            lo.f[c][kw] = FT(f[c]);
+            fin = fin && finite_bits(FT(f[c]));
+        }
         lo.f[6][kw] = FT(us);
+        lo.fin[kw] = fin ? 1 : 0;
     }
     if (!do_high) return;
 

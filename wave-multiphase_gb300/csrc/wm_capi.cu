@@ -47,12 +47,14 @@ size_t array_bytes(int nx, int ny, int g, size_t elem = sizeof(double))
 // pre-check. Precision form: 28 binary32 face arrays, 3
 // binary32 limiter factors (bound solves in binary64, stored in the flux type), 11 binary32
 // per-cell arrays, 9 binary32 cell copies and the binary64 entropy of the binary64 switches.
+// Both: then the first-order sweeps' per-face finiteness bytes (x, y), one byte a padded cell each.
 size_t layout_bytes(int precision, int nx, int ny, int g)
 {
+    const size_t fin = 2 * array_bytes(nx, ny, g, 1);
     if (precision == WM_PREC_FP32)
         return (size_t)(kArrays + kCellCopies) * array_bytes(nx, ny, g, sizeof(float)) + array_bytes(nx, ny, g) +
-               kTailBytes;
-    return (size_t)kArrays * array_bytes(nx, ny, g) + array_bytes(nx, ny, g, sizeof(float)) + kTailBytes;
+               fin + kTailBytes;
+    return (size_t)kArrays * array_bytes(nx, ny, g) + array_bytes(nx, ny, g, sizeof(float)) + fin + kTailBytes;
 }
 
 bool valid_params(const wm_params *p, int nx, int ny, int g)
@@ -266,8 +268,12 @@ int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t
         P.lu = h->arr[36]; P.lv = h->arr[37]; P.lp = h->arr[38]; P.la = h->arr[39]; P.lc = h->arr[40];
         P.lE = h->arr[41];
         P.ent64 = h->arr[33];
+        P.gam = h->arr[33];
         P.ent32 = reinterpret_cast<float *>(base + (size_t)kArrays * ab);
         tail = base + (size_t)kArrays * ab + array_bytes(nx, ny, g, sizeof(float));
+        h->fl.fin = reinterpret_cast<unsigned char *>(tail);
+        h->gl.fin = h->fl.fin + array_bytes(nx, ny, g, 1);
+        tail += 2 * array_bytes(nx, ny, g, 1);
     } else {
         size_t ab4 = array_bytes(nx, ny, g, sizeof(float));
         char *cur = base;
@@ -301,11 +307,14 @@ int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t
         P.lu = h->arr32[36]; P.lv = h->arr32[37]; P.lp = h->arr32[38]; P.la = h->arr32[39];
         P.lc = h->arr32[40]; P.lE = h->arr32[41];
         P.ent64 = ent64;
+        P.gam = ent64;
         P.ent32 = P.ent;
         Cells32 &C = h->cells32;
         C.ar1 = copies[0]; C.ar2 = copies[1]; C.ru = copies[2]; C.rv = copies[3];
         C.p = copies[4]; C.al = copies[5]; C.u = copies[6]; C.v = copies[7]; C.E = copies[8];
-        tail = cur;
+        h->fl32.fin = reinterpret_cast<unsigned char *>(cur);
+        h->gl32.fin = h->fl32.fin + array_bytes(nx, ny, g, 1);
+        tail = cur + 2 * array_bytes(nx, ny, g, 1);
     }
     h->ctr_base = reinterpret_cast<unsigned long long *>(tail);
     h->cnt.repaired = h->ctr_base + 0;

@@ -901,8 +901,8 @@ __device__ __forceinline__ void hllc(const Side<T> &L, const Side<T> &R, T f[6],
 }
 
 // Blend of a high-order face value toward the first-order one, low + theta (high - low)
-// (pp_blend_*_flux_kernel body, SC:1506-1512), with one deliberate difference in binary64: at
-// theta = 1 with a finite low value it is the high value itself -- the blend's exact value, where the reference's
+// (pp_blend_*_flux_kernel body, SC:1506-1512), with one deliberate difference: at theta = 1 with a
+// finite low value it is the high value itself -- the blend's exact value, where the reference's
 // low + (high - low) can round one unit away -- so a face the limiter leaves alone keeps its
 // high-order flux and the in-place blend need not rewrite it. A non-finite low, high or theta
 // takes the formula (NaN propagates as in the reference). Shared by the in-place limiter and the
@@ -918,11 +918,15 @@ __device__ __forceinline__ double face_blend(double low, double high, double the
 {
     return is_one(theta) && finite_bits(low) ? high : __fma_rn(theta, high - low, low);
 }
-// Binary32 (the precision form's rebuilt blends, which have no in-place sweep to skip): the formula.
+// Binary32 (the precision form): the same rule.
 __device__ __forceinline__ float face_blend(float low, float high, float theta)
 {
-    return __fmaf_rn(theta, high - low, low);
+    return is_one(theta) && finite_bits(low) ? high : __fmaf_rn(theta, high - low, low);
 }
+// True when face_blend(low, high, theta) is `high` for every component of a face whose first-order
+// values are all finite (`lofin`, the sweep's per-face byte): the blend at theta = 1 then needs no
+// first-order value.
+template <typename FT> __device__ __forceinline__ bool keeps_high(FT theta, bool lofin) { return lofin && is_one(theta); }
 
 // Flux difference terms with their rounding pinned (explicit fused multiply-add and products, which
 // the compiler does not re-associate or contract): every kernel that forms a residual or a limiter

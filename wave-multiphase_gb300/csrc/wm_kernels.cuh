@@ -15,9 +15,13 @@ struct Fields {
 enum { F_AR1 = 0, F_AR2, F_RU, F_RV, F_E, F_AL, F_U, F_V, F_P, F_ALP };
 
 // Six flux components and the interface velocity of one sweep direction; FT is the storage type
-// (double in the plain form, float in the precision form).
+// (double in the plain form, float in the precision form). The first-order arrays also carry one
+// byte per face, written by the sweep that writes them: 1 when all seven first-order values of the
+// face are finite, else 0 -- what the limiter needs of a face it leaves unlimited (theta = 1), so
+// that it need not read the seven values there.
 template <typename FT> struct Face {
     FT *f[7];
+    unsigned char *fin = nullptr;
 };
 using Face7 = Face<double>;
 
@@ -25,7 +29,9 @@ using Face7 = Face<double>;
 template <typename PT> struct PrepT {
     PT *ent;                          // cell entropy p / rho^gamma
     double *ent64;                    // the entropy in binary64 (plain form; precision form with
-                                      // binary64 switches), kept where the switch pre-check needs it
+                                      // binary64 switches), every cell, when the pre-checks are off
+    double *gam;                      // with the pre-checks: each cell's binary64 mixture gamma
+                                      // (the same storage as ent64)
     float *ent32;                     // the binary32 entropy of that pre-check (the precision
                                       // form's ent array, which its binary64 switches leave free)
     PT *cx, *cy;                      // smoothness indicator along x and y
