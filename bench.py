@@ -740,7 +740,7 @@ def main():
                     help="time one form alone (profiling captures, full-length batched/served runs)")
     ap.add_argument("--batch-steps", type=int, default=300,
                     help="steps of the 64-solve batched workload (the workload is 300 steps)")
-    ap.add_argument("--serve-requests", type=int, default=24, help="requests of the serving workload")
+    ap.add_argument("--serve-requests", type=int, default=48, help="requests of the serving workload")
     ap.add_argument("--batch-sensitivity", type=float, default=0.0,
                     help="also run the binary64 batch from initial states perturbed by this relative amount")
     ap.add_argument("--m10-steps", type=int, default=500, help="steps of the Mach-10 precision run")

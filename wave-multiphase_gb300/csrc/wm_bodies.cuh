@@ -419,14 +419,15 @@ struct CellFaces {
             tym[p] = face_theta_y(g, theta[p], ky, j - 1);
         }
     }
-    // A pass at theta = 1 on a face whose first-order values are all finite leaves the value as it
-    // is (face_blend's rule), so the first-order value is read only for the other passes.
+    // Binary64: a pass at theta = 1 on a face whose first-order values are all finite leaves the
+    // value as it is (face_blend's rule), so the first-order value is read only for the other
+    // passes. Binary32: every pass blends (face_blend's formula).
     __device__ __forceinline__ FT chain(const FT *hi, const FT *lo, const unsigned char *fin, long long k,
                                         const FT *t) const
     {
         FT v = hi[k];
         bool lofin = false;
-        if (NP > 0) lofin = fin[k] != 0;
+        if (NP > 0 && sizeof(FT) == 8) lofin = fin[k] != 0;
 #pragma unroll
         for (int p = 0; p < NP; ++p)
             if (!keeps_high(t[p], lofin)) v = face_blend(lo[k], v, t[p]);
@@ -489,25 +490,23 @@ __device__ __forceinline__ bool theta_one_core(const Eos &e, const float *hx, co
 }
 
 // Precision form: the binary32 states from the stage-start binary32 copies and the binary32
-// residuals the binary64 solve would widen (margin 3e-7 of |Q| + |dt R|). The binary64 low-order
-// state is finite when the state and the binary32 first-order values of the four faces are
-// (`lofin`, the sweep's per-face bytes): binary32 values stay far inside binary64's range.
+// residuals the binary64 solve would widen (margin 3e-7 of |Q| + |dt R|).
 template <int STAGE>
 __device__ __forceinline__ bool theta_one_f32(const Eos &e, const Cells32 &c, long long kw, const float *rh,
-                                              bool lofin, float dtf)
+                                              const float *rl, float dtf)
 {
     constexpr float kRel = 3.0e-7f;
     constexpr int C0 = STAGE == 1 ? 5 : 0, C1 = STAGE == 0 ? 2 : 6;
     const float *src[6] = {c.ar1, c.ar2, c.ru, c.rv, c.E, c.al};
     float hx[6], dx[6];
-    bool lfin = lofin;
+    bool lfin = true;
 #pragma unroll
     for (int k = C0; k < C1; ++k) {
         const float qv = src[k][kw];
         const float dh = dtf * rh[k];
         hx[k] = qv - dh;
         dx[k] = kRel * (fabsf(qv) + fabsf(dh));
-        lfin = lfin && isfinite(qv);
+        if (STAGE != 2 || (k >= 2 && k <= 4)) lfin = lfin && isfinite(qv - dtf * rl[k]);
     }
     return theta_one_core<STAGE>(e, hx, dx, lfin);
 }
@@ -582,29 +581,22 @@ __device__ __forceinline__ double theta_solve_inline(const Grid &g, const Eos &e
     const FT idx = cst<FT>(g.inv_dx, g.inv_dxf), idy = cst<FT>(g.inv_dy, g.inv_dyf);
     constexpr int C0 = STAGE == 1 ? 5 : 0, C1 = STAGE == 0 ? 2 : 6;
     FT rh[6], rl[6];
-    FT a = FT(0);
-    if (C1 == 6) {
-        if constexpr (sizeof(FT) == 4) a = to_f32(q.f[F_ALP][kf]);
-        else a = q.f[F_ALP][kf];
-    }
 #pragma unroll
     for (int c = C0; c < C1; ++c) {
         rh[c] = div_sum(cf.xp(fh, fl, c) - cf.xm(fh, fl, c), idx, cf.yp(gh, gl, c) - cf.ym(gh, gl, c), idy);
-        if (c == 5)
+        rl[c] = div_sum(fl.f[c][kw] - fl.f[c][kx], idx, gl.f[c][kw] - gl.f[c][ky], idy);
+        if (c == 5) {
+            FT a;
+            if constexpr (sizeof(FT) == 4) a = to_f32(q.f[F_ALP][kf]);
+            else a = q.f[F_ALP][kf];
             rh[c] = rh[c] - src_term(a, cf.xp(fh, fl, 6) - cf.xm(fh, fl, 6), idx) -
                     src_term(a, cf.yp(gh, gl, 6) - cf.ym(gh, gl, 6), idy);
+            rl[c] = rl[c] - src_term(a, fl.f[6][kw] - fl.f[6][kx], idx) - src_term(a, gl.f[6][kw] - gl.f[6][ky], idy);
+        }
     }
     if constexpr (sizeof(FT) == 4) {
-        const bool lofin = fl.fin[kw] && fl.fin[kx] && gl.fin[kw] && gl.fin[ky];
-        one = theta_one_f32<STAGE>(e, c32, kw, rh, lofin, to_f32(dt));
+        one = theta_one_f32<STAGE>(e, c32, kw, rh, rl, to_f32(dt));
         if (!VERIFY && one && prechecks) return 1.0;
-    }
-    // the first-order residual: only for the cells the pre-check left
-#pragma unroll
-    for (int c = C0; c < C1; ++c) {
-        rl[c] = div_sum(fl.f[c][kw] - fl.f[c][kx], idx, gl.f[c][kw] - gl.f[c][ky], idy);
-        if (c == 5)
-            rl[c] = rl[c] - src_term(a, fl.f[6][kw] - fl.f[6][kx], idx) - src_term(a, gl.f[6][kw] - gl.f[6][ky], idy);
     }
     double l[6], h[6];
 #pragma unroll
@@ -673,18 +665,19 @@ __device__ __forceinline__ void blend_body(const Grid &g, const Face<FT> &fh, co
                                            const FT *theta, int i, int j)
 {
     long long kw = kw_of(g, i, j);
-    // A face at theta = 1 whose low-order values are all finite keeps its high-order values
-    // (face_blend's value there): only its theta and its finiteness byte are read, nothing is written.
+    // Binary64: a face at theta = 1 whose low-order values are all finite keeps its high-order
+    // values (face_blend's value there): only its theta and its finiteness byte are read, nothing
+    // is written. Binary32: the formula on every face.
     if (j >= g.g) {  // x face between (i, j) and (i+1, j)
         const FT t = face_theta_x(g, theta, kw, i);
-        if (!keeps_high(t, fl.fin[kw] != 0)) {
+        if (!(sizeof(FT) == 8 && keeps_high(t, fl.fin[kw] != 0))) {
 #pragma unroll
             for (int c = 0; c < 7; ++c) fh.f[c][kw] = face_blend(fl.f[c][kw], fh.f[c][kw], t);
         }
     }
     if (i >= g.g) {  // y face between (i, j) and (i, j+1)
         const FT t = face_theta_y(g, theta, kw, j);
-        if (!keeps_high(t, gl.fin[kw] != 0)) {
+        if (!(sizeof(FT) == 8 && keeps_high(t, gl.fin[kw] != 0))) {
 #pragma unroll
             for (int c = 0; c < 7; ++c) gh.f[c][kw] = face_blend(gl.f[c][kw], gh.f[c][kw], t);
         }
@@ -1099,7 +1092,7 @@ __device__ __forceinline__ void face_body(const Eos &e, const V &v, const Face<F
             fin = fin && finite_bits(FT(f[c]));
         }
         lo.f[6][kw] = FT(us);
-        lo.fin[kw] = fin ? 1 : 0;
+        if constexpr (sizeof(FT) == 8) lo.fin[kw] = fin ? 1 : 0;  // read by the binary64 limiter
     }
     if (!do_high) return;
 

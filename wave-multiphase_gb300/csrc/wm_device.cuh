@@ -901,10 +901,10 @@ __device__ __forceinline__ void hllc(const Side<T> &L, const Side<T> &R, T f[6],
 }
 
 // Blend of a high-order face value toward the first-order one, low + theta (high - low)
-// (pp_blend_*_flux_kernel body, SC:1506-1512), with one deliberate difference: at theta = 1 with a
-// finite low value it is the high value itself -- the blend's exact value, where the reference's
-// low + (high - low) can round one unit away -- so a face the limiter leaves alone keeps its
-// high-order flux and the in-place blend need not rewrite it. A non-finite low, high or theta
+// (pp_blend_*_flux_kernel body, SC:1506-1512), with one deliberate difference in binary64: at
+// theta = 1 with a finite low value it is the high value itself -- the blend's exact value, where
+// the reference's low + (high - low) can round one unit away -- so a face the limiter leaves alone
+// keeps its high-order flux and the in-place blend need not rewrite it. A non-finite low, high or theta
 // takes the formula (NaN propagates as in the reference). Shared by the in-place limiter and the
 // fused stage so both give the same bits. The tests are integer compares of the bit patterns.
 __device__ __forceinline__ bool is_one(double t) { return __double_as_longlong(t) == 0x3ff0000000000000LL; }
@@ -918,15 +918,19 @@ __device__ __forceinline__ double face_blend(double low, double high, double the
 {
     return is_one(theta) && finite_bits(low) ? high : __fma_rn(theta, high - low, low);
 }
-// Binary32 (the precision form): the same rule.
+// Binary32 (the precision form's rebuilt blends): the reference's formula. The theta = 1 rule with
+// the first-order finiteness bytes was measured slower there (triple point 2604 -> 2325
+// Mcell-stage/s): the latency-bound rebuilt blends then wait on the byte before the first-order
+// load, which costs more than the 4-byte loads it saves.
 __device__ __forceinline__ float face_blend(float low, float high, float theta)
 {
-    return is_one(theta) && finite_bits(low) ? high : __fmaf_rn(theta, high - low, low);
+    return __fmaf_rn(theta, high - low, low);
 }
 // True when face_blend(low, high, theta) is `high` for every component of a face whose first-order
-// values are all finite (`lofin`, the sweep's per-face byte): the blend at theta = 1 then needs no
-// first-order value.
-template <typename FT> __device__ __forceinline__ bool keeps_high(FT theta, bool lofin) { return lofin && is_one(theta); }
+// values are all finite (`lofin`, the sweep's per-face byte): the binary64 blend at theta = 1 then
+// needs no first-order value. Binary32 always blends.
+__device__ __forceinline__ bool keeps_high(double theta, bool lofin) { return lofin && is_one(theta); }
+__device__ __forceinline__ bool keeps_high(float, bool) { return false; }
 
 // Flux difference terms with their rounding pinned (explicit fused multiply-add and products, which
 // the compiler does not re-associate or contract): every kernel that forms a residual or a limiter
