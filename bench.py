@@ -42,15 +42,13 @@ for _p in (ROOT, os.path.join(ROOT, "wave-multiphase_gb300")):
 NX, NY, G = 7168, 3072, 5
 WORKLOAD = f"triple_point_{NX}x{NY}"
 ALG_BYTES_PER_CELL_STAGE = 128.0     # read stage state + step-start state, write new state (avg)
-# Face-sweep binary64 work per face (x or y) and traffic per cell-stage, from the ncu captures
-# summarised in profiles/ (None until measured).
-# Binary64 FLOP per face: 721 (DFMA x 2 + DADD + DMUL) measured by ncu
-# (profiles/face_kernel_triple_point_2048x1024_fp64.md) before two later changes that remove, by
-# the source, about 8 (HLLC forms one side's energy: 3 DFMA, 2 DMUL) and about 20 (MP5's limiter test
-# settled on the integer pipe: a DADD and a DMUL on nearly all ten evaluations of a face).
-FP64_FLOP_PER_FACE = 693.0
-DRAM_BYTES_PER_CELL_STAGE_FP32 = 1265.0
-DRAM_BYTES_PER_CELL_STAGE = 1673.0  # profiles/dram_traffic_triple_point_2048x1024.md
+# Face-sweep binary64 work per face (x or y) and DRAM traffic per cell-stage, from the ncu captures
+# summarised in profiles/ (2048 x 1024 triple point, one kernel per capture): 704 binary64 FLOP per
+# face (DFMA x 2 + DADD + DMUL, profiles/face_kernel_triple_point_2048x1024_fp64.md), and the
+# per-kernel DRAM bytes of one stage summed (profiles/dram_traffic_triple_point_2048x1024.md).
+FP64_FLOP_PER_FACE = 704.0
+DRAM_BYTES_PER_CELL_STAGE_FP32 = 883.0
+DRAM_BYTES_PER_CELL_STAGE = 1314.0
 
 
 def params(nx=None, ny=None, precision="fp64"):
