@@ -39,6 +39,7 @@ def ratio_precheck(p, r, g, e0):
     ok &= (np.abs(p0) >= F(8.67361738e-19)) & (np.abs(p0) <= F(3e38)) & (r0 >= F(8.67361738e-19)) & (r0 <= F(3e38))
     with np.errstate(all="ignore"):
         lnr0 = np.log(r0).astype(F)
+        ip0, ir0 = (F(1) / p0).astype(F), (F(1) / r0).astype(F)
         w0 = F(1) + np.abs(lnr0)
         d = np.zeros((n, 5), dtype=F)
         D = np.zeros((n, 5), dtype=F)
@@ -46,7 +47,7 @@ def ratio_precheck(p, r, g, e0):
             dp = (p[:, k] - p[:, 2]).astype(F)
             dr = (r[:, k] - r[:, 2]).astype(F)
             dg = (g[:, k] - g[:, 2]).astype(F)
-            xp, xr = dp / p0, dr / r0
+            xp, xr = (dp * ip0).astype(F), (dr * ir0).astype(F)
             ok &= (np.abs(xp) <= F(0.5)) & (np.abs(xr) <= F(0.5))
             gk = g[:, k].astype(F)
             ok &= (gk > 0) & (gk <= F(64)) & (np.abs(dg) <= F(64))

@@ -110,8 +110,9 @@ __device__ __forceinline__ int thinc_side_pre(float em2, float em1, float e0, fl
 // an identity for e_k = p_k / r_k^g_k with the differences dp, dr (the clamped densities) and dg
 // (the cells' binary64 mixture gammas) taken in binary64 -- a uniform region gives d = 0 exactly, as
 // its binary64 entropies are equal -- and the rest in binary32, inside the ranges where the bound
-// below holds (|dp / p_0|, |dr / r_0|, |L| <= 0.5). Error bound of d_k: the conversions, quotients
-// and products round by 2^-24, log1pf, logf and expm1f are within 1 ulp (CUDA's documented bounds),
+// below holds (|dp / p_0|, |dr / r_0|, |L| <= 0.5). Error bound of d_k: the conversions, reciprocals
+// and products round by 2^-24 (a quotient dp / p_0 so within 2^-21.9), log1pf, logf and expm1f are
+// within 1 ulp (CUDA's documented bounds),
 // and |x| <= 1.24 |log1p(x)| there; together |dL| <= 2^-19 (|log1p(xp)| + |g log1p(xr)| +
 // |dg| (1 + |ln r_0|)) and |dd| <= 2^-23 |d| + 1.7 |dL|. A and B get those errors through their
 // coefficients, 2^-21 of their magnitudes for their own roundings, and 2^-44 (6.4 + their magnitude)
@@ -130,6 +131,7 @@ __device__ __forceinline__ int thinc_side_delta(const double p[5], const double 
     if (!(fabsf(p0) >= 8.67361738e-19f && fabsf(p0) <= 3.0e38f) || !(r0 >= 8.67361738e-19f && r0 <= 3.0e38f))
         return -1;
     const float lnr0 = logf(r0), w0 = 1.0f + fabsf(lnr0);
+    const float ip0 = __frcp_rn(p0), ir0 = __frcp_rn(r0);  // correctly rounded reciprocals
     float d[5], D[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
@@ -139,7 +141,7 @@ __device__ __forceinline__ int thinc_side_delta(const double p[5], const double 
             continue;
         }
         const double dp = p[k] - p[2], dr = r[k] - r[2], dg = gm[k] - gm[2];
-        const float xp = to_f32(dp) / p0, xr = to_f32(dr) / r0;
+        const float xp = to_f32(dp) * ip0, xr = to_f32(dr) * ir0;
         if (!(fabsf(xp) <= 0.5f) || !(fabsf(xr) <= 0.5f)) return -1;
         const float gk = to_f32(gm[k]), dgf = to_f32(dg);
         if (!(gk > 0.0f && gk <= 64.0f) || !(fabsf(dgf) <= 64.0f)) return -1;
