@@ -177,6 +177,12 @@ int wm_set_prechecks(wm_handle *h, int on);
  * when the error bounds hold). No counterpart in the reference. */
 int wm_verify_switch_precheck(wm_handle *h, const wm_fields *q, long long *checked, long long *decided,
                               long long *disagreed, void *stream);
+/* Diagnostic of the Ducros sensor pre-check on state q (binary64, any form; variant SC's sensor):
+ * for both directions of every cell with a full stencil, the binary32 pre-check (from the binary32
+ * roundings of u, v, p) and the binary64 decision sigma < 0.01 are evaluated from q. Counts as
+ * wm_verify_switch_precheck. No counterpart in the reference. */
+int wm_verify_ducros_precheck(wm_handle *h, const wm_fields *q, long long *checked, long long *decided,
+                              long long *disagreed, void *stream);
 /* Diagnostic of the limiter pre-check (after wm_compute_fluxes and wm_compute_low_fluxes, like
  * wm_limit_fluxes, whose work it does): every bound pass evaluates both the binary32 pre-check that
  * lets cells skip the binary64 bound solve and the solve itself; *decided counts cells the

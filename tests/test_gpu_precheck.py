@@ -267,3 +267,68 @@ def test_switch_precheck_does_not_change_bits(case):
         b, _ = run_steps(pc, qc, nxc, nyc, False, steps=3)
         for k in pu.ALL:
             assert np.array_equal(a[k], b[k], equal_nan=True), (case, precision, k)
+
+
+def stepped(params, q, nx, ny, steps):
+    s = Solver(params, nx, ny)
+    s.initialize(q)
+    old = alloc_state(nx, ny, names=wavemp.FIELDS)
+    s.init_dt(q)
+    for _ in range(steps):
+        s.step(q, old, None, sync=False)
+    return s
+
+
+def test_ducros_precheck_settles_the_droplet_and_the_triple_point():
+    """The binary32 Ducros pre-check (ducros_pre) never contradicts the binary64 sigma < 0.01 and
+    settles nearly every stencil of the Mach-2.4 water cylinder (SI units) and the triple point
+    after 20 steps, shocks, interfaces and vortices included."""
+    nx, ny = 400, 200
+    q = ic.shock_droplet(nx, ny, 1.0, 0.5, mach=2.4)
+    s = stepped(wavemp.SolverParams(dx=1.0 / nx, dy=0.5 / ny, gamma1=4.4, pinf1=6e8, recon="mp5c6",
+                                    bc=("transmissive",) * 4), q, nx, ny, 20)
+    checked, decided, disagreed = s.verify_ducros_precheck(q)
+    assert checked == 2 * (nx + 6) * (ny + 6)
+    assert disagreed == 0
+    assert decided >= 0.99 * checked, (checked, decided)
+    nx, ny = 448, 192
+    q = ic.triple_point(nx, ny)
+    s = stepped(wavemp.SolverParams(dx=7.0 / nx, dy=3.0 / ny, gamma1=1.5, pinf1=0.0, gamma2=1.4, pinf2=0.0,
+                                    recon="mp5c6", bc=("slip",) * 4), q, nx, ny, 20)
+    checked, decided, disagreed = s.verify_ducros_precheck(q)
+    assert disagreed == 0
+    assert decided >= 0.99 * checked, (checked, decided)
+
+
+@pytest.mark.parametrize("seed", [31, 32])
+def test_ducros_precheck_on_noisy_states(seed):
+    """Seeded states whose pressure noise puts the Ducros sigma around 0.01 (relative noise 0.03:
+    a / b about 0.6 of it) and on either side, with noisy velocities, at SI scales: no stencil is
+    decided against the binary64 decision."""
+    nx, ny = 512, 256
+    rng = np.random.default_rng(seed)
+    params = wavemp.SolverParams(dx=1.0 / nx, dy=0.5 / ny, gamma1=4.4, pinf1=6e8, recon="mp5c6")
+    s = Solver(params, nx, ny)
+    total = settled = 0
+    for amp in (1e-4, 3e-3, 0.03, 0.3):
+        q = ic.random_valid(nx, ny, rng, amp=amp)
+        shape = tuple(q["p_p"].shape)
+        noise = torch.from_numpy(1.0 + amp * rng.standard_normal(shape)).cuda()
+        q["p_p"].mul_(noise)
+        for k in ("u_p", "v_p"):
+            q[k].add_(torch.from_numpy(100.0 * amp * rng.standard_normal(shape)).cuda())
+        checked, decided, disagreed = s.verify_ducros_precheck(q)
+        assert disagreed == 0, (amp, checked, decided)
+        total += checked
+        settled += decided
+    assert settled >= 0.99 * total, (settled, total)
+
+
+@pytest.mark.parametrize("case", pu.CASES)
+def test_ducros_precheck_on_fixtures(case):
+    d = pu.load_case(case)
+    nx, ny = int(d["meta_nx"]), int(d["meta_ny"])
+    s = Solver(pu.params_from(d), nx, ny)
+    checked, decided, disagreed = s.verify_ducros_precheck(load_state(d))
+    assert disagreed == 0, (case, checked, decided)
+    assert decided > 0

@@ -61,7 +61,7 @@ __device__ __forceinline__ float side_of(double v, double threshold)
 constexpr float kEnt32Rel = 6.1035156e-05f;  // 2^-14
 __device__ __forceinline__ float entropy32(double ge, double rho_e, double pp)
 {
-    if (pp == 0.0) return 0.0f;
+    if ((__double_as_longlong(pp) << 1) == 0) return 0.0f;  // pp == 0, either sign
     const float r = to_f32(rho_e), gm = to_f32(ge), pf = to_f32(pp), ap = fabsf(pf);
     const float nan = __int_as_float(0x7fc00000);
     if (!(r >= 1.17549435e-38f && r <= 3.0e38f) || !(gm > 0.0f && gm <= 64.0f) ||
@@ -220,21 +220,48 @@ __device__ __forceinline__ double thinc_side(const Eos &e, const Fields &q, cons
     return side_of(cator2_val(v[0], v[1], v[2], v[3], v[4]), kThincThresh);
 }
 
+// Bit equality of two binary64 values, on the integer pipe.
+__device__ __forceinline__ bool same_bits(double a, double b)
+{
+    return __double_as_longlong(a) == __double_as_longlong(b);
+}
+
+// The mixture gamma and p_inf of a cell from its Gamma and Pi (mix_gamma_pinf's formula, with the
+// face sweep's refined reciprocal for 1 / (Gamma (1 + Gamma))): the one evaluation behind every
+// binary64 entropy -- both forms' preparation, the switch pre-checks and their diagnostic -- so the
+// THINC switch is decided on the same values in every form.
+__device__ __forceinline__ void entropy_gamma(double gb, double pb, double &g, double &pi)
+{
+    mix_from_pibig<double, true>(gb, pb, g, pi);
+}
+
+// prim_to_energy (SC:105-110) from the mixture's Gamma and Pi: the same expression.
+__device__ __forceinline__ double energy_gp(double gb, double pb, double rho, double u, double v, double p)
+{
+    return gb * p + pb + 0.5 * rho * (u * u + v * v);
+}
+
 // What prep leaves for thinc_side: with the pre-checks the binary32 entropy and the cell's
 // binary64 mixture gamma (the ratio pre-check's input, and with the cell state all that the binary64
 // entropy of an undecided stencil needs); without, the binary64 entropy.
 template <typename PT>
-__device__ __forceinline__ void store_entropy(const PrepT<PT> &p, long long kw, double ge, double ar1, double ar2,
-                                              double pp, bool prechecks)
+__device__ __forceinline__ void store_entropy_r(const PrepT<PT> &p, long long kw, double ge, double rho, double pp,
+                                                bool prechecks)
 {
-    double rho_e = ar1 + ar2;
-    if (rho_e < kTiny) rho_e = kTiny;
+    double rho_e = rho;
+    if (flt(rho_e, kTiny)) rho_e = kTiny;
     if (prechecks) {
         p.ent32[kw] = entropy32(ge, rho_e, pp);
         p.gam[kw] = ge;
     } else {
         p.ent64[kw] = entropy64_r(ge, rho_e, pp);
     }
+}
+template <typename PT>
+__device__ __forceinline__ void store_entropy(const PrepT<PT> &p, long long kw, double ge, double ar1, double ar2,
+                                              double pp, bool prechecks)
+{
+    store_entropy_r(p, kw, ge, ar1 + ar2, pp, prechecks);
 }
 
 // (x / d < c) as the reference evaluates it, x / d rounded, for d > 0 and c > 0: settled from the
@@ -266,24 +293,28 @@ __device__ __forceinline__ void prep_body(const Grid &g, const Eos &e, const Fie
     double ar1 = q.f[F_AR1][kf], ar2 = q.f[F_AR2][kf], ru = q.f[F_RU][kf], rv = q.f[F_RV][kf];
     double pp = q.f[F_P][kf], al = q.f[F_AL][kf];
 
-    double ge, pie;
-    mix_gamma_pinf(e, al, ge, pie);
+    double gb, pb, ge, pie;
+    mix_gamma_pibig(e, al, gb, pb);
+    entropy_gamma(gb, pb, ge, pie);
     store_entropy(p, kw, ge, ar1, ar2, pp, prechecks);
 
     double rho = ar1 + ar2;
     double ir = rcp_nr(rho);  // 1 / rho (the face sweep's refined reciprocal)
     double a = clamp01_pp(al);
     double gg = ge, pi = pie;
-    if (!(a == al)) mix_gamma_pinf(e, a, gg, pi);
+    if (!same_bits(a, al)) {  // a clamped fraction: its own mixture
+        mix_gamma_pibig(e, a, gb, pb);
+        entropy_gamma(gb, pb, gg, pi);
+    }
     double pl = pp;
-    if (isnan(pl) || floor_quotient_below(pl + pi, gg - 1.0, kPpCtilde)) pl = kPpCtilde * (gg - 1.0) - pi;
+    if (wisnan(pl) || floor_quotient_below(pl + pi, gg - 1.0, kPpCtilde)) pl = kPpCtilde * (gg - 1.0) - pi;
     double u = ru * ir, v = rv * ir;
     p.lu[kw] = u;
     p.lv[kw] = v;
     p.lp[kw] = pl;
     p.la[kw] = a;
     p.lc[kw] = sound_speed_gp(gg, pi, ir, pl);  // the sound speed of the clamped cell's mixture
-    p.lE[kw] = prim_to_energy(e, rho, u, v, pl, a);
+    p.lE[kw] = energy_gp(gb, pb, rho, u, v, pl);  // prim_to_energy with the mixture at hand
 }
 
 // The terms of the Ducros sensor of an interior cell (ducros_kernel, SC:875-916), binary64:
@@ -341,12 +372,101 @@ __device__ __forceinline__ float sigma_side(double a, double b, double d2, doubl
     return side_of((a / den_b) * (d2 / den), kSigmaSmooth);
 }
 
-// Both Ducros sensors of an interior cell as sigma_side codes.
-__device__ __forceinline__ void ducros_sides(const Fields &q, int i, int j, float &cx, float &cy)
+// ------------------------------------------------------------------------------------------------
+// Binary32 pre-check of the Ducros sensor's side of kSigmaSmooth. The face sweep uses sigma only
+// through sigma < 0.01, so the sensor pass first makes that comparison from the binary32 roundings
+// of the stencil's u, v and p (the binary32 form's cell copies, or to_f32 of the state) with an error
+// bound, and evaluates the binary64 sigma (ducros_terms, sigma_side) only where the bound does not
+// settle it. Where it decides, the decision is that of the binary64 evaluation: the same bits.
+//
+// Bound. The binary64 a = |-p_-2 + 16 p_-1 - 30 p_0 + 16 p_1 - p_2| (b with + signs) rounds at most 5
+// times, each within 2^-53 of a partial sum bounded by M = |p_-2| + 16 |p_-1| + 30 |p_0| + 16 |p_1| +
+// |p_2|; the binary32 one differs from the exact a of the binary64 pressures by the inputs' roundings
+// (2^-24 of each, weighted: 2^-24 M) and its own (5 x 2^-24 M); with M computed in binary32 (within
+// 2^-21.3 of M) both are inside E = 2^-20 M of the binary32 value -- also after E is added or
+// subtracted in binary32. The velocity terms: div = 0.5 (u_1 - u_-1) + 0.5 (v_1 - v_-1) (curl alike)
+// in binary64 within 2^-51.9 Mu, Mu = 0.5 (|u_1| + |u_-1| + |v_1| + |v_-1|), and in binary32 within
+// 4 x 2^-24 Mu of the exact value, plus 2^-147 for inputs or results below binary32's normal range:
+// both inside 2^-21 Mu + 2^-140. D = div^2 / (div^2 + curl^2 + 1e-30) rises with |div| and falls
+// with |curl|, so its binary64 value (six roundings: within 2^-50.4) lies between D at the interval
+// ends; evaluated in binary32 those are within 2^-21.6 relative and 2^-49 absolute (a square below
+// the normal range moves D by at most 2^-150 / 1e-30), covered by the factors 1 -+ 2^-20 and 2^-48.
+// sigma = (a / (b + 1e-30)) D in binary64 is within 2^-50 of its exact value, so sigma < 0.01 holds
+// when a_hi D_hi < 0.01 (1 - 2^-18) b_lo, and sigma >= 0.01 when a_lo D_lo > 0.01 (1 + 2^-18)
+// (b_hi + 1e-30): the margins cover the products' binary32 roundings and 0.01f against 0.01. No
+// decision for M outside [2^-90, 2^100] (relative bounds; no overflow), Mu or Mc above 2^60 (squares
+// in range), b_lo below 2^-100 (the products stay normal where it matters), or NaN anywhere.
+__device__ __forceinline__ float f32_of(float x) { return x; }
+__device__ __forceinline__ float f32_of(double x) { return to_f32(x); }
+
+// The pressure terms of one direction: bounds on the binary64 a and b; false where they do not hold.
+__device__ __forceinline__ bool ducros_ab(float pm2, float pm1, float p0, float pp1, float pp2, float &alo,
+                                          float &ahi, float &blo, float &bhi)
 {
+    const float a = fabsf(-pm2 + 16.0f * pm1 - 30.0f * p0 + 16.0f * pp1 - pp2);
+    const float b = fabsf(pm2 + 16.0f * pm1 + 30.0f * p0 + 16.0f * pp1 + pp2);
+    const float M = fabsf(pm2) + 16.0f * fabsf(pm1) + 30.0f * fabsf(p0) + 16.0f * fabsf(pp1) + fabsf(pp2);
+    const float E = 0x1p-20f * M;
+    alo = fmaxf(a - E, 0.0f);
+    ahi = a + E;
+    blo = b - E;
+    bhi = b + E;
+    return M >= 0x1p-90f && M <= 0x1p100f;
+}
+
+__device__ __forceinline__ int ducros_decide(bool ok, float alo, float ahi, float blo, float bhi, float Dlo, float Dhi)
+{
+    if (!ok) return -1;
+    if (blo >= 0x1p-100f && ahi * Dhi < 0.009999962f * blo) return 0;  // 0.01 (1 - 2^-18)
+    if (alo * Dlo > 0.010000038f * (bhi + 1.0e-30f)) return 1;           // 0.01 (1 + 2^-18)
+    return -1;
+}
+
+// Both directions' pre-check codes (0, 1, or -1 undecided) of the cell at k, from arrays of binary64
+// (converted here) or binary32 roundings, with strides sx, sy between x and y neighbours.
+template <typename T>
+__device__ __forceinline__ void ducros_pre(const T *U, const T *V, const T *P, long long k, long long sx,
+                                           long long sy, int &dx, int &dy)
+{
+    const float uxm = f32_of(U[k - sx]), uxp = f32_of(U[k + sx]), uym = f32_of(U[k - sy]), uyp = f32_of(U[k + sy]);
+    const float vxm = f32_of(V[k - sx]), vxp = f32_of(V[k + sx]), vym = f32_of(V[k - sy]), vyp = f32_of(V[k + sy]);
+    const float div = 0.5f * (-uxm + uxp) + 0.5f * (-vym + vyp);
+    const float curl = 0.5f * (-vxm + vxp) - 0.5f * (-uym + uyp);
+    const float Mu = 0.5f * (fabsf(uxm) + fabsf(uxp) + fabsf(vym) + fabsf(vyp));
+    const float Mc = 0.5f * (fabsf(vxm) + fabsf(vxp) + fabsf(uym) + fabsf(uyp));
+    const float Ed = fmaf(0x1p-21f, Mu, 0x1p-140f), Ec = fmaf(0x1p-21f, Mc, 0x1p-140f);
+    const float dlo = fmaxf(fabsf(div) - Ed, 0.0f), dhi = fabsf(div) + Ed;
+    const float clo = fmaxf(fabsf(curl) - Ec, 0.0f), chi = fabsf(curl) + Ec;
+    const float dlo2 = dlo * dlo, dhi2 = dhi * dhi;
+    const float Dlo = fmaxf(fmaf(dlo2 / (dlo2 + chi * chi + 1.0e-30f), 1.0f - 0x1p-20f, -0x1p-48f), 0.0f);
+    const float Dhi = fmaf(dhi2 / (dhi2 + clo * clo + 1.0e-30f), 1.0f + 0x1p-20f, 0x1p-48f);
+    const bool okv = Mu <= 0x1p60f && Mc <= 0x1p60f;
+    const float p0 = f32_of(P[k]);
+    float alo, ahi, blo, bhi;
+    bool ok = okv && ducros_ab(f32_of(P[k - 2 * sx]), f32_of(P[k - sx]), p0, f32_of(P[k + sx]), f32_of(P[k + 2 * sx]),
+                               alo, ahi, blo, bhi);
+    dx = ducros_decide(ok, alo, ahi, blo, bhi, Dlo, Dhi);
+    ok = okv && ducros_ab(f32_of(P[k - 2 * sy]), f32_of(P[k - sy]), p0, f32_of(P[k + sy]), f32_of(P[k + 2 * sy]),
+                          alo, ahi, blo, bhi);
+    dy = ducros_decide(ok, alo, ahi, blo, bhi, Dlo, Dhi);
+}
+
+// Both Ducros sensors' codes of an interior cell: the binary32 pre-check's decisions from the
+// arrays U, V, P (k, sx, sy as ducros_pre), the binary64 sigma_side where it leaves one open.
+template <typename T>
+__device__ __forceinline__ void ducros_sides_pre(const Fields &q, int i, int j, const T *U, const T *V, const T *P,
+                                                 long long k, long long sx, long long sy, float &cx, float &cy)
+{
+    int dx, dy;
+    ducros_pre(U, V, P, k, sx, sy, dx, dy);
+    if (dx >= 0 && dy >= 0) {
+        cx = float(dx);
+        cy = float(dy);
+        return;
+    }
     const DucrosTerms t = ducros_terms(q, i, j);
-    cx = sigma_side(t.ax, t.bx, t.d2, t.den);
-    cy = sigma_side(t.ay, t.by, t.d2, t.den);
+    cx = dx >= 0 ? float(dx) : sigma_side(t.ax, t.bx, t.d2, t.den);
+    cy = dy >= 0 ? float(dy) : sigma_side(t.ay, t.by, t.d2, t.den);
 }
 
 // The THINC switch per cell and direction (cator2_val < 0.35, SC:318-325, 1028-1032) and the
@@ -367,7 +487,7 @@ __device__ __forceinline__ void sensor_body(const Grid &g, const Eos &e, const F
     }
     if (prechecks) {
         float cx, cy;
-        ducros_sides(q, i, j, cx, cy);
+        ducros_sides_pre(q, i, j, q.f[F_U], q.f[F_V], q.f[F_P], kf, q.pitch, 1, cx, cy);
         p.sx[kw] = cx;
         p.sy[kw] = cy;
     } else {
@@ -893,6 +1013,23 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
     return dt_bits;
 }
 
+// (num gb < kPpCtilde gp1) as binary64 evaluates it, for Gamma gb > 0 and gp1 = 1 + gb: the
+// pressure-floor test of the first-order state below, num = (1 + Gamma) p + Pi. Decided from the
+// binary32 roundings where the products are more than 2^-20 apart: each side is within 3 x 2^-24 of
+// its binary64 value (two operand roundings and the product's; 1e-8f is within 2^-25 of 1e-8, a
+// product below the normal range is off by 2^-150 against a right side above 1e-8), and a negative
+// num is below at once. Elsewhere, and for operands outside [2^-100, 2^100], binary64 decides.
+__device__ __forceinline__ bool below_floor(double num, double gb, double gp1)
+{
+    const float g = to_f32(gb), h = to_f32(gp1);
+    if (g >= 0x1p-100f && g <= 0x1p100f && h <= 0x1p100f) {
+        const float lhs = to_f32(num) * g, rhs = float(kPpCtilde) * h;
+        if (lhs > rhs * (1.0f + 0x1p-20f)) return false;
+        if (lhs < rhs * (1.0f - 0x1p-20f)) return true;
+    }
+    return num * gb < kPpCtilde * gp1;
+}
+
 // Binary32 copies of the cell state for the face sweep, the entropy in binary32, and the
 // first-order HLLC cell state whose pressure floor and the numerator of its sound speed are
 // recovered in binary64 (the stiffened-gas p + p_inf cancels to round-off of p_inf ~ 6e8 in
@@ -915,10 +1052,13 @@ __device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const F
     c.v[kw] = to_f32(q.f[F_V][kf]);
     c.E[kw] = to_f32(q.f[F_E][kf]);
 
+    double gb, pb;  // Gamma and Pi of the cell's own fraction
+    mix_gamma_pibig(e, al, gb, pb);
+    const double rho = ar1 + ar2;
     if (sw64) {  // binary64 switches: the entropy of the binary64 form (ent32 is the ent array)
         double ge, pie;
-        mix_gamma_pinf(e, al, ge, pie);
-        store_entropy(p, kw, ge, ar1, ar2, pp, prechecks);
+        entropy_gamma(gb, pb, ge, pie);
+        store_entropy_r(p, kw, ge, rho, pp, prechecks);
     } else {
         float ge, pie;
         mix_gamma_pinf(e, alf, ge, pie);
@@ -929,20 +1069,20 @@ __device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const F
 
     // With g = 1 + 1/Gamma and p_inf = Pi / (1 + Gamma): (p + p_inf) / (g - 1) < floor  <=>
     // ((1 + Gamma) p + Pi) Gamma < floor (1 + Gamma), and c^2 = ((1 + Gamma) p + Pi) / (Gamma rho).
-    const double rho = ar1 + ar2;
     const double a = clamp01_pp(al);
-    double gb, pb;
-    mix_gamma_pibig(e, a, gb, pb);
+    if (!same_bits(a, al)) mix_gamma_pibig(e, a, gb, pb);  // a clamped fraction: its own mixture
     const double gp1 = 1.0 + gb;
     double pl = pp;
-    if (isnan(pl) || (gp1 * pl + pb) * gb < kPpCtilde * gp1) {
+    // the numerator cancels for p near -p_inf and stays binary64; the quotient and root do not
+    double num = gp1 * pl + pb;
+    if (wisnan(pl) || below_floor(num, gb, gp1)) {
         double gg, pi;
         mix_gamma_pinf(e, a, gg, pi);
         pl = kPpCtilde * (gg - 1.0) - pi;
+        num = gp1 * pl + pb;
     }
-    // the numerator cancels for p near -p_inf and stays binary64; the quotient and root do not
     const float rhof = ar1f + ar2f;
-    float val = to_f32(gp1 * pl + pb) / (to_f32(gb) * to_f32(rho));
+    float val = to_f32(num) / (to_f32(gb) * to_f32(rho));
     if (val < float(kTiny)) val = float(kTiny);
     const float irf = 1.0f / rhof;
     const float u = ruf * irf, v = rvf * irf;
@@ -971,8 +1111,8 @@ __device__ __forceinline__ void sensor32_body(const Grid &g, const Eos &e, const
             p.sy[kw] = side_of(1.0, kSigmaSmooth);
             return;
         }
-        if (prechecks) {
-            ducros_sides(q, i, j, p.sx[kw], p.sy[kw]);
+        if (prechecks) {  // the pre-check reads prep's binary32 copies (to_f32 of the state)
+            ducros_sides_pre(q, i, j, c.u, c.v, c.p, kw, W, 1, p.sx[kw], p.sy[kw]);
         } else {
             double sx, sy;
             ducros_xy(q, i, j, sx, sy);

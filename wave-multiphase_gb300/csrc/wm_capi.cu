@@ -849,6 +849,31 @@ int wm_verify_switch_precheck(wm_handle *h, const wm_fields *q, long long *check
     return WM_OK;
 }
 
+int wm_verify_ducros_precheck(wm_handle *h, const wm_fields *q, long long *checked, long long *decided,
+                              long long *disagreed, void *stream)
+{
+    if (!h || !fields_ok(h, q) || !checked || !decided || !disagreed) return WM_ERR_INVALID;
+    unsigned long long *ctr = nullptr, host[3] = {0, 0, 0};
+    cudaStream_t s = as_stream(stream);
+    cudaError_t err = cudaMalloc(&ctr, sizeof host);
+    if (err == cudaSuccess) err = cudaMemsetAsync(ctr, 0, sizeof host, s);
+    if (err == cudaSuccess) {
+        launch_verify_ducros(h->g, to_fields(q), ctr, s);
+        err = cudaGetLastError();
+    }
+    if (err == cudaSuccess) err = cudaMemcpyAsync(host, ctr, sizeof host, cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    cudaFree(ctr);
+    if (err != cudaSuccess) {
+        set_error("wm_verify_ducros_precheck", err);
+        return WM_ERR_CUDA;
+    }
+    *checked = (long long)host[0];
+    *decided = (long long)host[1];
+    *disagreed = (long long)host[2];
+    return WM_OK;
+}
+
 int wm_set_prechecks(wm_handle *h, int on)
 {
     if (!h) return WM_ERR_INVALID;

@@ -292,15 +292,21 @@ __device__ __forceinline__ void mix_gamma_pibig(const Eos &e, T a1, T &gb, T &pb
 
 // mixture gamma and p_inf: g = 1/Gamma + 1, p_inf = (g-1) Pi / g = Pi / (1 + Gamma), with the two
 // reciprocals taken from one division 1 / (Gamma (1 + Gamma)). SW: the face sweep's reciprocal.
+// mix_from_pibig: the same from Gamma and Pi already at hand.
+template <typename T, bool SW = false>
+__device__ __forceinline__ void mix_from_pibig(T gb, T pb, T &g, T &pi)
+{
+    const T gp1 = T(1) + gb;
+    const T inv = SW ? sw_rcp(gb * gp1) : T(1) / (gb * gp1);
+    g = gp1 * inv + T(1);
+    pi = pb * (gb * inv);
+}
 template <typename T, bool SW = false>
 __device__ __forceinline__ void mix_gamma_pinf(const Eos &e, T a1, T &g, T &pi)
 {
     T gb, pb;
     mix_gamma_pibig(e, a1, gb, pb);
-    const T gp1 = T(1) + gb;
-    const T inv = SW ? sw_rcp(gb * gp1) : T(1) / (gb * gp1);
-    g = gp1 * inv + T(1);
-    pi = pb * (gb * inv);
+    mix_from_pibig<T, SW>(gb, pb, g, pi);
 }
 
 // sound_speed(rho, p, a1) with 1/rho supplied. SW (the face sweep): the square root and, in

@@ -99,6 +99,9 @@ void launch_fp64_probe(double *out, int iters, cudaStream_t s, int blocks, int t
 // verify[0..2]: stencils, decided by the pre-check, decided differently.
 void launch_verify_switch(const Grid &g, const Eos &e, const Fields &q, unsigned long long *verify,
                           cudaStream_t s);
+// The Ducros pre-check against the binary64 decision, both directions of every cell with a full
+// stencil; verify[0..2] as launch_verify_switch.
+void launch_verify_ducros(const Grid &g, const Fields &q, unsigned long long *verify, cudaStream_t s);
 
 // Precision form (binary32 face sweep).
 void launch_prep32(const Grid &g, const Eos &e, const Fields &q, const PrepT<float> &p,

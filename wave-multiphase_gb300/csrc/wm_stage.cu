@@ -165,8 +165,9 @@ __global__ void __launch_bounds__(BX *BY) switch_verify_kernel(Grid g, Eos e, Fi
         double v[5], pk[5], rk[5], gk[5];
         for (int k = 0; k < 5; ++k) {
             const long long c = kf + (k - 2) * sq;
-            double ge, pie;
-            mix_gamma_pinf(e, q.f[F_AL][c], ge, pie);
+            double gb, pb, ge, pie;
+            mix_gamma_pibig(e, q.f[F_AL][c], gb, pb);
+            entropy_gamma(gb, pb, ge, pie);
             double rho_e = q.f[F_AR1][c] + q.f[F_AR2][c];
             if (rho_e < kTiny) rho_e = kTiny;
             s[k] = entropy32(ge, rho_e, q.f[F_P][c]);
@@ -179,6 +180,29 @@ __global__ void __launch_bounds__(BX *BY) switch_verify_kernel(Grid g, Eos e, Fi
         int d = thinc_side_pre(s[0], s[1], s[2], s[3], s[4]);
         if (d < 0) d = thinc_side_delta(pk, rk, gk, s[2]);
         const float exact = side_of(cator2_val(v[0], v[1], v[2], v[3], v[4]), kThincThresh);
+        count_if(&verify[0], true);
+        count_if(&verify[1], d >= 0);
+        count_if(&verify[2], d >= 0 && !(float(d) == exact));
+    }
+}
+
+// The Ducros pre-check (ducros_pre on to_f32 of the state, the binary32 form's cell copies) and the
+// binary64 decision (side_of of ducros_xy, the reference's sigma), for both directions of every cell
+// with a full stencil.
+__global__ void __launch_bounds__(BX *BY) ducros_verify_kernel(Grid g, Fields q, unsigned long long *verify)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i < 2 || i >= g.nxg - 2 || j < 2 || j >= g.nyg - 2) return;
+    const long long kf = kf_of(q, i, j);
+    int dx, dy;
+    ducros_pre(q.f[F_U], q.f[F_V], q.f[F_P], kf, q.pitch, 1, dx, dy);
+    double sx, sy;
+    ducros_xy(q, i, j, sx, sy);
+    const float ex = side_of(sx, kSigmaSmooth), ey = side_of(sy, kSigmaSmooth);
+    for (int dir = 0; dir < 2; ++dir) {
+        const int d = dir == 0 ? dx : dy;
+        const float exact = dir == 0 ? ex : ey;
         count_if(&verify[0], true);
         count_if(&verify[1], d >= 0);
         count_if(&verify[2], d >= 0 && !(float(d) == exact));
@@ -347,6 +371,11 @@ void launch_verify_switch(const Grid &g, const Eos &e, const Fields &q, unsigned
                           cudaStream_t s)
 {
     switch_verify_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, e, q, verify);
+}
+
+void launch_verify_ducros(const Grid &g, const Fields &q, unsigned long long *verify, cudaStream_t s)
+{
+    ducros_verify_kernel<<<grid2(g.nyg, g.nxg), dim3(BX, BY), 0, s>>>(g, q, verify);
 }
 
 void launch_widen(const float *src, double *dst, long long n, cudaStream_t s)

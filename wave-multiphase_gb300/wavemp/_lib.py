@@ -79,7 +79,7 @@ EXPORTS = ("wm_version", "wm_last_error", "wm_workspace_bytes", "wm_create", "wm
            "wm_batch_profile_read", "wm_schlieren", "wm_run", "wm_run_uses_graph",
            "wm_set_limiter_sweeps", "wm_batch_dt_log", "wm_verify_limiter_precheck",
            "wm_check_conversions", "wm_set_prechecks", "wm_verify_switch_precheck",
-           "wm_check_sweep_arith", "wm_batch_spin_limit")
+           "wm_check_sweep_arith", "wm_batch_spin_limit", "wm_verify_ducros_precheck")
 STATIC_MAX_CELLS = 32768
 PROF_GROUPS = ("bc", "prep", "faces", "limiter", "final")
 BATCH_PHASES = ("bc_x", "bc_y", "prep", "sensor", "faces", "theta0", "theta1", "theta2", "final",
@@ -155,6 +155,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.wm_verify_limiter_precheck.argtypes = [vp, F, d, ctypes.POINTER(ctypes.c_longlong),
                                              ctypes.POINTER(ctypes.c_longlong), vp]
     L.wm_verify_switch_precheck.argtypes = [vp, F, ctypes.POINTER(ctypes.c_longlong),
+                                            ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong), vp]
+    L.wm_verify_ducros_precheck.argtypes = [vp, F, ctypes.POINTER(ctypes.c_longlong),
                                             ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong), vp]
     L.wm_batch_profile_read.argtypes = [vp, ctypes.POINTER(d * len(BATCH_PHASES)), i, vp]
     for name in EXPORTS:

@@ -226,6 +226,16 @@ class Solver:
                                                     _stream()), "verify_switch_precheck")
         return a.value, b.value, c.value
 
+    def verify_ducros_precheck(self, q) -> tuple[int, int, int]:
+        """Diagnostic of the Ducros sensor pre-check on state q: (direction stencils checked, settled
+        by the binary32 pre-check, settled differently from the binary64 sigma < 0.01 -- 0 when its
+        error bound holds)."""
+        a, b, c = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        _lib.check(self.L.wm_verify_ducros_precheck(self._h, ctypes.byref(self._fields(q, need_prims=True)),
+                                                    ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                                    _stream()), "verify_ducros_precheck")
+        return a.value, b.value, c.value
+
     def set_prechecks(self, on: bool):
         """Binary32 pre-checks that skip binary64 tests they decide -- the limiter's bound solves,
         the combine's admissibility tests, the THINC switch of binary64 sensors (default on; the
