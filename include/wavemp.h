@@ -303,8 +303,9 @@ int wm_schlieren(const wm_fields *q, int nx, int ny, int g, const double *xh, co
 /* The integer-pipe binary64 -> binary32 and binary32 -> binary64 conversions and binary64
  * compares / min / max / sign against the hardware ones on n device bit patterns (each read as a
  * binary64, paired with the next one for the compares, and by its low 32 bits as a binary32): the
- * numbers of results that differ (0 expected; NaN counts as equal to NaN). No counterpart in the
- * reference. */
+ * numbers of results that differ (0 expected; NaN counts as equal to NaN). *bad_f32 also counts
+ * binary32 pairs hi + lo of the switch pre-check whose lo is not the hardware rounding of x - hi
+ * (for |x| in [2^-74, 2^128)) or not 0 (elsewhere). No counterpart in the reference. */
 int wm_check_conversions(const unsigned long long *bits, long long n, long long *bad_f32,
                          long long *bad_f64, long long *bad_cmp, void *stream);
 /* The binary64 face sweep's reciprocal, quotient and square root (a binary32 seed refined by fused
@@ -353,7 +354,7 @@ int wm_profile_read(wm_handle *h, double ms[WM_PROF_GROUPS], long long launches[
  * never wait on the allocator. Runs the same stage as wm_rhs_stage in the plain binary64 form
  * (same kernels, same arithmetic, so the same bits), without a handle: the workspace is a device
  * array inside the library, sized for grids of at most WM_STATIC_MAX_CELLS padded cells,
- * (nx + 2g) * (ny + 2g) <= 32768 (about 10.8 MiB, held by every GPU that loads the library until
+ * (nx + 2g) * (ny + 2g) <= 32768 (about 11.3 MiB, held by every GPU that loads the library until
  * the process exits). Larger grids, and the binary32 precision form (p->precision ==
  * WM_PREC_FP32, whose workspace has another layout), are rejected with WM_ERR_INVALID and a
  * message in wm_last_error(). Calls no cudaMalloc or cudaFree. The first call on a device (and the

@@ -36,10 +36,11 @@ def bytes_for(lib, p, nx, ny, g=5):
     return lib.wm_workspace_bytes(ctypes.byref(p), nx, ny, g)
 
 
-@pytest.mark.parametrize("precision, per_cell", [("fp64", 42 * 8 + 4 + 2), ("fp32", 51 * 4 + 8 + 2)])
+@pytest.mark.parametrize("precision, per_cell", [("fp64", 42 * 8 + 5 * 4 + 2), ("fp32", 54 * 4 + 8 + 2)])
 def test_workspace_bytes_per_padded_cell(lib, precision, per_cell):
-    """Plain form: 42 binary64 arrays and one binary32 array per padded cell (336 + 4 B); precision
-    form: 51 binary32 arrays and one binary64 array (212 B); both: two bytes of first-order
+    """Plain form: 42 binary64 arrays and five binary32 arrays per padded cell (the switch
+    pre-check's entropy and four of its pair arrays: 336 + 20 B); precision form: 54 binary32 arrays
+    (three of them pair arrays) and one binary64 array (224 B); both: two bytes of first-order
     finiteness (x and y faces); each array 256-byte aligned."""
     p = params(precision=precision)
     prev = 0

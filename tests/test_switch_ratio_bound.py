@@ -3,11 +3,12 @@ restated in numpy binary32 on the CPU and checked against the binary64 decision 
 
 The switch is cator2 < 0.35 over the five cell entropies of a stencil (SC:318-325, 1028-1032). The
 pre-check works with the entropies' ratios to the centre's, d_k = e_k / e_0 - 1 =
-expm1(log1p(dp/p0) - g_k log1p(dr/r0) - dg ln r0), the differences in binary64 and the rest in
-binary32, and decides only when its interval bound clears the threshold. Here the same steps run
+expm1(log1p(dp/p0) - g_k log1p(dr/r0) - dg ln r0), the differences from binary32 pairs hi + lo of
+the binary64 values (split32) and the rest in binary32, and decides only when its interval bound
+clears the threshold. Here the same steps run
 in numpy (binary32 arrays, IEEE operations, the C library's log1pf / logf / expm1f, each within an
 ulp as CUDA's are) on a million seeded stencils: smooth one-fluid flow at SI and dimensionless
-scales with fluctuations from 1e-12 to 1e-2, gradients, mixtures with varying gamma, and stencils
+scales with fluctuations from 1e-15 to 1e-2, gradients, mixtures with varying gamma, and stencils
 placed on the threshold. Wherever it decides, the decision must equal the binary64 one (p / rho^g
 with binary64 pow, cator2 in binary64); and it must decide most smooth stencils.
 """
@@ -28,6 +29,13 @@ def binary64_side(p, r, g):
     return np.where(c < 0.35, 0, 1), e[:, 2]
 
 
+def split32(x):
+    """split32: x as binary32 hi + lo (hi = x rounded, lo = (x - hi) rounded)."""
+    with np.errstate(all="ignore"):
+        hi = x.astype(F)
+        return hi, (x - hi.astype(np.float64)).astype(F)
+
+
 def ratio_precheck(p, r, g, e0):
     """thinc_side_delta restated: 0 / 1 where it decides, -1 where it does not."""
     n = p.shape[0]
@@ -35,7 +43,10 @@ def ratio_precheck(p, r, g, e0):
     ok = np.ones(n, dtype=bool)
     ae0 = np.abs(F(e0))
     ok &= (ae0 > 0) & (ae0 <= F(3e38))
-    p0, r0 = p[:, 2].astype(F), r[:, 2].astype(F)
+    ph, pl = split32(p)
+    rh, rl = split32(r)
+    gh, gl_ = split32(g)
+    p0, r0, g0 = ph[:, 2], rh[:, 2], gh[:, 2]
     ok &= (np.abs(p0) >= F(8.67361738e-19)) & (np.abs(p0) <= F(3e38)) & (r0 >= F(8.67361738e-19)) & (r0 <= F(3e38))
     with np.errstate(all="ignore"):
         lnr0 = np.log(r0).astype(F)
@@ -44,19 +55,20 @@ def ratio_precheck(p, r, g, e0):
         d = np.zeros((n, 5), dtype=F)
         D = np.zeros((n, 5), dtype=F)
         for k in (0, 1, 3, 4):
-            dp = (p[:, k] - p[:, 2]).astype(F)
-            dr = (r[:, k] - r[:, 2]).astype(F)
-            dg = (g[:, k] - g[:, 2]).astype(F)
+            dp = (ph[:, k] - p0) + (pl[:, k] - pl[:, 2])
+            dr = (rh[:, k] - r0) + (rl[:, k] - rl[:, 2])
+            dg = (gh[:, k] - g0) + (gl_[:, k] - gl_[:, 2])
             xp, xr = (dp * ip0).astype(F), (dr * ir0).astype(F)
             ok &= (np.abs(xp) <= F(0.5)) & (np.abs(xr) <= F(0.5))
-            gk = g[:, k].astype(F)
-            ok &= (gk > 0) & (gk <= F(64)) & (np.abs(dg) <= F(64))
+            gk = gh[:, k]
+            ok &= (gk > 0) & (gk <= F(64)) & (g0 > 0) & (g0 <= F(64)) & (np.abs(dg) <= F(64))
             lp = np.log1p(xp).astype(F)
             gl = (gk * np.log1p(xr).astype(F)).astype(F)
             dl = (dg * lnr0).astype(F)
             L = ((lp - gl) - dl).astype(F)
             ok &= np.abs(L) <= F(0.5)
-            dL = F(1.9073486e-06) * (np.abs(lp) + np.abs(gl) + np.abs(dg) * w0)
+            dL = F(1.9073486e-06) * (np.abs(lp) + np.abs(gl) + np.abs(dg) * w0) + \
+                F(2.0 ** -43) * (F(1) + gk + (gk + g0) * np.abs(lnr0))
             d[:, k] = np.expm1(L).astype(F)
             D[:, k] = F(1.1920929e-07) * np.abs(d[:, k]) + F(1.7) * dL
         A = F(0.25) * np.abs(d[:, 0] - F(4) * d[:, 1]) + K13 * np.abs(d[:, 0] - F(2) * d[:, 1])
@@ -115,7 +127,7 @@ def test_smooth_one_fluid_stencils_are_settled_correctly():
     settled = total = 0
     for p0, r0, al0 in ((1.0e5, 1.2, 1e-6), (1.0e5, 1000.0, 1 - 1e-6), (1.165e7, 6.857, 1e-6),
                         (1.0, 1.0, 1 - 1e-6), (0.1, 0.125, 1 - 1e-6), (3.0e5, 500.0, 0.5)):
-        for sigma in (0.0, 1e-12, 1e-9, 1e-6, 1e-4, 1e-2):
+        for sigma in (0.0, 1e-15, 1e-12, 1e-9, 1e-6, 1e-4, 1e-2):  # 1e-15: differences in the lo parts only
             for slope in (0.0, 1e-4, 1e-2, 1e-1):
                 s, t = check(*stencils(rng, 4000, p0, r0, al0, sigma, slope))
                 settled += s

@@ -547,9 +547,10 @@ size_t wm_solve_workspace_bytes(const wm_batch_params *p, int nx, int ny)
     if (!p || nx < 1 || ny < 1) return 0;
     const int g = p->g;
     const size_t fin = 2 * arr_bytes(nx, ny, g, 1);  // first-order finiteness bytes, x and y
+    // the switch pre-check's pairs: 3 binary32 arrays (precision form) or 4 beyond the density pair
     if (p->precision == WM_PREC_FP32)
-        return (size_t)(28 + 3 + 11 + 9) * arr_bytes(nx, ny, g, 4) + arr_bytes(nx, ny, g, 8) + fin;
-    return (size_t)42 * arr_bytes(nx, ny, g, 8) + arr_bytes(nx, ny, g, 4) + fin;
+        return (size_t)(28 + 3 + 11 + 9 + 3) * arr_bytes(nx, ny, g, 4) + arr_bytes(nx, ny, g, 8) + fin;
+    return (size_t)42 * arr_bytes(nx, ny, g, 8) + (size_t)(1 + 4) * arr_bytes(nx, ny, g, 4) + fin;
 }
 
 int wm_batch_create(const wm_batch_params *p, int capacity, wm_batch **out)
@@ -660,6 +661,7 @@ int wm_batch_set(wm_batch *b, int slot, const wm_solve_desc *d, void *workspace,
     S.dt_log_len = 0;
     S.dt_mode = 0;
     char *cur = static_cast<char *>(workspace);
+    const size_t cells = (size_t)(d->nx + 2 * g) * (size_t)(d->ny + 2 * g);
     if (b->P.precision == WM_PREC_FP32) {
         size_t a4 = arr_bytes(d->nx, d->ny, g, 4);
         float *f4[28 + 11 + 9 + 3];
@@ -678,9 +680,10 @@ int wm_batch_set(wm_batch *b, int slot, const wm_solve_desc *d, void *workspace,
         C.u = f4[45]; C.v = f4[46]; C.E = f4[47];
         for (int k = 0; k < 3; ++k) S.theta32[k] = f4[48 + k];
         P.ent64 = reinterpret_cast<double *>(cur);
-        P.gam = P.ent64;
         P.ent32 = P.ent;
         cur += arr_bytes(d->nx, d->ny, g, 8);
+        set_pairs(P.pair, reinterpret_cast<float *>(P.ent64), cells, cur, a4, C.p);
+        cur += 3 * a4;
         S.fl32.fin = reinterpret_cast<unsigned char *>(cur);
         S.gl32.fin = S.fl32.fin + arr_bytes(d->nx, d->ny, g, 1);
     } else {
@@ -698,9 +701,11 @@ int wm_batch_set(wm_batch *b, int slot, const wm_solve_desc *d, void *workspace,
         P.sx = f8[31]; P.sy = f8[32]; P.ent = f8[33]; P.cx = f8[34]; P.cy = f8[35]; P.lu = f8[36];
         P.lv = f8[37]; P.lp = f8[38]; P.la = f8[39]; P.lc = f8[40]; P.lE = f8[41];
         P.ent64 = f8[33];
-        P.gam = f8[33];
         P.ent32 = reinterpret_cast<float *>(cur);  // the binary32 entropy of the switch pre-check
-        cur += arr_bytes(d->nx, d->ny, g, 4);
+        const size_t a4 = arr_bytes(d->nx, d->ny, g, 4);
+        cur += a4;
+        set_pairs(P.pair, reinterpret_cast<float *>(f8[33]), cells, cur, a4, nullptr);
+        cur += 4 * a4;
         S.fl.fin = reinterpret_cast<unsigned char *>(cur);
         S.gl.fin = S.fl.fin + arr_bytes(d->nx, d->ny, g, 1);
     }

@@ -33,6 +33,27 @@ __device__ __forceinline__ double entropy64(double ge, double ar1, double ar2, d
     return entropy64_r(ge, rho_e, pp);
 }
 
+// Bit equality of two binary64 values, on the integer pipe.
+__device__ __forceinline__ bool same_bits(double a, double b)
+{
+    return __double_as_longlong(a) == __double_as_longlong(b);
+}
+
+// The mixture gamma and p_inf of a cell from its Gamma and Pi (mix_gamma_pinf's formula, with the
+// face sweep's refined reciprocal for 1 / (Gamma (1 + Gamma))): the one evaluation behind every
+// binary64 entropy -- both forms' preparation, the switch pre-checks and their diagnostic -- so the
+// THINC switch is decided on the same values in every form.
+__device__ __forceinline__ void entropy_gamma(double gb, double pb, double &g, double &pi)
+{
+    mix_from_pibig<double, true>(gb, pb, g, pi);
+}
+
+// prim_to_energy (SC:105-110) from the mixture's Gamma and Pi: the same expression.
+__device__ __forceinline__ double energy_gp(double gb, double pb, double rho, double u, double v, double p)
+{
+    return gb * p + pb + 0.5 * rho * (u * u + v * v);
+}
+
 // A sensor value reduced to its side of the face sweep's threshold: 0 below it, 1 at or above it,
 // NaN for NaN. The map is monotone, so it commutes with the reference's a<b?a:b minimum and maximum
 // over the four cells of a face (NaN included), and (encoded < threshold) holds exactly when
@@ -108,26 +129,34 @@ __device__ __forceinline__ int thinc_side_pre(float em2, float em1, float e0, fl
 // so cator2 < 0.35  <=>  2AB - 0.35 (A^2 + B^2) + 0.65 eps / e_0^2 < 0. Each
 //   d_k = expm1(L_k),  L_k = ln(e_k / e_0) = log1p(dp_k / p_0) - g_k log1p(dr_k / r_0) - dg_k ln r_0,
 // an identity for e_k = p_k / r_k^g_k with the differences dp, dr (the clamped densities) and dg
-// (the cells' binary64 mixture gammas) taken in binary64 -- a uniform region gives d = 0 exactly, as
-// its binary64 entropies are equal -- and the rest in binary32, inside the ranges where the bound
-// below holds (|dp / p_0|, |dr / r_0|, |L| <= 0.5). Error bound of d_k: the conversions, reciprocals
-// and products round by 2^-24 (a quotient dp / p_0 so within 2^-21.9), log1pf, logf and expm1f are
-// within 1 ulp (CUDA's documented bounds),
-// and |x| <= 1.24 |log1p(x)| there; together |dL| <= 2^-19 (|log1p(xp)| + |g log1p(xr)| +
-// |dg| (1 + |ln r_0|)) and |dd| <= 2^-23 |d| + 1.7 |dL|. A and B get those errors through their
-// coefficients, 2^-21 of their magnitudes for their own roundings, and 2^-44 (6.4 + their magnitude)
-// for the binary64 evaluation the decision must reproduce (pow within 2 ulp, the quotient, five
-// roundings of aa). |e_0| comes from the binary32 entropy (within kEnt32Rel). f is bounded over the
-// box by interval arithmetic; a decision needs the interval clear of zero by 2^-18 of f's terms
-// (binary32 roundings of f and the binary64 quotient's). Returns 0 or 1 as the decision, -1 when
-// undecided (NaN or out-of-range inputs included).
-__device__ __forceinline__ int thinc_side_delta(const double p[5], const double r[5], const double gm[5], float e0)
+// (the cells' binary64 mixture gammas) of the binary64 values, here taken from their binary32
+// pairs x = hi + lo (split32, within 2^-48 |x|) as (hi_k - hi_0) + (lo_k - lo_0): within
+// 2^-23 |dx| + 2^-46 (|x_k| + |x_0|) of the binary64 difference, and exactly 0 where the binary64
+// values are equal -- a uniform region gives d = 0 exactly, as its binary64 entropies are equal. The
+// rest is binary32, inside the ranges where the bound below holds (|dp / p_0|, |dr / r_0|,
+// |L| <= 0.5). Error bound of d_k: the pair differences, the hi parts (the binary32 roundings of
+// p_0, r_0, g_k), the reciprocals and the products put a quotient dp / p_0 within 2^-21.68 relative
+// and 2^-44.6 absolute; log1pf, logf and expm1f are within 1 ulp (CUDA's documented bounds), and
+// |x| <= 1.24 |log1p(x)| there; together |dL| <= 2^-19 (|log1p(xp)| + |g log1p(xr)| +
+// |dg| (1 + |ln r_0|)) + 2^-43 (1 + g_k + (g_k + g_0) |ln r_0|) and |dd| <= 2^-23 |d| + 1.7 |dL|.
+// A and B get those errors through their coefficients, 2^-21 of their magnitudes for their own
+// roundings, and 2^-44 (6.4 + their magnitude) for the binary64 evaluation the decision must
+// reproduce (pow within 2 ulp, the quotient, five roundings of aa). |e_0| comes from the binary32
+// entropy (within kEnt32Rel). f is bounded over the box by interval arithmetic; a decision needs
+// the interval clear of zero by 2^-18 of f's terms (binary32 roundings of f and the binary64
+// quotient's). Returns 0 or 1 as the decision, -1 when undecided (NaN or out-of-range inputs
+// included). No binary64 arithmetic.
+struct SwitchPairs {
+    float ph[5], pl[5], rh[5], rl[5], gh[5], gl[5];
+};
+__device__ __forceinline__ int thinc_side_delta(const SwitchPairs &w, float e0)
 {
     const float ae0 = fabsf(e0);
     if (!(ae0 > 0.0f) || !(ae0 <= 3.0e38f)) return -1;
     // |p_0|, r_0 >= 2^-60: a difference that is subnormal in binary32 then moves its quotient by
-    // at most 2^-90, far inside the bound's binary64 floor below
-    const float p0 = to_f32(p[2]), r0 = to_f32(r[2]);
+    // at most 2^-90, far inside the bound's binary64 floor below; with |dp / p_0|, |dr / r_0| <= 0.5
+    // every pressure and density of the stencil lies in split32's domain (|x| >= 2^-74)
+    const float p0 = w.ph[2], r0 = w.rh[2], g0 = w.gh[2];
     if (!(fabsf(p0) >= 8.67361738e-19f && fabsf(p0) <= 3.0e38f) || !(r0 >= 8.67361738e-19f && r0 <= 3.0e38f))
         return -1;
     const float lnr0 = logf(r0), w0 = 1.0f + fabsf(lnr0);
@@ -140,15 +169,21 @@ __device__ __forceinline__ int thinc_side_delta(const double p[5], const double 
             D[k] = 0.0f;
             continue;
         }
-        const double dp = p[k] - p[2], dr = r[k] - r[2], dg = gm[k] - gm[2];
-        const float xp = to_f32(dp) * ip0, xr = to_f32(dr) * ir0;
+        const float dp = (w.ph[k] - p0) + (w.pl[k] - w.pl[2]);
+        const float dr = (w.rh[k] - r0) + (w.rl[k] - w.rl[2]);
+        const float dgf = (w.gh[k] - g0) + (w.gl[k] - w.gl[2]);
+        const float xp = dp * ip0, xr = dr * ir0;
         if (!(fabsf(xp) <= 0.5f) || !(fabsf(xr) <= 0.5f)) return -1;
-        const float gk = to_f32(gm[k]), dgf = to_f32(dg);
-        if (!(gk > 0.0f && gk <= 64.0f) || !(fabsf(dgf) <= 64.0f)) return -1;
+        const float gk = w.gh[k];
+        // gammas in [2^-60, 64]: inside split32's domain, and the bound's range
+        if (!(gk >= 8.67361738e-19f && gk <= 64.0f) || !(g0 >= 8.67361738e-19f && g0 <= 64.0f) ||
+            !(fabsf(dgf) <= 64.0f))
+            return -1;
         const float lp = log1pf(xp), gl = gk * log1pf(xr), dl = dgf * lnr0;
         const float L = (lp - gl) - dl;
         if (!(fabsf(L) <= 0.5f)) return -1;
-        const float dL = 1.9073486e-06f * (fabsf(lp) + fabsf(gl) + fabsf(dgf) * w0);  // 2^-19
+        const float dL = 1.9073486e-06f * (fabsf(lp) + fabsf(gl) + fabsf(dgf) * w0) +  // 2^-19
+                         0x1p-43f * (1.0f + gk + (gk + g0) * fabsf(lnr0));
         d[k] = expm1f(L);
         D[k] = 1.1920929e-07f * fabsf(d[k]) + 1.7f * dL;  // 2^-23
     }
@@ -181,6 +216,18 @@ __device__ __forceinline__ int thinc_side_delta(const double p[5], const double 
     return -1;
 }
 
+// The binary64 entropy of the cell at kf from its state: the mixture gamma of entropy_gamma and the
+// clamped density, as the preparation pass evaluates them (the same bits).
+__device__ __forceinline__ double cell_entropy64(const Eos &e, const Fields &q, long long c)
+{
+    double gb, pb, ge, pie;
+    mix_gamma_pibig(e, q.f[F_AL][c], gb, pb);
+    entropy_gamma(gb, pb, ge, pie);
+    double rho_e = q.f[F_AR1][c] + q.f[F_AR2][c];
+    if (flt(rho_e, kTiny)) rho_e = kTiny;
+    return entropy64_r(ge, rho_e, q.f[F_P][c]);
+}
+
 // The THINC switch of the cell at kw (its state at kf) along one direction -- workspace stride sw,
 // state stride sq. With the pre-checks, as side_of's code: the binary32 decision where it is
 // settled, else the ratio pre-check's (thinc_side_delta), else cator2_val of the binary64
@@ -198,47 +245,28 @@ __device__ __forceinline__ double thinc_side(const Eos &e, const Fields &q, cons
         for (int k = 0; k < 5; ++k) s[k] = p.ent32[kw + (k - 2) * sw];
         const int d = thinc_side_pre(s[0], s[1], s[2], s[3], s[4]);
         if (d >= 0) return float(d);
-        // the stencil's pressures, clamped densities and (prep's) binary64 mixture gammas
-        double pk[5], rk[5], gk[5];
+        SwitchPairs w;  // prep's pairs of the stencil's pressures, clamped densities and gammas
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
-            const long long c = kf + (k - 2) * sq;
-            pk[k] = q.f[F_P][c];
-            rk[k] = q.f[F_AR1][c] + q.f[F_AR2][c];
-            if (rk[k] < kTiny) rk[k] = kTiny;
-            gk[k] = p.gam[kw + (k - 2) * sw];
+            const long long c = kw + (k - 2) * sw;
+            w.ph[k] = p.pair[PR_PH][c];
+            w.pl[k] = p.pair[PR_PL][c];
+            w.rh[k] = p.pair[PR_RH][c];
+            w.rl[k] = p.pair[PR_RL][c];
+            w.gh[k] = p.pair[PR_GH][c];
+            w.gl[k] = p.pair[PR_GL][c];
         }
-        const int d2 = thinc_side_delta(pk, rk, gk, s[2]);
+        const int d2 = thinc_side_delta(w, s[2]);
         if (d2 >= 0) return float(d2);
+        // the binary64 entropies from the state, as prep evaluates them
 #pragma unroll
-        for (int k = 0; k < 5; ++k) v[k] = entropy64_r(gk[k], rk[k], pk[k]);
+        for (int k = 0; k < 5; ++k) v[k] = cell_entropy64(e, q, kf + (k - 2) * sq);
     } else {
 #pragma unroll
         for (int k = 0; k < 5; ++k) v[k] = p.ent64[kw + (k - 2) * sw];
         if constexpr (sizeof(PT) == 8) return cator2_val(v[0], v[1], v[2], v[3], v[4]);
     }
     return side_of(cator2_val(v[0], v[1], v[2], v[3], v[4]), kThincThresh);
-}
-
-// Bit equality of two binary64 values, on the integer pipe.
-__device__ __forceinline__ bool same_bits(double a, double b)
-{
-    return __double_as_longlong(a) == __double_as_longlong(b);
-}
-
-// The mixture gamma and p_inf of a cell from its Gamma and Pi (mix_gamma_pinf's formula, with the
-// face sweep's refined reciprocal for 1 / (Gamma (1 + Gamma))): the one evaluation behind every
-// binary64 entropy -- both forms' preparation, the switch pre-checks and their diagnostic -- so the
-// THINC switch is decided on the same values in every form.
-__device__ __forceinline__ void entropy_gamma(double gb, double pb, double &g, double &pi)
-{
-    mix_from_pibig<double, true>(gb, pb, g, pi);
-}
-
-// prim_to_energy (SC:105-110) from the mixture's Gamma and Pi: the same expression.
-__device__ __forceinline__ double energy_gp(double gb, double pb, double rho, double u, double v, double p)
-{
-    return gb * p + pb + 0.5 * rho * (u * u + v * v);
 }
 
 // What prep leaves for thinc_side: with the pre-checks the binary32 entropy and the cell's
@@ -252,7 +280,9 @@ __device__ __forceinline__ void store_entropy_r(const PrepT<PT> &p, long long kw
     if (flt(rho_e, kTiny)) rho_e = kTiny;
     if (prechecks) {
         p.ent32[kw] = entropy32(ge, rho_e, pp);
-        p.gam[kw] = ge;
+        split32(pp, p.pair[PR_PH][kw], p.pair[PR_PL][kw]);
+        split32(rho_e, p.pair[PR_RH][kw], p.pair[PR_RL][kw]);
+        split32(ge, p.pair[PR_GH][kw], p.pair[PR_GL][kw]);
     } else {
         p.ent64[kw] = entropy64_r(ge, rho_e, pp);
     }
@@ -1054,10 +1084,11 @@ __device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const F
 
     double gb, pb;  // Gamma and Pi of the cell's own fraction
     mix_gamma_pibig(e, al, gb, pb);
+    double gp1 = 1.0 + gb;
     const double rho = ar1 + ar2;
     if (sw64) {  // binary64 switches: the entropy of the binary64 form (ent32 is the ent array)
         double ge, pie;
-        entropy_gamma(gb, pb, ge, pie);
+        mix_from_gp1<double, true>(gb, gp1, pb, ge, pie);  // entropy_gamma, 1 + Gamma at hand
         store_entropy_r(p, kw, ge, rho, pp, prechecks);
     } else {
         float ge, pie;
@@ -1070,8 +1101,10 @@ __device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const F
     // With g = 1 + 1/Gamma and p_inf = Pi / (1 + Gamma): (p + p_inf) / (g - 1) < floor  <=>
     // ((1 + Gamma) p + Pi) Gamma < floor (1 + Gamma), and c^2 = ((1 + Gamma) p + Pi) / (Gamma rho).
     const double a = clamp01_pp(al);
-    if (!same_bits(a, al)) mix_gamma_pibig(e, a, gb, pb);  // a clamped fraction: its own mixture
-    const double gp1 = 1.0 + gb;
+    if (!same_bits(a, al)) {  // a clamped fraction: its own mixture
+        mix_gamma_pibig(e, a, gb, pb);
+        gp1 = 1.0 + gb;
+    }
     double pl = pp;
     // the numerator cancels for p near -p_inf and stays binary64; the quotient and root do not
     double num = gp1 * pl + pb;

@@ -34,6 +34,10 @@ int check_launch(const char *where)
 constexpr int kFaceArrays = 28, kThetaArrays = 3, kPrepArrays = 11;
 constexpr int kArrays = kFaceArrays + kThetaArrays + kPrepArrays;
 constexpr int kCellCopies = 9;  // binary32 cell copies of the precision form
+// The switch pre-check's binary32 pairs (PrepT::pair) beyond the density pair, which overlays the
+// binary64 entropy: pressure hi and lo and gamma hi and lo; the precision form's pressure hi is its
+// binary32 pressure copy.
+constexpr int kPairArrays64 = 4, kPairArrays32 = 3;
 constexpr size_t kAlign = 256;
 constexpr size_t kTailBytes = 256;  // counters and dt slots
 
@@ -43,18 +47,20 @@ size_t array_bytes(int nx, int ny, int g, size_t elem = sizeof(double))
     return (n + kAlign - 1) / kAlign * kAlign;
 }
 
-// Workspace of the plain form: 42 binary64 arrays and the binary32 entropy of the switch
-// pre-check. Precision form: 28 binary32 face arrays, 3
+// Workspace of the plain form: 42 binary64 arrays, the binary32 entropy of the switch pre-check and
+// 4 binary32 arrays of its pairs. Precision form: 28 binary32 face arrays, 3
 // binary32 limiter factors (bound solves in binary64, stored in the flux type), 11 binary32
-// per-cell arrays, 9 binary32 cell copies and the binary64 entropy of the binary64 switches.
+// per-cell arrays, 9 binary32 cell copies, the binary64 entropy of the binary64 switches and 3
+// binary32 arrays of the pairs.
 // Both: then the first-order sweeps' per-face finiteness bytes (x, y), one byte a padded cell each.
 size_t layout_bytes(int precision, int nx, int ny, int g)
 {
     const size_t fin = 2 * array_bytes(nx, ny, g, 1);
     if (precision == WM_PREC_FP32)
-        return (size_t)(kArrays + kCellCopies) * array_bytes(nx, ny, g, sizeof(float)) + array_bytes(nx, ny, g) +
-               fin + kTailBytes;
-    return (size_t)kArrays * array_bytes(nx, ny, g) + array_bytes(nx, ny, g, sizeof(float)) + fin + kTailBytes;
+        return (size_t)(kArrays + kCellCopies + kPairArrays32) * array_bytes(nx, ny, g, sizeof(float)) +
+               array_bytes(nx, ny, g) + fin + kTailBytes;
+    return (size_t)kArrays * array_bytes(nx, ny, g) + (size_t)(1 + kPairArrays64) * array_bytes(nx, ny, g, sizeof(float)) +
+           fin + kTailBytes;
 }
 
 bool valid_params(const wm_params *p, int nx, int ny, int g)
@@ -246,6 +252,7 @@ int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t
         return WM_ERR_CUDA;
     }
     char *base = static_cast<char *>(h->ws);
+    const size_t cells = (size_t)(nx + 2 * g) * (size_t)(ny + 2 * g);
     char *tail;
     h->fp32 = p->precision == WM_PREC_FP32;
     // measured on the triple point: rebuilding the blends in registers pays in binary32 (1525 ->
@@ -268,9 +275,11 @@ int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t
         P.lu = h->arr[36]; P.lv = h->arr[37]; P.lp = h->arr[38]; P.la = h->arr[39]; P.lc = h->arr[40];
         P.lE = h->arr[41];
         P.ent64 = h->arr[33];
-        P.gam = h->arr[33];
+        const size_t ab4 = array_bytes(nx, ny, g, sizeof(float));
         P.ent32 = reinterpret_cast<float *>(base + (size_t)kArrays * ab);
-        tail = base + (size_t)kArrays * ab + array_bytes(nx, ny, g, sizeof(float));
+        set_pairs(P.pair, reinterpret_cast<float *>(h->arr[33]), cells, base + (size_t)kArrays * ab + ab4, ab4,
+                  nullptr);
+        tail = base + (size_t)kArrays * ab + (size_t)(1 + kPairArrays64) * ab4;
         h->fl.fin = reinterpret_cast<unsigned char *>(tail);
         h->gl.fin = h->fl.fin + array_bytes(nx, ny, g, 1);
         tail += 2 * array_bytes(nx, ny, g, 1);
@@ -289,6 +298,8 @@ int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t
         }
         double *ent64 = reinterpret_cast<double *>(cur);
         cur += array_bytes(nx, ny, g);
+        char *pairs = cur;
+        cur += (size_t)kPairArrays32 * ab4;
         h->sw64 = p->fp64_switches != 0;
         for (int c = 0; c < 7; ++c) {
             h->fh32.f[c] = h->arr32[WM_WS_FX + c];
@@ -307,11 +318,11 @@ int wm_create(const wm_params *p, int nx, int ny, int g, void *workspace, size_t
         P.lu = h->arr32[36]; P.lv = h->arr32[37]; P.lp = h->arr32[38]; P.la = h->arr32[39];
         P.lc = h->arr32[40]; P.lE = h->arr32[41];
         P.ent64 = ent64;
-        P.gam = ent64;
         P.ent32 = P.ent;
         Cells32 &C = h->cells32;
         C.ar1 = copies[0]; C.ar2 = copies[1]; C.ru = copies[2]; C.rv = copies[3];
         C.p = copies[4]; C.al = copies[5]; C.u = copies[6]; C.v = copies[7]; C.E = copies[8];
+        set_pairs(P.pair, reinterpret_cast<float *>(ent64), cells, pairs, ab4, C.p);
         h->fl32.fin = reinterpret_cast<unsigned char *>(cur);
         h->gl32.fin = h->fl32.fin + array_bytes(nx, ny, g, 1);
         tail = cur + 2 * array_bytes(nx, ny, g, 1);

@@ -103,6 +103,30 @@ __device__ __forceinline__ double to_f64(float x)
     return (double)x;
 }
 
+// x as the binary32 pair hi + lo on the integer pipe: hi = to_f32(x), lo = the binary32 rounding of
+// x - hi. x - hi is exact in binary64: a signed multiple of x's last-place unit 2^(e - 1075) below
+// 2^28 in magnitude, which x's low 29 significand bits and the rounding direction of hi give
+// directly; its conversion (round to nearest) and the exact power-of-two scaling give the same bits
+// as to_f32(x - hi) in binary64. Domain: binary64 exponent e in [949, 1150] (|x| in [2^-74, 2^128),
+// every scaled remainder a normal binary32) -- there hi + lo is within 2^-48 |x| of x, unless hi
+// rounded up to infinity; elsewhere lo = 0.
+__device__ __forceinline__ void split32(double x, float &hi, float &lo)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
+    const int e = (int)((hw >> 20) & 0x7ffu);
+    hi = to_f32(x);
+    lo = 0.0f;
+    if (e >= 949 && e <= 1150) {
+        const unsigned f = ((hw & 0xfffffu) << 3) | (lw >> 29);
+        const int r = (int)(lw & 0x1fffffffu);
+        const bool up = r > 0x10000000 || (r == 0x10000000 && (f & 1u));  // to_f32's rounding
+        const int rem = up ? r - 0x20000000 : r;                           // |x| - |hi| in units
+        // x - hi times 2^(e - 1075); a zero remainder gives +0, as x - hi does
+        lo = __int2float_rn((hw >> 31) ? -rem : rem) * __int_as_float((e - 948) << 23);
+    }
+}
+
 // IEEE a < b on binary64 by integer compares of the bit patterns, off GB300's narrow binary64 pipe:
 // false when either operand is NaN; otherwise the order of the signed magnitudes, in which both
 // zeros map to 0 (so -0 < +0 is false, as IEEE has it).
@@ -292,14 +316,18 @@ __device__ __forceinline__ void mix_gamma_pibig(const Eos &e, T a1, T &gb, T &pb
 
 // mixture gamma and p_inf: g = 1/Gamma + 1, p_inf = (g-1) Pi / g = Pi / (1 + Gamma), with the two
 // reciprocals taken from one division 1 / (Gamma (1 + Gamma)). SW: the face sweep's reciprocal.
-// mix_from_pibig: the same from Gamma and Pi already at hand.
+// mix_from_pibig: the same from Gamma and Pi already at hand; mix_from_gp1 with gp1 = 1 + Gamma too.
 template <typename T, bool SW = false>
-__device__ __forceinline__ void mix_from_pibig(T gb, T pb, T &g, T &pi)
+__device__ __forceinline__ void mix_from_gp1(T gb, T gp1, T pb, T &g, T &pi)
 {
-    const T gp1 = T(1) + gb;
     const T inv = SW ? sw_rcp(gb * gp1) : T(1) / (gb * gp1);
     g = gp1 * inv + T(1);
     pi = pb * (gb * inv);
+}
+template <typename T, bool SW = false>
+__device__ __forceinline__ void mix_from_pibig(T gb, T pb, T &g, T &pi)
+{
+    mix_from_gp1<T, SW>(gb, T(1) + gb, pb, g, pi);
 }
 template <typename T, bool SW = false>
 __device__ __forceinline__ void mix_gamma_pinf(const Eos &e, T a1, T &g, T &pi)

@@ -30,8 +30,9 @@ template <typename PT> struct PrepT {
     PT *ent;                          // cell entropy p / rho^gamma
     double *ent64;                    // the entropy in binary64 (plain form; precision form with
                                       // binary64 switches), every cell, when the pre-checks are off
-    double *gam;                      // with the pre-checks: each cell's binary64 mixture gamma
-                                      // (the same storage as ent64)
+    float *pair[6];                   // with the pre-checks: each cell's pressure, clamped density
+                                      // and binary64 mixture gamma as binary32 pairs hi + lo
+                                      // (PR_* order; the density pair overlays ent64)
     float *ent32;                     // the binary32 entropy of that pre-check (the precision
                                       // form's ent array, which its binary64 switches leave free)
     PT *cx, *cy;                      // smoothness indicator along x and y
@@ -40,6 +41,24 @@ template <typename PT> struct PrepT {
                                       // pressure, clamped alpha, sound speed, energy
 };
 using Prep = PrepT<double>;
+// PrepT::pair: x = hi + lo with hi = x rounded to binary32, lo = the rest rounded (split32)
+enum { PR_PH = 0, PR_PL, PR_RH, PR_RL, PR_GH, PR_GL };
+
+// Places PrepT::pair in a workspace: the density pair in the binary64 entropy's slot (two binary32
+// arrays of `cells` each, which the slot holds), the pressure and gamma pairs in consecutive
+// binary32 arrays `stride` bytes apart from `next` -- the pressure hi first, unless `p_hi` (the
+// precision form's binary32 pressure copy, the same values) is given: 4 arrays, or 3.
+inline void set_pairs(float *pair[6], float *ent64_slot, size_t cells, char *next, size_t stride, float *p_hi)
+{
+    pair[PR_RH] = ent64_slot;
+    pair[PR_RL] = ent64_slot + cells;
+    int k = 0;
+    auto take = [&]() { return reinterpret_cast<float *>(next + (size_t)(k++) * stride); };
+    pair[PR_PH] = p_hi ? p_hi : take();
+    pair[PR_PL] = take();
+    pair[PR_GH] = take();
+    pair[PR_GL] = take();
+}
 
 // Binary32 copies of the cell state read by the precision form's face sweep (workspace pitch).
 struct Cells32 {

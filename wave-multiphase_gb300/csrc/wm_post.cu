@@ -109,7 +109,16 @@ __global__ void conv_check_kernel(const unsigned long long *in, long long n, uns
         const float y = __uint_as_float((unsigned)in[k]);
         const double c = wm::to_f64(y), d = (double)y;
         const bool same64 = __double_as_longlong(c) == __double_as_longlong(d) || (c != c && d != d);
-        if (!same32) atomicAdd(&bad[0], 1ull);
+        // split32: hi is to_f32; lo the hardware rounding of x - hi (exact in binary64) in its
+        // domain, 0 outside it
+        float sh, sl;
+        wm::split32(x, sh, sl);
+        const int ex = (int)((__double_as_longlong(x) >> 52) & 0x7ff);
+        const bool dom = ex >= 949 && ex <= 1150 && !isinf(sh);
+        const float lref = dom ? __double2float_rn(x - (double)sh) : 0.0f;
+        const bool split_ok = __float_as_uint(sh) == __float_as_uint(a) &&
+                              (dom ? __float_as_uint(sl) == __float_as_uint(lref) : (isinf(sh) || sl == 0.0f));
+        if (!same32 || !split_ok) atomicAdd(&bad[0], 1ull);
         if (!same64) atomicAdd(&bad[1], 1ull);
         // integer binary64 compares against the hardware ones (pairs of neighbouring inputs)
         const double z = __longlong_as_double((long long)in[k + 1 < n ? k + 1 : 0]);

@@ -162,23 +162,24 @@ __global__ void __launch_bounds__(BX *BY) switch_verify_kernel(Grid g, Eos e, Fi
         if (dir == 0 ? (i < 2 || i >= g.nxg - 2) : (j < 2 || j >= g.nyg - 2)) continue;
         const long long sq = dir == 0 ? q.pitch : 1;
         float s[5];
-        double v[5], pk[5], rk[5], gk[5];
+        double v[5];
+        SwitchPairs w;  // the pairs prep stores, from the same binary64 values
         for (int k = 0; k < 5; ++k) {
             const long long c = kf + (k - 2) * sq;
             double gb, pb, ge, pie;
             mix_gamma_pibig(e, q.f[F_AL][c], gb, pb);
             entropy_gamma(gb, pb, ge, pie);
             double rho_e = q.f[F_AR1][c] + q.f[F_AR2][c];
-            if (rho_e < kTiny) rho_e = kTiny;
+            if (flt(rho_e, kTiny)) rho_e = kTiny;
             s[k] = entropy32(ge, rho_e, q.f[F_P][c]);
-            v[k] = entropy64_r(ge, rho_e, q.f[F_P][c]);
-            pk[k] = q.f[F_P][c];
-            rk[k] = rho_e;
-            gk[k] = ge;
+            v[k] = cell_entropy64(e, q, c);
+            split32(q.f[F_P][c], w.ph[k], w.pl[k]);
+            split32(rho_e, w.rh[k], w.rl[k]);
+            split32(ge, w.gh[k], w.gl[k]);
         }
         // both pre-checks, in the sensor's order: binary32 entropies, then entropy ratios
         int d = thinc_side_pre(s[0], s[1], s[2], s[3], s[4]);
-        if (d < 0) d = thinc_side_delta(pk, rk, gk, s[2]);
+        if (d < 0) d = thinc_side_delta(w, s[2]);
         const float exact = side_of(cator2_val(v[0], v[1], v[2], v[3], v[4]), kThincThresh);
         count_if(&verify[0], true);
         count_if(&verify[1], d >= 0);

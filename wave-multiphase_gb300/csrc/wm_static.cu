@@ -6,7 +6,7 @@
 // (same kernels, same arithmetic) without a handle and without allocating: the face fluxes,
 // limiter factors and per-cell sensors live in wm_stage_scratch below, a file-scope device array
 // sized for grids of at most WM_STATIC_MAX_CELLS padded cells. Every GPU that loads this library
-// keeps that array (about 10.8 MiB) until the process exits.
+// keeps that array (about 11.3 MiB) until the process exits.
 //
 // The array is shared by every call on a device and keeps the previous call's contents. Nothing
 // in it needs to start at zero: each entry a stage reads is written earlier in the same stage.
@@ -30,8 +30,9 @@ using namespace wm;
 
 namespace {
 
-constexpr int kArrays = 43;  // 28 face arrays, 3 limiter factors, 11 per-cell arrays, the binary32
-                             // entropy of the switch pre-check (in a binary64-sized slot)
+constexpr int kArrays = 45;  // 28 face arrays, 3 limiter factors, 11 per-cell arrays, the binary32
+                             // entropy of the switch pre-check (in a binary64-sized slot), and two
+                             // slots for four binary32 arrays of its pairs
 constexpr size_t kArrayBytes = ((size_t)WM_STATIC_MAX_CELLS * sizeof(double) + 255) / 256 * 256;
 constexpr size_t kFinBytes = ((size_t)WM_STATIC_MAX_CELLS + 255) / 256 * 256;  // finiteness bytes
 constexpr size_t kScratchBytes = (size_t)kArrays * kArrayBytes + 2 * kFinBytes;
@@ -198,8 +199,9 @@ extern "C" int wm_rhs_stage_static(const wm_params *p, int nx, int ny, int g, co
     P.sx = arr[31]; P.sy = arr[32]; P.ent = arr[33]; P.cx = arr[34]; P.cy = arr[35];
     P.lu = arr[36]; P.lv = arr[37]; P.lp = arr[38]; P.la = arr[39]; P.lc = arr[40]; P.lE = arr[41];
     P.ent64 = arr[33];
-    P.gam = arr[33];
     P.ent32 = reinterpret_cast<float *>(arr[42]);
+    set_pairs(P.pair, reinterpret_cast<float *>(arr[33]), (size_t)G.nxg * (size_t)G.nyg,
+              reinterpret_cast<char *>(arr[43]), kArrayBytes / 2, nullptr);
     Counters none = {nullptr, nullptr, nullptr, nullptr};
 
     Fields F = fields_of(q), O = alpha != 0.0 ? fields_of(q_old) : F;
