@@ -11,7 +11,8 @@ using namespace wm;
 
 enum {
     U_MP5_UL = 0, U_MP5_UR, U_CENTRAL6, U_MUSCL_UL, U_MUSCL_UR, U_THINC_UL, U_THINC_UR, U_CATOR2,
-    U_MM4, U_MM2, U_EOS, U_HLLC_X, U_HLLC_Y, U_EIGEN, U_PPLIM, U_THETA, U_SIGN_SELECT, U_COUNT
+    U_MM4, U_MM2, U_EOS, U_HLLC_X, U_HLLC_Y, U_EIGEN, U_PPLIM, U_THETA, U_SIGN_SELECT, U_LOG1P_PC,
+    U_EXPM1_PC, U_COUNT
 };
 
 // A side of the high-order Riemann problem, built as the sweep builds it from a back-projected
@@ -112,6 +113,8 @@ __global__ void unit_kernel(int fn, long long n, const double *in, int is, doubl
     case U_THETA:
         for (int s = 0; s < 3; ++s) o[s] = theta_cons_stage(e, a, a + 6, s);
         break;
+    case U_LOG1P_PC: o[0] = (double)log1p_pc((float)a[0]); break;  // binary32 arguments, given exactly
+    case U_EXPM1_PC: o[0] = (double)expm1_pc((float)a[0]); break;
     case U_SIGN_SELECT:  // the interface velocity's choice of side by wp.sign(SP) (SC:686, 770)
         o[0] = sign_select(wsign(a[0]), a[1], a[2]);
         break;

@@ -147,3 +147,21 @@ def test_staged_limiter_and_bound_solves(u):
     normwise(got, u["pplim_out"], "pp_limit_reconstructed_state")
     got = ul.unit("theta", np.concatenate([u["theta_l"], u["theta_h"]], axis=1), 3)
     normwise(got, u["theta_out"], "theta_cons_stage", scale=1.0)
+
+
+def test_ratio_precheck_series_within_their_bound():
+    """log1p_pc and expm1_pc (the ratio pre-check's log1p and expm1: the fifth-order series for
+    |x| <= 2^-5, CUDA's log1pf / expm1f beyond) within 2^-22.9 of the exact values on binary32
+    arguments over the range the pre-check admits (|x| <= 0.5), the series' edge included."""
+    rng = np.random.default_rng(9)
+    x = np.concatenate([rng.uniform(-0.5, 0.5, 400_000),
+                        np.sign(rng.standard_normal(400_000)) * 10.0 ** rng.uniform(-38, -1.5, 400_000),
+                        np.array([0.0, -0.0, 0.03125, -0.03125, 0.0312500037, -0.0312500037, 2.0 ** -126,
+                                  1e-45, 0.5, -0.5])]).astype(np.float32).astype(np.float64)
+    for fn, ref in (("log1p_pc", np.log1p), ("expm1_pc", np.expm1)):
+        got = ul.unit(fn, x[:, None], 1)[:, 0]
+        exact = ref(x)
+        tiny = np.abs(exact) < 2.0 ** -126  # binary32 subnormal results: absolute 2^-149
+        rel = np.abs(got - exact) / np.where(tiny, 1.0, np.abs(exact))
+        bound = np.where(tiny, 2.0 ** -148, 2.0 ** -22.9)
+        assert (rel <= bound).all(), (fn, x[rel > bound][:4], got[rel > bound][:4])

@@ -6,8 +6,8 @@ pre-check works with the entropies' ratios to the centre's, d_k = e_k / e_0 - 1 
 expm1(log1p(dp/p0) - g_k log1p(dr/r0) - dg ln r0), the differences from binary32 pairs hi + lo of
 the binary64 values (split32) and the rest in binary32, and decides only when its interval bound
 clears the threshold. Here the same steps run
-in numpy (binary32 arrays, IEEE operations, the C library's log1pf / logf / expm1f, each within an
-ulp as CUDA's are) on a million seeded stencils: smooth one-fluid flow at SI and dimensionless
+in numpy (binary32 arrays, IEEE operations, the fifth-order series of log1p and expm1 for small
+arguments, the C library's log1pf / logf / expm1f, each within an ulp as CUDA's are, beyond) on a million seeded stencils: smooth one-fluid flow at SI and dimensionless
 scales with fluctuations from 1e-15 to 1e-2, gradients, mixtures with varying gamma, and stencils
 placed on the threshold. Wherever it decides, the decision must equal the binary64 one (p / rho^g
 with binary64 pow, cator2 in binary64); and it must decide most smooth stencils.
@@ -27,6 +27,30 @@ def binary64_side(p, r, g):
     bb = 0.25 * np.abs(3.0 * e0 - 4.0 * ep1 + ep2) + (13.0 / 12.0) * np.abs(e0 - 2.0 * ep1 + ep2)
     c = (2.0 * aa * bb + YUXIN) / (aa * aa + bb * bb + YUXIN)
     return np.where(c < 0.35, 0, 1), e[:, 2]
+
+
+def fmaf(x, y, z):
+    return (x.astype(np.float64) * np.float64(y) + np.float64(z)).astype(F)
+
+
+def log1p_pc(x):
+    """log1p_pc: the fifth-order series for |x| <= 2^-5, else the library's log1pf."""
+    t = fmaf(x, 0.2, -0.25)
+    t = fmaf(x, t, F(0.33333334))
+    t = fmaf(x, t, -0.5)
+    t = fmaf(x, t, 1.0)
+    with np.errstate(all="ignore"):
+        return np.where(np.abs(x) <= F(0.03125), (x * t).astype(F), np.log1p(x).astype(F))
+
+
+def expm1_pc(x):
+    """expm1_pc: the fifth-order series for |x| <= 2^-5, else the library's expm1f."""
+    t = fmaf(x, F(0.008333334), F(0.041666668))
+    t = fmaf(x, t, F(0.16666667))
+    t = fmaf(x, t, 0.5)
+    t = fmaf(x, t, 1.0)
+    with np.errstate(all="ignore"):
+        return np.where(np.abs(x) <= F(0.03125), (x * t).astype(F), np.expm1(x).astype(F))
 
 
 def split32(x):
@@ -62,15 +86,15 @@ def ratio_precheck(p, r, g, e0):
             ok &= (np.abs(xp) <= F(0.5)) & (np.abs(xr) <= F(0.5))
             gk = gh[:, k]
             ok &= (gk > 0) & (gk <= F(64)) & (g0 > 0) & (g0 <= F(64)) & (np.abs(dg) <= F(64))
-            lp = np.log1p(xp).astype(F)
-            gl = (gk * np.log1p(xr).astype(F)).astype(F)
+            lp = log1p_pc(xp)
+            gl = (gk * log1p_pc(xr)).astype(F)
             dl = (dg * lnr0).astype(F)
             L = ((lp - gl) - dl).astype(F)
             ok &= np.abs(L) <= F(0.5)
             dL = F(1.9073486e-06) * (np.abs(lp) + np.abs(gl) + np.abs(dg) * w0) + \
                 F(2.0 ** -43) * (F(1) + gk + (gk + g0) * np.abs(lnr0))
-            d[:, k] = np.expm1(L).astype(F)
-            D[:, k] = F(1.1920929e-07) * np.abs(d[:, k]) + F(1.7) * dL
+            d[:, k] = expm1_pc(L)
+            D[:, k] = F(2.3841858e-07) * np.abs(d[:, k]) + F(1.7) * dL
         A = F(0.25) * np.abs(d[:, 0] - F(4) * d[:, 1]) + K13 * np.abs(d[:, 0] - F(2) * d[:, 1])
         B = F(0.25) * np.abs(d[:, 4] - F(4) * d[:, 3]) + K13 * np.abs(d[:, 4] - F(2) * d[:, 3])
         MA = F(0.25) * (np.abs(d[:, 0]) + F(4) * np.abs(d[:, 1])) + K13 * (np.abs(d[:, 0]) + F(2) * np.abs(d[:, 1]))

@@ -13,7 +13,7 @@ LIB = os.path.join(HERE, "csrc", "libwm_units.so")
 INC = os.path.join(os.path.dirname(HERE), "wave-multiphase_gb300", "csrc")
 FN = {name: k for k, name in enumerate(
     ("mp5_ul", "mp5_ur", "central6", "muscl_ul", "muscl_ur", "thinc_ul", "thinc_ur", "cator2", "mm4",
-     "mm2", "eos", "hllc_x", "hllc_y", "eigen", "pplim", "theta", "sign_select"))}
+     "mm2", "eos", "hllc_x", "hllc_y", "eigen", "pplim", "theta", "sign_select", "log1p_pc", "expm1_pc"))}
 
 
 def build(force: bool = False) -> str:

@@ -136,9 +136,10 @@ __device__ __forceinline__ int thinc_side_pre(float em2, float em1, float e0, fl
 // rest is binary32, inside the ranges where the bound below holds (|dp / p_0|, |dr / r_0|,
 // |L| <= 0.5). Error bound of d_k: the pair differences, the hi parts (the binary32 roundings of
 // p_0, r_0, g_k), the reciprocals and the products put a quotient dp / p_0 within 2^-21.68 relative
-// and 2^-44.6 absolute; log1pf, logf and expm1f are within 1 ulp (CUDA's documented bounds), and
-// |x| <= 1.24 |log1p(x)| there; together |dL| <= 2^-19 (|log1p(xp)| + |g log1p(xr)| +
-// |dg| (1 + |ln r_0|)) + 2^-43 (1 + g_k + (g_k + g_0) |ln r_0|) and |dd| <= 2^-23 |d| + 1.7 |dL|.
+// and 2^-44.6 absolute; log1p_pc and expm1_pc are within 2^-22.9 relative and logf within 1 ulp
+// (CUDA's documented bound), and |x| <= 1.24 |log1p(x)| there; together |dL| <= 2^-19 (|log1p(xp)| +
+// |g log1p(xr)| + |dg| (1 + |ln r_0|)) + 2^-43 (1 + g_k + (g_k + g_0) |ln r_0|) and
+// |dd| <= 2^-22 |d| + 1.7 |dL|.
 // A and B get those errors through their coefficients, 2^-21 of their magnitudes for their own
 // roundings, and 2^-44 (6.4 + their magnitude) for the binary64 evaluation the decision must
 // reproduce (pow within 2 ulp, the quotient, five roundings of aa). |e_0| comes from the binary32
@@ -146,17 +147,27 @@ __device__ __forceinline__ int thinc_side_pre(float em2, float em1, float e0, fl
 // the interval clear of zero by 2^-18 of f's terms (binary32 roundings of f and the binary64
 // quotient's). Returns 0 or 1 as the decision, -1 when undecided (NaN or out-of-range inputs
 // included). No binary64 arithmetic.
+// The stencil's pairs: at(k, PR_*) is the pair array's value at stencil cell k (0..4, centre 2) --
+// read from prep's arrays as needed (PairsAt) or held in registers (SwitchPairs).
 struct SwitchPairs {
-    float ph[5], pl[5], rh[5], rl[5], gh[5], gl[5];
+    float v[6][5];
+    __device__ __forceinline__ float operator()(int k, int w) const { return v[w][k]; }
 };
-__device__ __forceinline__ int thinc_side_delta(const SwitchPairs &w, float e0)
+struct PairsAt {
+    float *const *pair;
+    long long c0, stride;
+    __device__ __forceinline__ float operator()(int k, int w) const { return pair[w][c0 + (k - 2) * stride]; }
+};
+template <typename At>
+__device__ __forceinline__ int thinc_side_delta(const At &at, float e0)
 {
     const float ae0 = fabsf(e0);
     if (!(ae0 > 0.0f) || !(ae0 <= 3.0e38f)) return -1;
     // |p_0|, r_0 >= 2^-60: a difference that is subnormal in binary32 then moves its quotient by
     // at most 2^-90, far inside the bound's binary64 floor below; with |dp / p_0|, |dr / r_0| <= 0.5
     // every pressure and density of the stencil lies in split32's domain (|x| >= 2^-74)
-    const float p0 = w.ph[2], r0 = w.rh[2], g0 = w.gh[2];
+    const float p0 = at(2, PR_PH), r0 = at(2, PR_RH), g0 = at(2, PR_GH);
+    const float pl0 = at(2, PR_PL), rl0 = at(2, PR_RL), gl0 = at(2, PR_GL);
     if (!(fabsf(p0) >= 8.67361738e-19f && fabsf(p0) <= 3.0e38f) || !(r0 >= 8.67361738e-19f && r0 <= 3.0e38f))
         return -1;
     const float lnr0 = logf(r0), w0 = 1.0f + fabsf(lnr0);
@@ -169,23 +180,23 @@ __device__ __forceinline__ int thinc_side_delta(const SwitchPairs &w, float e0)
             D[k] = 0.0f;
             continue;
         }
-        const float dp = (w.ph[k] - p0) + (w.pl[k] - w.pl[2]);
-        const float dr = (w.rh[k] - r0) + (w.rl[k] - w.rl[2]);
-        const float dgf = (w.gh[k] - g0) + (w.gl[k] - w.gl[2]);
+        const float dp = (at(k, PR_PH) - p0) + (at(k, PR_PL) - pl0);
+        const float dr = (at(k, PR_RH) - r0) + (at(k, PR_RL) - rl0);
+        const float gk = at(k, PR_GH);
+        const float dgf = (gk - g0) + (at(k, PR_GL) - gl0);
         const float xp = dp * ip0, xr = dr * ir0;
         if (!(fabsf(xp) <= 0.5f) || !(fabsf(xr) <= 0.5f)) return -1;
-        const float gk = w.gh[k];
         // gammas in [2^-60, 64]: inside split32's domain, and the bound's range
         if (!(gk >= 8.67361738e-19f && gk <= 64.0f) || !(g0 >= 8.67361738e-19f && g0 <= 64.0f) ||
             !(fabsf(dgf) <= 64.0f))
             return -1;
-        const float lp = log1pf(xp), gl = gk * log1pf(xr), dl = dgf * lnr0;
+        const float lp = log1p_pc(xp), gl = gk * log1p_pc(xr), dl = dgf * lnr0;
         const float L = (lp - gl) - dl;
         if (!(fabsf(L) <= 0.5f)) return -1;
         const float dL = 1.9073486e-06f * (fabsf(lp) + fabsf(gl) + fabsf(dgf) * w0) +  // 2^-19
                          0x1p-43f * (1.0f + gk + (gk + g0) * fabsf(lnr0));
-        d[k] = expm1f(L);
-        D[k] = 1.1920929e-07f * fabsf(d[k]) + 1.7f * dL;  // 2^-23
+        d[k] = expm1_pc(L);
+        D[k] = 2.3841858e-07f * fabsf(d[k]) + 1.7f * dL;  // 2^-22
     }
     const float k13 = 13.0f / 12.0f;
     const float A = 0.25f * fabsf(d[0] - 4.0f * d[1]) + k13 * fabsf(d[0] - 2.0f * d[1]);
@@ -245,18 +256,8 @@ __device__ __forceinline__ double thinc_side(const Eos &e, const Fields &q, cons
         for (int k = 0; k < 5; ++k) s[k] = p.ent32[kw + (k - 2) * sw];
         const int d = thinc_side_pre(s[0], s[1], s[2], s[3], s[4]);
         if (d >= 0) return float(d);
-        SwitchPairs w;  // prep's pairs of the stencil's pressures, clamped densities and gammas
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            const long long c = kw + (k - 2) * sw;
-            w.ph[k] = p.pair[PR_PH][c];
-            w.pl[k] = p.pair[PR_PL][c];
-            w.rh[k] = p.pair[PR_RH][c];
-            w.rl[k] = p.pair[PR_RL][c];
-            w.gh[k] = p.pair[PR_GH][c];
-            w.gl[k] = p.pair[PR_GL][c];
-        }
-        const int d2 = thinc_side_delta(w, s[2]);
+        // prep's pairs of the stencil's pressures, clamped densities and gammas
+        const int d2 = thinc_side_delta(PairsAt{p.pair, kw, sw}, s[2]);
         if (d2 >= 0) return float(d2);
         // the binary64 entropies from the state, as prep evaluates them
 #pragma unroll
@@ -926,14 +927,24 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
             res[5] = div_sum(cf.xp(fh, fl, 5) - cf.xm(fh, fl, 5), idx, cf.yp(gh, gl, 5) - cf.ym(gh, gl, 5), idy) -
                      src6x - src6y;
             long long ko = (long long)i * old.pitch + j;
+            if constexpr (sizeof(FT) == 4) {
+                // binary32 residuals: the increment -beta dt R formed in binary32 (two roundings of
+                // 2^-24 on a residual that is itself binary32), then alpha old + beta Q + increment
+                // in binary64 -- two fused multiply-adds instead of three operations
+                const float sdt = to_f32(-beta * dt);
 #pragma unroll
-            for (int c = 0; c < 6; ++c) {
-                double rc;
-                if constexpr (sizeof(FT) == 4) rc = to_f64(res[c]);
-                else rc = res[c];
-                double base = __fma_rn(-dt, rc, Q[c]);
-                if (beta != 1.0) base = __dmul_rn(beta, base);  // 1 * x is x: stage 1 skips it
-                Q[c] = (flags & FIN_OLD_READ) ? __fma_rn(alpha, old.f[c][ko], base) : base;
+                for (int c = 0; c < 6; ++c) {
+                    const double inc = to_f64(res[c] * sdt);
+                    double base = beta != 1.0 ? __fma_rn(beta, Q[c], inc) : __dadd_rn(Q[c], inc);
+                    Q[c] = (flags & FIN_OLD_READ) ? __fma_rn(alpha, old.f[c][ko], base) : base;
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < 6; ++c) {
+                    double base = __fma_rn(-dt, res[c], Q[c]);
+                    if (beta != 1.0) base = __dmul_rn(beta, base);  // 1 * x is x: stage 1 skips it
+                    Q[c] = (flags & FIN_OLD_READ) ? __fma_rn(alpha, old.f[c][ko], base) : base;
+                }
             }
             wrote_q = true;
         }

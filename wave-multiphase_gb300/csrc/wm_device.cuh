@@ -20,9 +20,10 @@ struct Eos {
     double g1, p1, g2, p2;  // gamma, p_inf of fluid 1 and 2
     double r1, r2;          // 1/(g1-1), 1/(g2-1)
     double k1, k2;          // g1*p1/(g1-1), g2*p2/(g2-1)
+    double dr, dk;          // r1 - r2, k1 - k2 (the mixture's slopes in alpha1)
     double thinc_t1;        // tanh(beta/2), beta = 1.8 (computed once on the host)
     double thinc_inv_t1;    // 1/tanh(beta/2)
-    float r1f, r2f, k1f, k2f;  // binary32 copies (binary32 kernels use these: no conversion on the
+    float r1f, r2f, k1f, k2f, drf, dkf;  // binary32 copies (binary32 kernels use these: no conversion on the
     float thinc_t1f, thinc_inv_t1f;  // device, where it would issue on the narrow binary64 pipe)
 };
 
@@ -35,7 +36,9 @@ inline Eos make_eos(double g1, double p1, double g2, double p2)
     E.k1 = g1 * p1 / (g1 - 1.0); E.k2 = g2 * p2 / (g2 - 1.0);
     E.thinc_t1 = std::tanh(1.8 * 0.5);
     E.thinc_inv_t1 = 1.0 / E.thinc_t1;
+    E.dr = E.r1 - E.r2; E.dk = E.k1 - E.k2;
     E.r1f = float(E.r1); E.r2f = float(E.r2); E.k1f = float(E.k1); E.k2f = float(E.k2);
+    E.drf = float(E.dr); E.dkf = float(E.dk);
     E.thinc_t1f = float(E.thinc_t1); E.thinc_inv_t1f = float(E.thinc_inv_t1);
     return E;
 }
@@ -125,6 +128,30 @@ __device__ __forceinline__ void split32(double x, float &hi, float &lo)
         // x - hi times 2^(e - 1075); a zero remainder gives +0, as x - hi does
         lo = __int2float_rn((hw >> 31) ? -rem : rem) * __int_as_float((e - 948) << 23);
     }
+}
+
+// log1p and expm1 of a binary32 x for the ratio pre-check: for |x| <= 2^-5 the Taylor series to the
+// fifth power by Horner's rule with fused multiply-adds (truncation below 2^-27.5 relative, the
+// last two roundings 2^-24 each: within 2^-22.9 of the exact value), elsewhere CUDA's log1pf /
+// expm1f (within 1 ulp). In smooth flow the arguments are that small, and the series costs five
+// operations.
+__device__ __forceinline__ float log1p_pc(float x)
+{
+    if (!(fabsf(x) <= 0.03125f)) return log1pf(x);
+    float t = __fmaf_rn(x, 0.2f, -0.25f);  // 1 - x/2 + x^2/3 - x^3/4 + x^4/5
+    t = __fmaf_rn(x, t, 0.33333334f);
+    t = __fmaf_rn(x, t, -0.5f);
+    t = __fmaf_rn(x, t, 1.0f);
+    return x * t;
+}
+__device__ __forceinline__ float expm1_pc(float x)
+{
+    if (!(fabsf(x) <= 0.03125f)) return expm1f(x);
+    float t = __fmaf_rn(x, 0.008333334f, 0.041666668f);  // 1 + x/2 + x^2/6 + x^3/24 + x^4/120
+    t = __fmaf_rn(x, t, 0.16666667f);
+    t = __fmaf_rn(x, t, 0.5f);
+    t = __fmaf_rn(x, t, 1.0f);
+    return x * t;
 }
 
 // IEEE a < b on binary64 by integer compares of the bit patterns, off GB300's narrow binary64 pipe:
@@ -293,6 +320,8 @@ __device__ __forceinline__ bool wisnan(double x)  // by integer compare of the b
     return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
 }
 __device__ __forceinline__ bool wisnan(float x) { return isnan(x); }
+__device__ __forceinline__ double wfma(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float wfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ double wsqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ float wsqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double wtanh(double x) { return tanh(x); }
@@ -305,13 +334,14 @@ template <typename T> struct S6 { T v[6]; };
 // ------------------------------------------------------------------------------------------------
 // Mixture stiffened-gas EOS (SC:83-110)
 // ------------------------------------------------------------------------------------------------
-// Gamma = sum a_k/(g_k-1), Pi = sum a_k g_k pi_k/(g_k-1)
+// Gamma = sum a_k/(g_k-1), Pi = sum a_k g_k pi_k/(g_k-1), with a2 = 1 - a1: linear in a1, so each
+// is one fused multiply-add from the second fluid's value and the slope (r1 - r2, k1 - k2, formed
+// once on the host) -- within a unit or two in the last place of the two-product sum.
 template <typename T>
 __device__ __forceinline__ void mix_gamma_pibig(const Eos &e, T a1, T &gb, T &pb)
 {
-    T a2 = T(1) - a1;
-    gb = a1 * cst<T>(e.r1, e.r1f) + a2 * cst<T>(e.r2, e.r2f);
-    pb = a1 * cst<T>(e.k1, e.k1f) + a2 * cst<T>(e.k2, e.k2f);
+    gb = wfma(a1, cst<T>(e.dr, e.drf), cst<T>(e.r2, e.r2f));
+    pb = wfma(a1, cst<T>(e.dk, e.dkf), cst<T>(e.k2, e.k2f));
 }
 
 // mixture gamma and p_inf: g = 1/Gamma + 1, p_inf = (g-1) Pi / g = Pi / (1 + Gamma), with the two

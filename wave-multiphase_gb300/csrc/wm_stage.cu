@@ -173,9 +173,9 @@ __global__ void __launch_bounds__(BX *BY) switch_verify_kernel(Grid g, Eos e, Fi
             if (flt(rho_e, kTiny)) rho_e = kTiny;
             s[k] = entropy32(ge, rho_e, q.f[F_P][c]);
             v[k] = cell_entropy64(e, q, c);
-            split32(q.f[F_P][c], w.ph[k], w.pl[k]);
-            split32(rho_e, w.rh[k], w.rl[k]);
-            split32(ge, w.gh[k], w.gl[k]);
+            split32(q.f[F_P][c], w.v[PR_PH][k], w.v[PR_PL][k]);
+            split32(rho_e, w.v[PR_RH][k], w.v[PR_RL][k]);
+            split32(ge, w.v[PR_GH][k], w.v[PR_GL][k]);
         }
         // both pre-checks, in the sensor's order: binary32 entropies, then entropy ratios
         int d = thinc_side_pre(s[0], s[1], s[2], s[3], s[4]);
