@@ -265,7 +265,7 @@ __device__ __forceinline__ void run_phase(const BatchDev &B, int phase, int stag
                     th = p == 0 ? theta_body<0, float, 0>(g, S.e, S.q, c, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta32, i, j)
                        : p == 1 ? theta_body<1, float, 1>(g, S.e, S.q, c, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta32, i, j)
                                 : theta_body<2, float, 2>(g, S.e, S.q, c, S.fh32, S.gh32, S.fl32, S.gl32, dt, S.theta32, i, j);
-                    S.theta32[p][kw_of(g, i, j)] = float(th);
+                    S.theta32[p][kw_of(g, i, j)] = store_as<float>(th);
                 } else {  // the earlier passes' blends are in place
                     const Cells32 none32{};
                     th = p == 0 ? theta_body<0, double, 0>(g, S.e, S.q, none32, S.fh, S.gh, S.fl, S.gl, dt, S.theta, i, j)

@@ -927,24 +927,14 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
             res[5] = div_sum(cf.xp(fh, fl, 5) - cf.xm(fh, fl, 5), idx, cf.yp(gh, gl, 5) - cf.ym(gh, gl, 5), idy) -
                      src6x - src6y;
             long long ko = (long long)i * old.pitch + j;
-            if constexpr (sizeof(FT) == 4) {
-                // binary32 residuals: the increment -beta dt R formed in binary32 (two roundings of
-                // 2^-24 on a residual that is itself binary32), then alpha old + beta Q + increment
-                // in binary64 -- two fused multiply-adds instead of three operations
-                const float sdt = to_f32(-beta * dt);
 #pragma unroll
-                for (int c = 0; c < 6; ++c) {
-                    const double inc = to_f64(res[c] * sdt);
-                    double base = beta != 1.0 ? __fma_rn(beta, Q[c], inc) : __dadd_rn(Q[c], inc);
-                    Q[c] = (flags & FIN_OLD_READ) ? __fma_rn(alpha, old.f[c][ko], base) : base;
-                }
-            } else {
-#pragma unroll
-                for (int c = 0; c < 6; ++c) {
-                    double base = __fma_rn(-dt, res[c], Q[c]);
-                    if (beta != 1.0) base = __dmul_rn(beta, base);  // 1 * x is x: stage 1 skips it
-                    Q[c] = (flags & FIN_OLD_READ) ? __fma_rn(alpha, old.f[c][ko], base) : base;
-                }
+            for (int c = 0; c < 6; ++c) {
+                double rc;
+                if constexpr (sizeof(FT) == 4) rc = to_f64(res[c]);
+                else rc = res[c];
+                double base = __fma_rn(-dt, rc, Q[c]);
+                if (!same_bits(beta, 1.0)) base = __dmul_rn(beta, base);  // 1 * x is x: stage 1 skips it
+                Q[c] = (flags & FIN_OLD_READ) ? __fma_rn(alpha, old.f[c][ko], base) : base;
             }
             wrote_q = true;
         }
@@ -1007,7 +997,8 @@ __device__ __forceinline__ unsigned long long final_body(const Grid &g, const Eo
                 if (a1 > 1.0 - kPrimAlphaFloor) a1 = 1.0 - kPrimAlphaFloor;
             }
             Q[F_AL] = a1;
-            double rho = Q[0] + Q[1];
+            // the admissibility block's density is Q[0] + Q[1] of the state as it left it
+            const double rho = (flags & FIN_ADMISSIBLE) ? rg_rho : Q[0] + Q[1];
             double gb, pb, inv;
             if (fast || (a1 == rg_a1 && rho == rg_rho)) {
                 gb = rg_gb; pb = rg_pb; inv = rg_inv;

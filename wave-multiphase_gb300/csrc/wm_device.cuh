@@ -80,7 +80,8 @@ constexpr double kPrimAlphaFloor = 1.0e-8;  // cons_to_prim clamp (SC:852-853)
 // round-to-nearest-even result bit for bit: to_f32 keeps the top 23 fraction bits and rounds at bit
 // 28 of the low word (ties to the even significand; a carry into the exponent is the correct
 // rounding, up to infinity), to_f64 widens exactly; zeros, subnormals, results outside binary32's
-// normal range, infinities and NaN take the hardware instruction.
+// normal range, infinities and NaN take the hardware instruction (an integer-pipe path for the
+// zeros of a state at rest measured slower: its test lengthens every conversion).
 __device__ __forceinline__ float to_f32(double x)
 {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
@@ -153,6 +154,12 @@ __device__ __forceinline__ float expm1_pc(float x)
     t = __fmaf_rn(x, t, 1.0f);
     return x * t;
 }
+
+// A binary64 result stored in the type T: to_f32 for binary32 storage (the same rounding as the
+// implicit conversion, on the integer pipe), unchanged for binary64.
+template <typename T> __device__ __forceinline__ T store_as(double x);
+template <> __device__ __forceinline__ float store_as<float>(double x) { return to_f32(x); }
+template <> __device__ __forceinline__ double store_as<double>(double x) { return x; }
 
 // IEEE a < b on binary64 by integer compares of the bit patterns, off GB300's narrow binary64 pipe:
 // false when either operand is NaN; otherwise the order of the signed magnitudes, in which both

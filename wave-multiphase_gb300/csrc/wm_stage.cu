@@ -97,8 +97,8 @@ theta_kernel(Grid g, Eos e, Fields q, Cells32 c32, Face<FT> fh, Face<FT> gh, Fac
     if (dt_dev) dt = *dt_dev;
     double th = theta_body<STAGE, FT, NP, VERIFY>(g, e, q, c32, fh, gh, fl, gl, dt, th3.t, i, j, verify,
                                                   prechecks != 0);
-    th3.t[STAGE][kw_of(g, i, j)] = FT(th);
-    if (limited) count_if(limited, th < 1.0);
+    th3.t[STAGE][kw_of(g, i, j)] = store_as<FT>(th);
+    if (limited) count_if(limited, flt(th, 1.0));
 }
 
 template <typename FT>
