@@ -331,9 +331,10 @@ __device__ __forceinline__ void prep_body(const Grid &g, const Eos &e, const Fie
 
     double rho = ar1 + ar2;
     double ir = rcp_nr(rho);  // 1 / rho (the face sweep's refined reciprocal)
-    double a = clamp01_pp(al);
+    double a = al;
     double gg = ge, pi = pie;
-    if (!same_bits(a, al)) {  // a clamped fraction: its own mixture
+    if (!alpha_inside(al)) {  // a clamped fraction: its own mixture
+        a = clamp01_pp(al);
         mix_gamma_pibig(e, a, gb, pb);
         entropy_gamma(gb, pb, gg, pi);
     }
@@ -1102,8 +1103,9 @@ __device__ __forceinline__ void prep32_body(const Grid &g, const Eos &e, const F
 
     // With g = 1 + 1/Gamma and p_inf = Pi / (1 + Gamma): (p + p_inf) / (g - 1) < floor  <=>
     // ((1 + Gamma) p + Pi) Gamma < floor (1 + Gamma), and c^2 = ((1 + Gamma) p + Pi) / (Gamma rho).
-    const double a = clamp01_pp(al);
-    if (!same_bits(a, al)) {  // a clamped fraction: its own mixture
+    double a = al;
+    if (!alpha_inside(al)) {  // a clamped fraction: its own mixture
+        a = clamp01_pp(al);
         mix_gamma_pibig(e, a, gb, pb);
         gp1 = 1.0 + gb;
     }

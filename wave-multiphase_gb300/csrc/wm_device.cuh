@@ -80,8 +80,9 @@ constexpr double kPrimAlphaFloor = 1.0e-8;  // cons_to_prim clamp (SC:852-853)
 // round-to-nearest-even result bit for bit: to_f32 keeps the top 23 fraction bits and rounds at bit
 // 28 of the low word (ties to the even significand; a carry into the exponent is the correct
 // rounding, up to infinity), to_f64 widens exactly; zeros, subnormals, results outside binary32's
-// normal range, infinities and NaN take the hardware instruction (an integer-pipe path for the
-// zeros of a state at rest measured slower: its test lengthens every conversion).
+// normal range, infinities and NaN take the hardware instruction. (Zero tests on the integer pipe --
+// in C++ or PTX, in either direction -- were measured: each made the kernels that convert a state
+// at rest slower, though it removed hardware conversions.)
 __device__ __forceinline__ float to_f32(double x)
 {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
@@ -161,39 +162,55 @@ template <typename T> __device__ __forceinline__ T store_as(double x);
 template <> __device__ __forceinline__ float store_as<float>(double x) { return to_f32(x); }
 template <> __device__ __forceinline__ double store_as<double>(double x) { return x; }
 
-// IEEE a < b on binary64 by integer compares of the bit patterns, off GB300's narrow binary64 pipe:
-// false when either operand is NaN; otherwise the order of the signed magnitudes, in which both
-// zeros map to 0 (so -0 < +0 is false, as IEEE has it).
+// IEEE comparisons of binary64 values by integer compares of their bit patterns, off GB300's narrow
+// binary64 pipe. Written in PTX: the same integer arithmetic in C++ is recognised by the compiler in
+// some contexts and turned back into binary64 compares and min / max instructions (measured: 2-3
+// binary64-pipe instructions for a minimum or a clamp written that way, 1 for the hardware compare,
+// 0 for these).
+// a < b: false when either operand is NaN; otherwise the order of the signed magnitudes
+// k = sign ? -|bits| : |bits|, in which both zeros map to 0 (so -0 < +0 is false, as IEEE has it);
+// a <= b likewise.
+#define WM_DCMP_PTX(OP)                                                                                       \
+    "{\n\t.reg .s64 ia, ib, ma, mb, na, nb;\n\t.reg .pred pa, pb, pc;\n\t"                                  \
+    "mov.b64 ia, %1;\n\tmov.b64 ib, %2;\n\t"                                                                 \
+    "and.b64 ma, ia, 0x7fffffffffffffff;\n\tand.b64 mb, ib, 0x7fffffffffffffff;\n\t"                          \
+    "setp.lt.s64 pa, ia, 0;\n\tneg.s64 na, ma;\n\tselp.s64 na, na, ma, pa;\n\t"                              \
+    "setp.lt.s64 pb, ib, 0;\n\tneg.s64 nb, mb;\n\tselp.s64 nb, nb, mb, pb;\n\t"                              \
+    "setp.le.s64 pc, ma, 0x7ff0000000000000;\n\tsetp.le.and.s64 pc, mb, 0x7ff0000000000000, pc;\n\t"        \
+    "setp." OP ".and.s64 pc, na, nb, pc;\n\tselp.u32 %0, 1, 0, pc;\n\t}"
 __device__ __forceinline__ bool dlt(double a, double b)
 {
-    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
-    const long long ma = ia & 0x7fffffffffffffffLL, mb = ib & 0x7fffffffffffffffLL;
-    const long long inf = 0x7ff0000000000000LL;
-    const long long ka = ia < 0 ? -ma : ma, kb = ib < 0 ? -mb : mb;
-    return ma <= inf && mb <= inf && ka < kb;
+    unsigned r;
+    asm(WM_DCMP_PTX("lt") : "=r"(r) : "d"(a), "d"(b));
+    return r != 0u;
 }
-// x < 0 on binary64: sign bit set, not a zero, not NaN
-__device__ __forceinline__ bool dneg(double x)
-{
-    const long long ix = __double_as_longlong(x);
-    const long long m = ix & 0x7fffffffffffffffLL;
-    return ix < 0 && m != 0 && m <= 0x7ff0000000000000LL;
-}
-
-// IEEE a <= b on binary64 the same way (both zeros map to 0, so -0 <= +0).
 __device__ __forceinline__ bool dle(double a, double b)
 {
-    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
-    const long long ma = ia & 0x7fffffffffffffffLL, mb = ib & 0x7fffffffffffffffLL;
-    const long long inf = 0x7ff0000000000000LL;
-    const long long ka = ia < 0 ? -ma : ma, kb = ib < 0 ? -mb : mb;
-    return ma <= inf && mb <= inf && ka <= kb;
+    unsigned r;
+    asm(WM_DCMP_PTX("le") : "=r"(r) : "d"(a), "d"(b));
+    return r != 0u;
 }
-// x > 0 on binary64: sign bit clear, not a zero, not NaN
+#undef WM_DCMP_PTX
+// x < 0: sign bit set, not a zero, not NaN
+__device__ __forceinline__ bool dneg(double x)
+{
+    unsigned r;
+    asm("{\n\t.reg .s64 ix, m;\n\t.reg .pred p;\n\tmov.b64 ix, %1;\n\t"
+        "and.b64 m, ix, 0x7fffffffffffffff;\n\tsetp.lt.s64 p, ix, 0;\n\t"
+        "setp.ne.and.s64 p, m, 0, p;\n\tsetp.le.and.s64 p, m, 0x7ff0000000000000, p;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r) : "d"(x));
+    return r != 0u;
+}
+// x > 0: sign bit clear, not a zero, not NaN (as a signed integer: in (0, +inf])
 __device__ __forceinline__ bool dpos(double x)
 {
-    const long long ix = __double_as_longlong(x);
-    return ix > 0 && ix <= 0x7ff0000000000000LL;
+    unsigned r;
+    asm("{\n\t.reg .s64 ix;\n\t.reg .pred p;\n\tmov.b64 ix, %1;\n\t"
+        "setp.gt.s64 p, ix, 0;\n\tsetp.le.and.s64 p, ix, 0x7ff0000000000000, p;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r) : "d"(x));
+    return r != 0u;
 }
 
 // IEEE comparisons in the arithmetic type T (binary64: the integer forms above, same results).
@@ -322,9 +339,14 @@ template <> __device__ __forceinline__ double wmax(double a, double b) { return 
 template <> __device__ __forceinline__ double wsign(double x) { return dneg(x) ? -1.0 : 1.0; }
 __device__ __forceinline__ double wabs(double x) { return fabs(x); }
 __device__ __forceinline__ float wabs(float x) { return fabsf(x); }
-__device__ __forceinline__ bool wisnan(double x)  // by integer compare of the bits
+__device__ __forceinline__ bool wisnan(double x)  // by integer compare of the bits, in PTX as dlt
 {
-    return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+    unsigned r;
+    asm("{\n\t.reg .s64 m;\n\t.reg .pred p;\n\tmov.b64 m, %1;\n\t"
+        "and.b64 m, m, 0x7fffffffffffffff;\n\tsetp.gt.s64 p, m, 0x7ff0000000000000;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r) : "d"(x));
+    return r != 0u;
 }
 __device__ __forceinline__ bool wisnan(float x) { return isnan(x); }
 __device__ __forceinline__ double wfma(double a, double b, double c) { return __fma_rn(a, b, c); }
@@ -414,6 +436,18 @@ template <typename T> __device__ __forceinline__ T clamp01_pp(T a1)
     if (flt(a, T(kPpAlpha))) a = T(kPpAlpha);
     if (fgt(a, T(1) - T(kPpAlpha))) a = T(1) - T(kPpAlpha);
     return a;
+}
+
+// True when clamp01_pp leaves a binary64 a1 unchanged: a1 in [kPpAlpha, 1 - kPpAlpha]. Positive
+// binary64 values order like their bit patterns, and negative values, NaN and values outside map
+// above the range after the unsigned subtraction, so one unsigned compare of the bits decides --
+// on the integer pipe (clamp01_pp's compares and selects were measured at three binary64-pipe
+// instructions).
+__device__ __forceinline__ bool alpha_inside(double a1)
+{
+    constexpr unsigned long long lo = 0x3DDB7CDFD9D7BDBBull;  // bits of kPpAlpha = 1e-10
+    constexpr unsigned long long hi = 0x3FEFFFFFFFF24190ull;  // bits of 1 - kPpAlpha
+    return (unsigned long long)__double_as_longlong(a1) - lo <= hi - lo;
 }
 
 __device__ __forceinline__ double pp_theta_lower(double base, double high, double floor_)
@@ -605,15 +639,29 @@ __device__ __forceinline__ double zero_times(double m, bool neg)
     const bool finite = (__double_as_longlong(m) & 0x7fffffffffffffffLL) < 0x7ff0000000000000LL;
     return finite ? with_sign(0.0, neg) : __longlong_as_double(0x7ff8000000000000LL);
 }
+// wmin(|x|, |y|) on the magnitudes' bit patterns (in PTX: a fabs feeding an integer compare would
+// be formed by a binary64 operation): |x| when |x| < |y| with neither NaN, else |y|.
+__device__ __forceinline__ double min_mag(double x, double y)
+{
+    double r;
+    asm("{\n\t.reg .s64 mx, my;\n\t.reg .pred p;\n\tmov.b64 mx, %1;\n\tmov.b64 my, %2;\n\t"
+        "and.b64 mx, mx, 0x7fffffffffffffff;\n\tand.b64 my, my, 0x7fffffffffffffff;\n\t"
+        "setp.le.s64 p, mx, 0x7ff0000000000000;\n\tsetp.le.and.s64 p, my, 0x7ff0000000000000, p;\n\t"
+        "setp.lt.and.s64 p, mx, my, p;\n\tselp.b64 mx, mx, my, p;\n\tmov.b64 %0, mx;\n\t}"
+        : "=d"(r) : "d"(x), "d"(y));
+    return r;
+}
 template <> __device__ __forceinline__ double mm2(double x, double y)
 {
-    const double m = wmin(fabs(x), fabs(y));
+    const double m = min_mag(x, y);
     const bool nx = dneg(x);
     return nx == dneg(y) ? with_sign(m, nx) : zero_times(m, false);
 }
 template <> __device__ __forceinline__ double mm4(double a, double b, double c, double d)
 {
-    const double m = wmin(wmin(fabs(a), fabs(b)), wmin(fabs(c), fabs(d)));
+    // wmin(wmin(|a|, |b|), wmin(|c|, |d|)): the inner minima are magnitudes (or NaN), so the outer
+    // one is min_mag of them
+    const double m = min_mag(min_mag(a, b), min_mag(c, d));
     const bool na = dneg(a), nb = dneg(b);
     if (na == nb && na == dneg(c) && na == dneg(d)) return with_sign(m, na);
     return zero_times(m, na && nb);
