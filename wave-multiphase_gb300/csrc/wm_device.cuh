@@ -625,6 +625,18 @@ template <typename T> __device__ __forceinline__ T mm4(T a, T b, T c, T d)
            wmin(wmin(wabs(a), wabs(b)), wmin(wabs(c), wabs(d)));
 }
 
+// |x| < c for c > 0 (false for NaN x): binary64 by the magnitude's bit pattern in PTX (a fabs
+// feeding the integer compare would be formed by a binary64 addition).
+template <typename T> __device__ __forceinline__ bool abs_lt(T x, T c) { return flt(wabs(x), c); }
+template <> __device__ __forceinline__ bool abs_lt(double x, double c)
+{
+    unsigned r;
+    asm("{\n\t.reg .s64 m, k;\n\t.reg .pred p;\n\tmov.b64 m, %1;\n\tmov.b64 k, %2;\n\t"
+        "and.b64 m, m, 0x7fffffffffffffff;\n\tsetp.lt.s64 p, m, k;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(r) : "d"(x), "d"(c));
+    return r != 0u;
+}
+
 // Binary64 mm2 / mm4 on the integer pipe, the same values as the products above: with the signs
 // of wsign (x < 0 ? -1 : 1) and m the a<b?a:b minimum of the magnitudes, the sign sum and product
 // are +-2 / +-4 when the signs agree (the result is +-m, negated by its sign bit) and 0 otherwise
@@ -669,12 +681,16 @@ template <> __device__ __forceinline__ double mm4(double a, double b, double c, 
 
 // x / 2: binary64 by subtracting 1 from the exponent on the integer pipe (the exact product) where
 // the result stays normal; zeros, subnormals, the smallest normals, infinities and NaN multiply.
+// x * c for the rare operands of the exponent-arithmetic forms below, out of line: inline, the
+// compiler evaluated the product for every operand (measured: one binary64 multiply per call).
+static __device__ __noinline__ double scaled_rare(double x, double c) { return x * c; }
+
 template <typename T> __device__ __forceinline__ T half_of(T x) { return T(0.5) * x; }
 template <> __device__ __forceinline__ double half_of(double x)
 {
     const long long b = __double_as_longlong(x);
     const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
-    return e - 2u < 2045u ? __longlong_as_double(b - (1LL << 52)) : 0.5 * x;
+    return e - 2u < 2045u ? __longlong_as_double(b - (1LL << 52)) : scaled_rare(x, 0.5);
 }
 
 // 0.5 (1 + s) a + 0.5 (1 - s) b for s = wsign(.) = +-1 (the interface velocity of hllc_x_src,
@@ -750,7 +766,7 @@ template <typename T> __device__ __forceinline__ T mp5_alpha_times(T x)
     if constexpr (sizeof(T) == 8) {
         const long long b = __double_as_longlong(x);
         const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
-        return e - 1u < 2044u ? __longlong_as_double(b + (2LL << 52)) : 4.0 * x;
+        return e - 1u < 2044u ? __longlong_as_double(b + (2LL << 52)) : scaled_rare(x, 4.0);
     } else {
         return T(kMp5Alpha) * x;
     }
@@ -968,7 +984,7 @@ __device__ __forceinline__ void hllc(const Side<T> &L, const Side<T> &R, T f[6],
     T SL = wmin(L.un - L.c, n_avg - c_avg);
     T SR = wmax(R.un + R.c, n_avg + c_avg);
     T denom = L.rho * (SL - L.un) - R.rho * (SR - R.un);
-    if (flt(wabs(denom), T(kTiny))) denom = T(kTiny);
+    if (abs_lt(denom, T(kTiny))) denom = T(kTiny);
     T SP = sw_div(R.p - L.p + L.rho * L.un * (SL - L.un) - R.rho * R.un * (SR - R.un), denom);
     T ratioL, ratioR;
     sw_div2(SL - L.un, SL - SP, SR - R.un, SR - SP, ratioL, ratioR);
