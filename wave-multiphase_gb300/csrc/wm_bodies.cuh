@@ -297,13 +297,15 @@ __device__ __forceinline__ void store_entropy(const PrepT<PT> &p, long long kw, 
 
 // (x / d < c) as the reference evaluates it, x / d rounded, for d > 0 and c > 0: settled from the
 // product c d when x is more than 2^-50 of it away (the quotient's and the product's roundings are
-// 2^-53 each), else by the division itself. NaN x takes the division (false).
+// 2^-53 each; the compares on the integer pipe), else by the division itself, out of line. NaN x
+// takes the division (false).
+static __device__ __noinline__ bool quotient_below_rare(double x, double d, double c) { return x / d < c; }
 __device__ __forceinline__ bool floor_quotient_below(double x, double d, double c)
 {
     const double cd = c * d;
-    if (x < cd * (1.0 - 8.8817841970012523e-16)) return true;
-    if (x > cd * (1.0 + 8.8817841970012523e-16)) return false;
-    return x / d < c;
+    if (dlt(x, cd * (1.0 - 8.8817841970012523e-16))) return true;
+    if (dlt(cd * (1.0 + 8.8817841970012523e-16), x)) return false;
+    return quotient_below_rare(x, d, c);
 }
 
 // sound_speed_r's formula for the mixture (g, pi) the caller already holds: sqrt(max(g (p + pi) / rho,

@@ -266,17 +266,22 @@ __device__ __forceinline__ double rcp_refine(double y, unsigned hy, unsigned ey)
     const double e = __fma_rn(-y, s, 1.0);
     return __fma_rn(s, __fma_rn(e, e, e), s);
 }
+// The IEEE operations for the operands the seeded forms below leave to them (zeros, subnormals,
+// infinities, NaN, out-of-range magnitudes), out of line, so that the compiler cannot evaluate
+// them for every operand (as it did with the rare products of the exponent-arithmetic forms).
+static __device__ __noinline__ double ieee_div_rare(double x, double y) { return x / y; }
+static __device__ __noinline__ double ieee_sqrt_rare(double x) { return sqrt(x); }
 __device__ __forceinline__ double rcp_nr(double y)
 {
     const unsigned hy = (unsigned)__double2hiint(y), ey = exp_bits(hy);
-    if (ey - 898u > 249u) return 1.0 / y;
+    if (ey - 898u > 249u) return ieee_div_rare(1.0, y);
     return rcp_refine(y, hy, ey);
 }
 __device__ __forceinline__ double div_nr(double x, double y)
 {
     const unsigned hy = (unsigned)__double2hiint(y), ey = exp_bits(hy);
     const unsigned ex = exp_bits((unsigned)__double2hiint(x));
-    if (ey - 898u > 249u || ex - 127u > 1792u) return x / y;
+    if (ey - 898u > 249u || ex - 127u > 1792u) return ieee_div_rare(x, y);
     const double s = rcp_refine(y, hy, ey);
     const double q0 = __dmul_rn(x, s);
     return __fma_rn(__fma_rn(-y, q0, x), s, q0);
@@ -284,7 +289,7 @@ __device__ __forceinline__ double div_nr(double x, double y)
 __device__ __forceinline__ double sqrt_nr(double x)
 {
     const unsigned hx = (unsigned)__double2hiint(x), ex = exp_bits(hx);
-    if ((hx >> 31) || ex - 898u > 249u) return sqrt(x);
+    if ((hx >> 31) || ex - 898u > 249u) return ieee_sqrt_rare(x);
     float hf;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(hf) : "f"(trunc_f32(hx, ex)));
     const double hh = widen_normal(0.5f * hf);  // h / 2, halved exactly in binary32
