@@ -1001,38 +1001,34 @@ __device__ __forceinline__ void hllc(const Side<T> &L, const Side<T> &R, T f[6],
         EL = ER = gb * p + pb + T(0.5) * rho * (un * un + ut * ut);
     }
 
-    if (fpos(SL)) {
-        f[0] = L.ar1 * L.un;
-        f[1] = L.ar2 * L.un;
-        f[N] = L.rho * L.un * L.un + L.p;
-        f[Tc] = L.rho * L.un * L.ut;
-        f[4] = (EL + L.p) * L.un;
-        f[5] = L.a * L.un;
-    } else if (fle(SL, T(0)) && fpos(SP)) {
-        T ratio = ratioL;
-        T E_star = EL + (SP - L.un) * (SP * L.rho + sw_div(L.p, SL - L.un));
-        f[0] = L.ar1 * L.un + SL * (L.ar1 * ratio - L.ar1);
-        f[1] = L.ar2 * L.un + SL * (L.ar2 * ratio - L.ar2);
-        f[N] = (L.rho * L.un * L.un + L.p) + SL * (L.rho * SP * ratio - L.rho * L.un);
-        f[Tc] = (L.rho * L.un * L.ut) + SL * (L.rho * L.ut * ratio - L.rho * L.ut);
-        f[4] = (EL + L.p) * L.un + SL * (E_star * ratio - EL);
-        f[5] = L.a * L.un + SL * (L.a * ratio - L.a);
-    } else if (fle(SP, T(0)) && fle(T(0), SR)) {
-        T ratio = ratioR;
-        T E_star = ER + (SP - R.un) * (SP * R.rho + sw_div(R.p, SR - R.un));
-        f[0] = R.ar1 * R.un + SR * (R.ar1 * ratio - R.ar1);
-        f[1] = R.ar2 * R.un + SR * (R.ar2 * ratio - R.ar2);
-        f[N] = (R.rho * R.un * R.un + R.p) + SR * (R.rho * SP * ratio - R.rho * R.un);
-        f[Tc] = (R.rho * R.un * R.ut) + SR * (R.rho * R.ut * ratio - R.rho * R.ut);
-        f[4] = (ER + R.p) * R.un + SR * (E_star * ratio - ER);
-        f[5] = R.a * R.un + SR * (R.a * ratio - R.a);
+    // The flux of the region the contact and wave speeds put the face in (SC:594-662): left
+    // supersonic (SL > 0), left star (SL <= 0 < SP), right star (SP <= 0 <= SR) or right supersonic
+    // (the rest, NaN cases included) -- formed from the one side K it reads, selected bit for bit,
+    // with the star correction S_K (U*_K - U_K) where the side is subsonic: the regions' expressions,
+    // without evaluating the other side's.
+    const bool b1 = fpos(SL);
+    const bool b2 = !b1 && fle(SL, T(0)) && fpos(SP);
+    const bool b3 = !b1 && !b2 && fle(SP, T(0)) && fle(T(0), SR);
+    const bool left = b1 || b2, star = b2 || b3;
+    const T ar1 = left ? L.ar1 : R.ar1, ar2 = left ? L.ar2 : R.ar2, rho = left ? L.rho : R.rho;
+    const T un = left ? L.un : R.un, ut = left ? L.ut : R.ut, p = left ? L.p : R.p, a = left ? L.a : R.a;
+    const T EK = left ? EL : ER;
+    if (star) {
+        const T S = left ? SL : SR, ratio = left ? ratioL : ratioR;
+        const T E_star = EK + (SP - un) * (SP * rho + sw_div(p, S - un));
+        f[0] = ar1 * un + S * (ar1 * ratio - ar1);
+        f[1] = ar2 * un + S * (ar2 * ratio - ar2);
+        f[N] = (rho * un * un + p) + S * (rho * SP * ratio - rho * un);
+        f[Tc] = (rho * un * ut) + S * (rho * ut * ratio - rho * ut);
+        f[4] = (EK + p) * un + S * (E_star * ratio - EK);
+        f[5] = a * un + S * (a * ratio - a);
     } else {
-        f[0] = R.ar1 * R.un;
-        f[1] = R.ar2 * R.un;
-        f[N] = R.rho * R.un * R.un + R.p;
-        f[Tc] = R.rho * R.un * R.ut;
-        f[4] = (ER + R.p) * R.un;
-        f[5] = R.a * R.un;
+        f[0] = ar1 * un;
+        f[1] = ar2 * un;
+        f[N] = rho * un * un + p;
+        f[Tc] = rho * un * ut;
+        f[4] = (EK + p) * un;
+        f[5] = a * un;
     }
     T left_part = L.un + wmin(T(0), SL) * (ratioL - T(1));
     T right_part = R.un + wmax(T(0), SR) * (ratioR - T(1));
