@@ -43,12 +43,12 @@ NX, NY, G = 7168, 3072, 5
 WORKLOAD = f"triple_point_{NX}x{NY}"
 ALG_BYTES_PER_CELL_STAGE = 128.0     # read stage state + step-start state, write new state (avg)
 # Face-sweep binary64 work per face (x or y) and DRAM traffic per cell-stage, from the ncu captures
-# summarised in profiles/ (2048 x 1024 triple point, one kernel per capture): 620 binary64 FLOP per
-# face (DFMA x 2 + DADD + DMUL, profiles/fp64_ops_stage_kernels_triple_point_2048x1024.md), and the
-# per-kernel DRAM bytes of one stage summed (profiles/dram_traffic_triple_point_2048x1024.md).
-FP64_FLOP_PER_FACE = 620.1
+# summarised in profiles/ (2048 x 1024 triple point, one kernel per capture): 577 binary64 FLOP per
+# face (DFMA x 2 + DADD + DMUL over the launch's faces, the face-sweep summary), and the per-kernel
+# DRAM bytes of one stage summed (the DRAM-traffic summary).
+FP64_FLOP_PER_FACE = 577.3
 DRAM_BYTES_PER_CELL_STAGE_FP32 = 869.0
-DRAM_BYTES_PER_CELL_STAGE = 1302.0
+DRAM_BYTES_PER_CELL_STAGE = 1255.0
 
 
 def params(nx=None, ny=None, precision="fp64"):

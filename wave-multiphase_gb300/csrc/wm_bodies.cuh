@@ -552,6 +552,35 @@ __device__ __forceinline__ FT face_theta_y(const Grid &g, const FT *theta, long 
     return th;
 }
 
+// The first-order sides of a face (fx_low_kernel's states, SC:1309-1327): cells 0 and 1's partial
+// densities and the preparation pass's first-order cell states (normal and tangential velocity,
+// floored pressure, clamped alpha, sound speed, energy). One builder for the sweep and for the
+// first-order values formed on demand, so both give the same bits.
+template <typename T>
+__device__ __forceinline__ void first_order_side(T ar1, T ar2, T un, T ut, T p, T a, T c, T E, Side<T> &S)
+{
+    S.ar1 = ar1; S.ar2 = ar2; S.rho = ar1 + ar2;
+    S.un = un; S.ut = ut; S.p = p; S.a = a; S.c = c; S.E = E;
+}
+
+// The seven first-order values of the face between the cell at (kw0 in the padded grid, kf0 in the
+// state) and its neighbour along DIR, formed from the face's LowSrc as the sweep forms them.
+template <int DIR>
+__device__ __forceinline__ void low_flux_on_demand(const LowSrc &s, long long kw0, long long kf0, double out[7])
+{
+    const long long sw = DIR == 0 ? s.nyg : 1, sf = DIR == 0 ? s.pitch : 1;
+    const double *un = DIR == 0 ? s.lu : s.lv, *ut = DIR == 0 ? s.lv : s.lu;
+    Side<double> L, R;
+    first_order_side(s.ar1[kf0], s.ar2[kf0], un[kw0], ut[kw0], s.lp[kw0], s.la[kw0], s.lc[kw0], s.lE[kw0], L);
+    const long long k1 = kw0 + sw, f1 = kf0 + sf;
+    first_order_side(s.ar1[f1], s.ar2[f1], un[k1], ut[k1], s.lp[k1], s.la[k1], s.lc[k1], s.lE[k1], R);
+    double f[6], us;
+    hllc<DIR>(L, R, f, us);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) out[c] = f[c];
+    out[6] = us;
+}
+
 // The four faces of interior cell (i, j) with NP limiter passes deferred: the flux a face holds
 // after passes 0..NP-1 is rebuilt from its high- and first-order values and the passes' cell
 // factors by the same face_blend chain blend_body applies in place, so the values are identical
@@ -724,8 +753,9 @@ __device__ __forceinline__ bool theta_one_f64in(const Grid &g, const Eos &e, con
 // as well and counts (verify[0]) cells the pre-check decided and (verify[1]) cells where the solve
 // disagreed with it -- a diagnostic of the pre-check's margins.
 // The binary64 bound solve of one cell (after any binary32 pre-check), binary32 pre-check of the
-// precision form included.
-template <int STAGE, typename FT, int NP, int VERIFY>
+// precision form included. OD: the first-order values may be formed on demand (Face::src.on);
+// instantiations that never do (the batched kernel) are compiled without that code.
+template <int STAGE, typename FT, int NP, int VERIFY, bool OD = false>
 __device__ __forceinline__ double theta_solve_inline(const Grid &g, const Eos &e, const Fields &q, const Cells32 &c32,
                                                      const Face<FT> &fh, const Face<FT> &gh,
                                                      const Face<FT> &fl, const Face<FT> &gl, double dt,
@@ -737,17 +767,37 @@ __device__ __forceinline__ double theta_solve_inline(const Grid &g, const Eos &e
     const FT idx = cst<FT>(g.inv_dx, g.inv_dxf), idy = cst<FT>(g.inv_dy, g.inv_dyf);
     constexpr int C0 = STAGE == 1 ? 5 : 0, C1 = STAGE == 0 ? 2 : 6;
     FT rh[6], rl[6];
+    // the first-order values of the four faces: formed here when the sweep left them unwritten
+    // (binary64 fused stage), else read
+    FT lxp[7], lxm[7], lyp[7], lym[7];
+    bool formed = false;
+    if constexpr (OD && sizeof(FT) == 8 && NP == 0) {
+        if (fl.src.on) {
+            low_flux_on_demand<0>(fl.src, kw, kf, lxp);
+            low_flux_on_demand<0>(fl.src, kx, kf - q.pitch, lxm);
+            low_flux_on_demand<1>(gl.src, kw, kf, lyp);
+            low_flux_on_demand<1>(gl.src, ky, kf - 1, lym);
+            formed = true;
+        }
+    }
 #pragma unroll
     for (int c = C0; c < C1; ++c) {
         rh[c] = div_sum(cf.xp(fh, fl, c) - cf.xm(fh, fl, c), idx, cf.yp(gh, gl, c) - cf.ym(gh, gl, c), idy);
-        rl[c] = div_sum(fl.f[c][kw] - fl.f[c][kx], idx, gl.f[c][kw] - gl.f[c][ky], idy);
+        if (formed)
+            rl[c] = div_sum(lxp[c] - lxm[c], idx, lyp[c] - lym[c], idy);
+        else
+            rl[c] = div_sum(fl.f[c][kw] - fl.f[c][kx], idx, gl.f[c][kw] - gl.f[c][ky], idy);
         if (c == 5) {
             FT a;
             if constexpr (sizeof(FT) == 4) a = to_f32(q.f[F_ALP][kf]);
             else a = q.f[F_ALP][kf];
             rh[c] = rh[c] - src_term(a, cf.xp(fh, fl, 6) - cf.xm(fh, fl, 6), idx) -
                     src_term(a, cf.yp(gh, gl, 6) - cf.ym(gh, gl, 6), idy);
-            rl[c] = rl[c] - src_term(a, fl.f[6][kw] - fl.f[6][kx], idx) - src_term(a, gl.f[6][kw] - gl.f[6][ky], idy);
+            if (formed)
+                rl[c] = rl[c] - src_term(a, lxp[6] - lxm[6], idx) - src_term(a, lyp[6] - lym[6], idy);
+            else
+                rl[c] = rl[c] - src_term(a, fl.f[6][kw] - fl.f[6][kx], idx) -
+                        src_term(a, gl.f[6][kw] - gl.f[6][ky], idy);
         }
     }
     if constexpr (sizeof(FT) == 4) {
@@ -782,17 +832,17 @@ __device__ __forceinline__ double theta_solve_inline(const Grid &g, const Eos &e
     return th;
 }
 
-template <int STAGE, int VERIFY>
+template <int STAGE, int VERIFY, bool OD>
 __device__ __noinline__ double theta_solve(const Grid &g, const Eos &e, const Fields &q, const Face<double> fh,
                                            const Face<double> gh, const Face<double> fl, const Face<double> gl,
                                            double dt, int i, int j, unsigned long long *verify, bool one)
 {
     double *const none[3] = {nullptr, nullptr, nullptr};
-    return theta_solve_inline<STAGE, double, 0, VERIFY>(g, e, q, Cells32{}, fh, gh, fl, gl, dt, none, i, j, verify,
-                                                         false, one);
+    return theta_solve_inline<STAGE, double, 0, VERIFY, OD>(g, e, q, Cells32{}, fh, gh, fl, gl, dt, none, i, j,
+                                                             verify, false, one);
 }
 
-template <int STAGE, typename FT, int NP = 0, int VERIFY = 0>
+template <int STAGE, typename FT, int NP = 0, int VERIFY = 0, bool OD = false>
 __device__ __forceinline__ double theta_body(const Grid &g, const Eos &e, const Fields &q, const Cells32 &c32,
                                              const Face<FT> &fh, const Face<FT> &gh,
                                              const Face<FT> &fl, const Face<FT> &gl, double dt,
@@ -806,7 +856,7 @@ __device__ __forceinline__ double theta_body(const Grid &g, const Eos &e, const 
         if (!VERIFY && one && prechecks) return 1.0;
         // the rare cells the pre-check leaves: out of line, so its registers do not hold down the
         // occupancy of the pass
-        return theta_solve<STAGE, VERIFY>(g, e, q, fh, gh, fl, gl, dt, i, j, verify, one);
+        return theta_solve<STAGE, VERIFY, OD>(g, e, q, fh, gh, fl, gl, dt, i, j, verify, one);
     } else {
         return theta_solve_inline<STAGE, FT, NP, VERIFY>(g, e, q, c32, fh, gh, fl, gl, dt, theta, i, j, verify,
                                                          prechecks);
@@ -814,8 +864,8 @@ __device__ __forceinline__ double theta_body(const Grid &g, const Eos &e, const 
 }
 
 // pp_blend_x_flux_kernel + pp_blend_y_flux_kernel (SC:1479-1548) in one launch: the thread at
-// (i, j) blends x-face (i, j) and y-face (i, j) when they exist.
-template <typename FT>
+// (i, j) blends x-face (i, j) and y-face (i, j) when they exist. OD as for theta_solve_inline.
+template <typename FT, bool OD = false>
 __device__ __forceinline__ void blend_body(const Grid &g, const Face<FT> &fh, const Face<FT> &gh,
                                            const Face<FT> &fl, const Face<FT> &gl,
                                            const FT *theta, int i, int j)
@@ -827,13 +877,32 @@ __device__ __forceinline__ void blend_body(const Grid &g, const Face<FT> &fh, co
     if (j >= g.g) {  // x face between (i, j) and (i+1, j)
         const FT t = face_theta_x(g, theta, kw, i);
         if (!(sizeof(FT) == 8 && keeps_high(t, fl.fin[kw] != 0))) {
+            if constexpr (OD && sizeof(FT) == 8) {
+                if (fl.src.on) {  // the first-order values formed here (binary64 fused stage)
+                    double low[7];
+                    low_flux_on_demand<0>(fl.src, kw, (long long)i * fl.src.pitch + j, low);
+#pragma unroll
+                    for (int c = 0; c < 7; ++c) fh.f[c][kw] = face_blend(low[c], fh.f[c][kw], t);
+                    goto y_face;
+                }
+            }
 #pragma unroll
             for (int c = 0; c < 7; ++c) fh.f[c][kw] = face_blend(fl.f[c][kw], fh.f[c][kw], t);
         }
     }
+y_face:
     if (i >= g.g) {  // y face between (i, j) and (i, j+1)
         const FT t = face_theta_y(g, theta, kw, j);
         if (!(sizeof(FT) == 8 && keeps_high(t, gl.fin[kw] != 0))) {
+            if constexpr (OD && sizeof(FT) == 8) {
+                if (gl.src.on) {
+                    double low[7];
+                    low_flux_on_demand<1>(gl.src, kw, (long long)i * gl.src.pitch + j, low);
+#pragma unroll
+                    for (int c = 0; c < 7; ++c) gh.f[c][kw] = face_blend(low[c], gh.f[c][kw], t);
+                    return;
+                }
+            }
 #pragma unroll
             for (int c = 0; c < 7; ++c) gh.f[c][kw] = face_blend(gl.f[c][kw], gh.f[c][kw], t);
         }
@@ -1245,8 +1314,9 @@ struct GlobalView {
 };
 
 // One face of the sweep in direction DIR: the face between cell (i, j) and its neighbour at +1
-// along the sweep. Callers guarantee that the face exists.
-template <int DIR, int VAR, int REC, typename T, typename V, typename FT>
+// along the sweep. Callers guarantee that the face exists. OD: the first-order values may be left to
+// their consumers (Face::src.on), only their finiteness byte written.
+template <int DIR, int VAR, int REC, typename T, bool OD = false, typename V, typename FT>
 __device__ __forceinline__ void face_body(const Eos &e, const V &v, const Face<FT> &hi, const Face<FT> &lo,
                                           bool do_high, bool do_low, long long kw)
 {
@@ -1260,20 +1330,40 @@ __device__ __forceinline__ void face_body(const Eos &e, const V &v, const Face<F
 
     if (do_low) {  // first-order HLLC of the two cell states (fx_low_kernel, SC:1303-1347)
         Side<T> L, R;
-        L.ar1 = U0[0]; L.ar2 = U0[1]; L.rho = U0[0] + U0[1];
-        L.un = v.un(0); L.ut = v.ut(0); L.p = v.lp(0); L.a = v.la(0); L.c = v.lc(0); L.E = v.lE(0);
-        R.ar1 = U1[0]; R.ar2 = U1[1]; R.rho = U1[0] + U1[1];
-        R.un = v.un(1); R.ut = v.ut(1); R.p = v.lp(1); R.a = v.la(1); R.c = v.lc(1); R.E = v.lE(1);
-        T f[6], us;
-        hllc<DIR>(L, R, f, us);
-        bool fin = finite_bits(FT(us));
+        first_order_side(U0[0], U0[1], v.un(0), v.ut(0), v.lp(0), v.la(0), v.lc(0), v.lE(0), L);
+        first_order_side(U1[0], U1[1], v.un(1), v.ut(1), v.lp(1), v.la(1), v.lc(1), v.lE(1), R);
+        bool done = false;
+        if constexpr (OD && sizeof(T) == 8 && sizeof(FT) == 8) {
+            if (lo.src.on) {
+                // binary64 fused stage: the values are formed on demand where the limiter reads
+                // them; here only their finiteness byte -- proved from the speeds where it can be
+                // (nearly every face), else from the values themselves: the same byte either way
+                T SL, SR, SP;
+                hllc_speeds(L, R, SL, SR, SP);
+                bool fin = hllc_surely_finite(L, R, SL, SR, SP);
+                if (!fin) {
+                    T f[6], us;
+                    hllc<DIR>(L, R, f, us);
+                    fin = finite_bits(FT(us));
 #pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            lo.f[c][kw] = FT(f[c]);
-            fin = fin && finite_bits(FT(f[c]));
+                    for (int c = 0; c < 6; ++c) fin = fin && finite_bits(FT(f[c]));
+                }
+                lo.fin[kw] = fin ? 1 : 0;
+                done = true;
+            }
         }
-        lo.f[6][kw] = FT(us);
-        if constexpr (sizeof(FT) == 8) lo.fin[kw] = fin ? 1 : 0;  // read by the binary64 limiter
+        if (!done) {
+            T f[6], us;
+            hllc<DIR>(L, R, f, us);
+            bool fin = finite_bits(FT(us));
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                lo.f[c][kw] = FT(f[c]);
+                fin = fin && finite_bits(FT(f[c]));
+            }
+            lo.f[6][kw] = FT(us);
+            if constexpr (sizeof(FT) == 8) lo.fin[kw] = fin ? 1 : 0;  // read by the binary64 limiter
+        }
     }
     if (!do_high) return;
 

@@ -515,6 +515,25 @@ int wm_get_dt(wm_handle *h, const wm_fields *q, double *dt, void *stream)
     return WM_OK;
 }
 
+// The binary64 form's first-order faces for the fused stage: the sweep writes only their finiteness
+// bytes, and the limiter's bound solve and blends form the values they read from the stage state's
+// partial densities and the preparation pass's first-order cell states (Face::src).
+static void on_demand_low(const wm_handle *h, const Fields &F, Face<double> &fl, Face<double> &gl)
+{
+    fl = h->fl;
+    gl = h->gl;
+    LowSrc s;
+    s.ar1 = F.f[F_AR1];
+    s.ar2 = F.f[F_AR2];
+    s.pitch = F.pitch;
+    s.lu = h->prep.lu; s.lv = h->prep.lv; s.lp = h->prep.lp;
+    s.la = h->prep.la; s.lc = h->prep.lc; s.lE = h->prep.lE;
+    s.nyg = h->g.nyg;
+    s.on = 1;
+    fl.src = s;
+    gl.src = s;
+}
+
 // One stage; `save_old` fuses copy_old, `dt_dev` (when non-null) replaces dt, `want_dt` appends
 // the time-step reduction of the updated state.
 static int run_stage(wm_handle *h, const Fields &F, const Fields &O, double dt, const double *dt_dev,
@@ -531,14 +550,18 @@ static int run_stage(wm_handle *h, const Fields &F, const Fields &O, double dt, 
         else
             launch_prep(h->g, h->e, F, h->prep, h->P.variant, s, h->prechecks);
     }
+    // binary64 with blends in place: first-order values formed on demand; with deferred blends the
+    // passes and the combine rebuild the blends from the stored values
+    const bool on_demand = !h->fp32 && !h->defer_limiter;
+    Face<double> fl = h->fl, gl = h->gl;
+    if (on_demand) on_demand_low(h, F, fl, gl);
     {
         ProfScope ps(h, WM_PROF_FACES, 2, s);
         if (h->fp32)
             launch_faces32(h->g, h->e, h->P.variant, h->P.recon, h->cells32, h->prep32, h->fh32,
                            h->gh32, h->fl32, h->gl32, true, true, s);
         else
-            launch_faces(h->g, h->e, h->P.variant, h->P.recon, F, h->prep, h->fh, h->gh, h->fl, h->gl,
-                         true, true, s);
+            launch_faces(h->g, h->e, h->P.variant, h->P.recon, F, h->prep, h->fh, h->gh, fl, gl, true, true, s);
     }
     {
         ProfScope ps(h, WM_PROF_LIMITER, h->defer_limiter ? 3 : 6, s);
@@ -546,7 +569,7 @@ static int run_stage(wm_handle *h, const Fields &F, const Fields &O, double dt, 
             launch_limiter(h->g, h->e, F, h->cells32, h->fh32, h->gh32, h->fl32, h->gl32, h->theta32, dt, dt_dev,
                            h->cnt, h->defer_limiter, s, nullptr, h->prechecks);
         else
-            launch_limiter(h->g, h->e, F, Cells32{}, h->fh, h->gh, h->fl, h->gl, h->theta, dt, dt_dev, h->cnt,
+            launch_limiter(h->g, h->e, F, Cells32{}, h->fh, h->gh, fl, gl, h->theta, dt, dt_dev, h->cnt,
                            h->defer_limiter, s, nullptr, h->prechecks);
     }
     unsigned flags = final_flags(h, alpha);
@@ -565,7 +588,8 @@ static int run_stage(wm_handle *h, const Fields &F, const Fields &O, double dt, 
             launch_final(h->g, h->e, flags, F, O, h->fh, h->gh, h->fl, h->gl, h->theta, h->defer_limiter,
                          dt, dt_dev, alpha, beta, h->cnt, s);
     }
-    h->fluxes_ready = h->low_ready = true;
+    h->fluxes_ready = true;
+    h->low_ready = !on_demand;  // formed on demand: the first-order arrays are left unwritten
     return check_launch("stage");
 }
 

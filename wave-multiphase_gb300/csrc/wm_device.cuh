@@ -979,18 +979,57 @@ template <typename T> struct Side {
 // LAZY_E: the sides carry Gamma and Pi instead of E, and hllc forms the total energy of the one side
 // its branch reads (L for the left and star-left fluxes, R for the others) by prim_to_energy's
 // expression -- the same value, for one side instead of two.
+// The wave speeds S_L, S_R and the contact speed S_P of hllc, the first part of it (shared, so that
+// a caller that needs only these gets hllc's own values).
+template <typename T>
+__device__ __forceinline__ void hllc_speeds(const Side<T> &L, const Side<T> &R, T &SL, T &SR, T &SP)
+{
+    T n_avg = half_of(L.un + R.un);
+    T c_avg = half_of(L.c + R.c);
+    SL = wmin(L.un - L.c, n_avg - c_avg);
+    SR = wmax(R.un + R.c, n_avg + c_avg);
+    T denom = L.rho * (SL - L.un) - R.rho * (SR - R.un);
+    if (abs_lt(denom, T(kTiny))) denom = T(kTiny);
+    SP = sw_div(R.p - L.p + L.rho * L.un * (SL - L.un) - R.rho * R.un * (SR - R.un), denom);
+}
+
+// |x| <= 2^60 and finite, |x| >= 2^-60: integer tests of a binary64's magnitude bits.
+__device__ __forceinline__ bool mag_at_most_2p60(double x)
+{
+    return ((unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull) <= 0x43B0000000000000ull;
+}
+__device__ __forceinline__ bool mag_at_least_2m60(double x)
+{
+    const unsigned long long m = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+    return m >= 0x3C30000000000000ull && m < 0x7ff0000000000000ull;
+}
+
+// True when hllc's outputs are certainly finite, from its inputs and its speeds: every side value
+// finite and at most 2^60 in magnitude, and each divisor hllc forms -- S_L - S_P and S_R - S_P (the
+// star ratios) and S_L - u_L, S_R - u_R (the star energies) -- at least 2^-60 in magnitude; its
+// contact-speed divisor is clamped to at least 1e-20. Then |S_L|, |S_R| <= 2^61, |S_P| < 2^251, the
+// ratios are below 2^122, the star energies below 2^563 and every flux component and u* below
+// 2^750, far from overflow: no infinity, and so no NaN, can arise. False otherwise (the caller then
+// forms the values).
+__device__ __forceinline__ bool hllc_surely_finite(const Side<double> &L, const Side<double> &R, double SL, double SR,
+                                                   double SP)
+{
+    bool ok = true;
+    const double v[18] = {L.ar1, L.ar2, L.rho, L.un, L.ut, L.p, L.a, L.c, L.E,
+                          R.ar1, R.ar2, R.rho, R.un, R.ut, R.p, R.a, R.c, R.E};
+#pragma unroll
+    for (int k = 0; k < 18; ++k) ok = ok && mag_at_most_2p60(v[k]);
+    return ok && mag_at_least_2m60(SL - L.un) && mag_at_least_2m60(SR - R.un) && mag_at_least_2m60(SL - SP) &&
+           mag_at_least_2m60(SR - SP);
+}
+
 template <int DIR, bool LAZY_E = false, typename T>
 __device__ __forceinline__ void hllc(const Side<T> &L, const Side<T> &R, T f[6], T &ustar)
 {
     constexpr int N = DIR == 0 ? 2 : 3;  // normal momentum component
     constexpr int Tc = DIR == 0 ? 3 : 2; // tangential momentum component
-    T n_avg = half_of(L.un + R.un);
-    T c_avg = half_of(L.c + R.c);
-    T SL = wmin(L.un - L.c, n_avg - c_avg);
-    T SR = wmax(R.un + R.c, n_avg + c_avg);
-    T denom = L.rho * (SL - L.un) - R.rho * (SR - R.un);
-    if (abs_lt(denom, T(kTiny))) denom = T(kTiny);
-    T SP = sw_div(R.p - L.p + L.rho * L.un * (SL - L.un) - R.rho * R.un * (SR - R.un), denom);
+    T SL, SR, SP;
+    hllc_speeds(L, R, SL, SR, SP);
     T ratioL, ratioR;
     sw_div2(SL - L.un, SL - SP, SR - R.un, SR - SP, ratioL, ratioR);
     T EL = L.E, ER = R.E;

@@ -134,7 +134,7 @@ __device__ __forceinline__ void staged_faces(const Grid &g, const Eos &e, const 
         v.bp = ti * S::cols(1) + tj;
         v.bs = ti * S::cols(3) + tj + 1;
     }
-    face_body<DIR, VAR, REC, T>(e, v, hi, lo, do_high != 0, do_low != 0, (long long)i * g.nyg + j);
+    face_body<DIR, VAR, REC, T, true>(e, v, hi, lo, do_high != 0, do_low != 0, (long long)i * g.nyg + j);
 }
 
 // Binary32 sweeps: registers capped for 8 resident blocks per SM (no spills; 64 registers instead
@@ -151,8 +151,8 @@ face_kernel(Grid g, Eos e, CS cs, PrepT<T> p, Face<FT> hi, Face<FT> lo, int do_h
         const int j = blockIdx.x * blockDim.x + threadIdx.x + (DIR == 0 ? g.g : g.g - 1);
         const int i = blockIdx.y * blockDim.y + threadIdx.y + (DIR == 0 ? g.g - 1 : g.g);
         if (i >= g.g + g.nx || j >= g.g + g.ny) return;
-        face_body<DIR, VAR, REC, T>(e, GlobalView<DIR, T, CS>(g, cs, p, i, j), hi, lo, do_high != 0, do_low != 0,
-                                    (long long)i * g.nyg + j);
+        face_body<DIR, VAR, REC, T, true>(e, GlobalView<DIR, T, CS>(g, cs, p, i, j), hi, lo, do_high != 0,
+                                          do_low != 0, (long long)i * g.nyg + j);
     } else {
         staged_faces<DIR, VAR, REC, T>(g, e, cs, p, hi, lo, do_high, do_low);
     }

@@ -19,9 +19,25 @@ enum { F_AR1 = 0, F_AR2, F_RU, F_RV, F_E, F_AL, F_U, F_V, F_P, F_ALP };
 // byte per face, written by the sweep that writes them: 1 when all seven first-order values of the
 // face are finite, else 0 -- what the limiter needs of a face it leaves unlimited (theta = 1), so
 // that it need not read the seven values there.
+// The inputs of the first-order flux of a face, for forming it on demand (the plain form's fused
+// stage: the sweep writes only the finiteness bytes, and the limiter's bound solve and blends form
+// the first-order values where they need them): the cells' partial densities (stage state, row
+// pitch `pitch`) and the preparation pass's first-order cell states (padded-grid rows of nyg).
+struct LowSrc {
+    const double *ar1 = nullptr, *ar2 = nullptr;
+    long long pitch = 0;
+    const double *lu = nullptr, *lv = nullptr, *lp = nullptr, *la = nullptr, *lc = nullptr, *lE = nullptr;
+    int nyg = 0;
+    int on = 0;  // 1: the f arrays are not written; form the values from these inputs
+};
 template <typename FT> struct Face {
     FT *f[7];
     unsigned char *fin = nullptr;
+};
+template <> struct Face<double> {
+    double *f[7];
+    unsigned char *fin = nullptr;
+    LowSrc src;  // first-order faces only: on-demand inputs (src.on = 1) instead of f
 };
 using Face7 = Face<double>;
 

@@ -85,8 +85,18 @@ __global__ void __launch_bounds__(BX *BY) sensor_kernel(Grid g, Eos e, Fields q,
 
 // Pass STAGE of the limiter; NP = STAGE rebuilds the blends of the earlier passes in registers
 // (fused stage), NP = 0 reads fh/gh as the in-place blend sweeps left them (closures).
+// Resident blocks per SM the limiter passes are compiled for (128 threads a block): passes 0 and 1
+// 16 (32 registers), pass 2 8 in binary64 with blends in place, where the rare cells that form the
+// first-order values on demand spill rather than every cell losing warps (64 registers), 10 in
+// binary32 (51), 6 for binary64 with deferred blends (85) -- the counts the passes had before.
+template <int STAGE, typename FT, int NP>
+constexpr int theta_min_blocks()
+{
+    return STAGE < 2 ? 16 : (sizeof(FT) == 4 ? 10 : (NP == 0 ? 8 : 6));
+}
+
 template <int STAGE, typename FT, int NP, int VERIFY = 0>
-__global__ void __launch_bounds__(BX *BY)
+__global__ void __launch_bounds__(BX *BY, (theta_min_blocks<STAGE, FT, NP>()))
 theta_kernel(Grid g, Eos e, Fields q, Cells32 c32, Face<FT> fh, Face<FT> gh, Face<FT> fl, Face<FT> gl,
              Theta3<FT> th3, double dt, const double *dt_dev, unsigned long long *limited,
              unsigned long long *verify, int prechecks)
@@ -95,20 +105,20 @@ theta_kernel(Grid g, Eos e, Fields q, Cells32 c32, Face<FT> fh, Face<FT> gh, Fac
     int i = blockIdx.y * blockDim.y + threadIdx.y + g.g;
     if (i >= g.g + g.nx || j >= g.g + g.ny) return;
     if (dt_dev) dt = *dt_dev;
-    double th = theta_body<STAGE, FT, NP, VERIFY>(g, e, q, c32, fh, gh, fl, gl, dt, th3.t, i, j, verify,
+    double th = theta_body<STAGE, FT, NP, VERIFY, true>(g, e, q, c32, fh, gh, fl, gl, dt, th3.t, i, j, verify,
                                                   prechecks != 0);
     th3.t[STAGE][kw_of(g, i, j)] = store_as<FT>(th);
     if (limited) count_if(limited, flt(th, 1.0));
 }
 
 template <typename FT>
-__global__ void __launch_bounds__(BX *BY)
+__global__ void __launch_bounds__(BX *BY, (sizeof(FT) == 8 ? 16 : 1))
 blend_kernel(Grid g, Face<FT> fh, Face<FT> gh, Face<FT> fl, Face<FT> gl, const FT *theta)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x + g.g - 1;
     int i = blockIdx.y * blockDim.y + threadIdx.y + g.g - 1;
     if (i >= g.g + g.nx || j >= g.g + g.ny) return;
-    blend_body(g, fh, gh, fl, gl, theta, i, j);
+    blend_body<FT, true>(g, fh, gh, fl, gl, theta, i, j);
 }
 
 template <typename FT, int NP>
