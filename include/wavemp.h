@@ -136,7 +136,10 @@ int wm_get_dt(wm_handle *h, const wm_fields *q, double *dt, void *stream);
 /* ---- fused forms ---------------------------------------------------------------------------- */
 /* One SSP-RK3 stage: apply_bc, compute_fluxes, compute_low_fluxes, limit_fluxes(dt),
  * rk3_update(alpha, beta, dt), enforce_admissible, update_prims -- the body of SC:2030-2055.
- * q_old may be NULL when alpha == 0. */
+ * q_old may be NULL when alpha == 0. In the binary64 form with blends in place (the default) the
+ * first-order fluxes are formed where the limiter reads them and are not stored: the WM_WS_FXL /
+ * WM_WS_GYL arrays are left as they were, and wm_limit_fluxes after this call returns WM_ERR_STATE
+ * until wm_compute_low_fluxes has run. */
 int wm_rhs_stage(wm_handle *h, const wm_fields *q, const wm_fields *q_old, double dt, double alpha,
                  double beta, void *stream);
 /* One SSP-RK3 step (SC:2033-2059): copy_old, three stages with (alpha, beta) = (0,1), (3/4,1/4),
@@ -324,7 +327,7 @@ int wm_check_sweep_arith(const unsigned long long *bits, long long n, long long 
  * (same padded shape, contiguous rows of ny + 2g). */
 #define WM_WS_FX 0      /* 7 arrays: high-order x fluxes 0..5 and srcx (after limit_fluxes: blended) */
 #define WM_WS_GY 7      /* 7 arrays: y fluxes and srcy */
-#define WM_WS_FXL 14    /* 7 arrays: first-order x fluxes and srcxl */
+#define WM_WS_FXL 14    /* 7 arrays: first-order x fluxes and srcxl (written by wm_compute_low_fluxes) */
 #define WM_WS_GYL 21    /* 7 arrays: first-order y fluxes and srcyl */
 #define WM_WS_THETA 28  /* 3 arrays: cell limiter factor of pass 0, 1, 2 */
 #define WM_WS_SIGMA_X 31

@@ -259,6 +259,9 @@ class Solver:
         return out
 
     def fluxes(self, which: str = "high") -> tuple[list, list]:
+        """The x and y face arrays of the workspace: "high" the high-order (after a limiter,
+        blended) fluxes, "low" the first-order ones of the last compute_low_fluxes -- a binary64
+        fused stage with blends in place forms those where the limiter reads them and stores none."""
         base_x, base_y = (_lib.WS_FX, _lib.WS_GY) if which == "high" else (_lib.WS_FXL, _lib.WS_GYL)
         return ([self.workspace(base_x + c) for c in range(7)],
                 [self.workspace(base_y + c) for c in range(7)])
