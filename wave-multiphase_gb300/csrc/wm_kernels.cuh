@@ -14,11 +14,6 @@ struct Fields {
 };
 enum { F_AR1 = 0, F_AR2, F_RU, F_RV, F_E, F_AL, F_U, F_V, F_P, F_ALP };
 
-// Six flux components and the interface velocity of one sweep direction; FT is the storage type
-// (double in the plain form, float in the precision form). The first-order arrays also carry one
-// byte per face, written by the sweep that writes them: 1 when all seven first-order values of the
-// face are finite, else 0 -- what the limiter needs of a face it leaves unlimited (theta = 1), so
-// that it need not read the seven values there.
 // The inputs of the first-order flux of a face, for forming it on demand (the plain form's fused
 // stage: the sweep writes only the finiteness bytes, and the limiter's bound solve and blends form
 // the first-order values where they need them): the cells' partial densities (stage state, row
@@ -30,6 +25,12 @@ struct LowSrc {
     int nyg = 0;
     int on = 0;  // 1: the f arrays are not written; form the values from these inputs
 };
+
+// Six flux components and the interface velocity of one sweep direction; FT is the storage type
+// (double in the plain form, float in the precision form). The first-order arrays also carry one
+// byte per face, written by the sweep that writes them: 1 when all seven first-order values of the
+// face are finite, else 0 -- what the limiter needs of a face it leaves unlimited (theta = 1), so
+// that it need not read the seven values there.
 template <typename FT> struct Face {
     FT *f[7];
     unsigned char *fin = nullptr;

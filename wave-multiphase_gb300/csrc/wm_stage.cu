@@ -105,12 +105,15 @@ theta_kernel(Grid g, Eos e, Fields q, Cells32 c32, Face<FT> fh, Face<FT> gh, Fac
     int i = blockIdx.y * blockDim.y + threadIdx.y + g.g;
     if (i >= g.g + g.nx || j >= g.g + g.ny) return;
     if (dt_dev) dt = *dt_dev;
-    double th = theta_body<STAGE, FT, NP, VERIFY, true>(g, e, q, c32, fh, gh, fl, gl, dt, th3.t, i, j, verify,
-                                                  prechecks != 0);
+    double th = theta_body<STAGE, FT, NP, VERIFY, true>(g, e, q, c32, fh, gh, fl, gl, dt, th3.t, i, j,
+                                                        verify, prechecks != 0);
     th3.t[STAGE][kw_of(g, i, j)] = store_as<FT>(th);
     if (limited) count_if(limited, flt(th, 1.0));
 }
 
+// Binary64: 16 resident blocks (32 registers). A face at theta = 1 reads its factor and byte only;
+// the few at theta < 1 that form their first-order values on demand spill instead of every face
+// losing warps.
 template <typename FT>
 __global__ void __launch_bounds__(BX *BY, (sizeof(FT) == 8 ? 16 : 1))
 blend_kernel(Grid g, Face<FT> fh, Face<FT> gh, Face<FT> fl, Face<FT> gl, const FT *theta)
