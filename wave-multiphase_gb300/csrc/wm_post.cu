@@ -15,6 +15,7 @@
 // [1, 2400] through a nine-step blue ramp (ColorBrewer "Blues", the anchors of matplotlib's Blues),
 // with the alpha1 = 0.5 level marked red where alpha1 - 0.5 changes sign towards the next cell in
 // x or y; and alpha1 in inverted grey (0 white, 1 black).
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 
@@ -265,6 +266,98 @@ extern "C" int wm_schlieren(const wm_fields *q, int nx, int ny, int g, const dou
     if (e != cudaSuccess) {
         char msg[200];
         snprintf(msg, sizeof msg, "wm_schlieren: %s", cudaGetErrorString(e));
+        wm::set_error_text(msg);
+        return WM_ERR_CUDA;
+    }
+    return WM_OK;
+}
+
+namespace {
+
+// n 16-byte words from src to dst by the SMs, four loads in flight per thread before its stores
+// (latency of a host-side operand read over the chip-to-chip link hidden by the loads in flight).
+__global__ void __launch_bounds__(256) state_copy_kernel(uint4 *__restrict__ dst, const uint4 *__restrict__ src,
+                                                         long long n)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; k + 3 * stride < n; k += 4 * stride) {
+        const uint4 a = src[k], b = src[k + stride], c = src[k + 2 * stride], d = src[k + 3 * stride];
+        dst[k] = a;
+        dst[k + stride] = b;
+        dst[k + 2 * stride] = c;
+        dst[k + 3 * stride] = d;
+    }
+    for (; k < n; k += stride) dst[k] = src[k];
+}
+
+// The address a kernel uses for p: p itself for device or managed memory, the mapped address of
+// page-locked host memory; nullptr for memory the device cannot address that way. `kind` receives
+// the memory type.
+const char *device_view(const void *p, int &kind)
+{
+    cudaPointerAttributes a;
+    kind = -1;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    kind = (int)a.type;
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return static_cast<const char *>(p);
+    if (a.type == cudaMemoryTypeHost) {
+        void *d = nullptr;
+        if (cudaHostGetDevicePointer(&d, const_cast<void *>(p), 0) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        return static_cast<const char *>(d);
+    }
+    return nullptr;
+}
+
+// Device view of the range [p, p + bytes): both ends in memory of the same kind that maps to one
+// contiguous device range, else nullptr.
+const char *range_view(const void *p, long long bytes)
+{
+    int k0, k1;
+    const char *d0 = device_view(p, k0);
+    const char *d1 = device_view(static_cast<const char *>(p) + (bytes - 1), k1);
+    if (!d0 || !d1 || k0 != k1 || d1 - d0 != bytes - 1) return nullptr;
+    return d0;
+}
+
+}  // namespace
+
+extern "C" int wm_copy_state(void *dst, const void *src, long long bytes, void *stream)
+{
+    if (!dst || !src || bytes < 0 || bytes % 16 != 0 || (reinterpret_cast<uintptr_t>(dst) & 15) ||
+        (reinterpret_cast<uintptr_t>(src) & 15)) {
+        wm::set_error_text("wm_copy_state: addresses must be 16-byte aligned and bytes a multiple of 16");
+        return WM_ERR_INVALID;
+    }
+    if (bytes == 0) return WM_OK;
+    const char *d = range_view(dst, bytes), *s = range_view(src, bytes);
+    if (!d || !s) {
+        wm::set_error_text("wm_copy_state: a buffer is neither device memory nor page-locked host memory "
+                           "mapped for the device over its whole range");
+        return WM_ERR_INVALID;
+    }
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+        cudaGetLastError();
+        wm::set_error_text("wm_copy_state: no CUDA device");
+        return WM_ERR_CUDA;
+    }
+    const long long n = bytes / 16;
+    // 4 resident blocks of 256 a SM (64 registers): one wave, four 16-byte loads in flight a thread
+    const long long blocks = std::min<long long>((n + 255) / 256, 4LL * sms);
+    state_copy_kernel<<<(unsigned)blocks, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+        reinterpret_cast<uint4 *>(const_cast<char *>(d)), reinterpret_cast<const uint4 *>(s), n);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        char msg[200];
+        snprintf(msg, sizeof msg, "wm_copy_state: %s", cudaGetErrorString(e));
         wm::set_error_text(msg);
         return WM_ERR_CUDA;
     }

@@ -76,7 +76,7 @@ EXPORTS = ("wm_version", "wm_last_error", "wm_workspace_bytes", "wm_create", "wm
            "wm_solve_workspace_bytes", "wm_batch_create", "wm_batch_destroy", "wm_batch_set",
            "wm_batch_clear", "wm_batch_init_dt", "wm_batch_run", "wm_batch_query",
            "wm_batch_tile_shape", "wm_batch_scalars", "wm_batch_info", "wm_batch_profile",
-           "wm_batch_profile_read", "wm_schlieren", "wm_run", "wm_run_uses_graph",
+           "wm_batch_profile_read", "wm_schlieren", "wm_copy_state", "wm_run", "wm_run_uses_graph",
            "wm_set_limiter_sweeps", "wm_batch_dt_log", "wm_verify_limiter_precheck",
            "wm_check_conversions", "wm_set_prechecks", "wm_verify_switch_precheck",
            "wm_check_sweep_arith", "wm_batch_spin_limit", "wm_verify_ducros_precheck")
@@ -144,6 +144,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     L.wm_batch_info.argtypes = [vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)]
     L.wm_batch_profile.argtypes = [vp, i]
     L.wm_schlieren.argtypes = [F, i, i, i, vp, vp, d, d, vp, vp, vp, vp]
+    L.wm_copy_state.argtypes = [vp, vp, ctypes.c_longlong, vp]
     L.wm_run.argtypes = [vp, F, F, ctypes.POINTER(WmSchedule), ctypes.c_longlong, vp]
     L.wm_run_uses_graph.argtypes = [vp]
     L.wm_set_limiter_sweeps.argtypes = [vp, i]

@@ -284,6 +284,19 @@ class Solver:
         return {k: getattr(st, k) for k, _ in _lib.WmStats._fields_}
 
 
+def copy_state(dst: torch.Tensor, src: torch.Tensor):
+    """dst <- src by the SMs (wm_copy_state): contiguous tensors of the same size in bytes, each on
+    the device or in page-locked host memory (pin_memory), asynchronous on the current stream."""
+    if not (dst.is_contiguous() and src.is_contiguous()):
+        raise ValueError("copy_state needs contiguous tensors")
+    nbytes = dst.numel() * dst.element_size()
+    if src.numel() * src.element_size() != nbytes:
+        raise ValueError("copy_state: sizes differ")
+    L = _lib.load()
+    _lib.check(L.wm_copy_state(ctypes.c_void_p(dst.data_ptr()), ctypes.c_void_p(src.data_ptr()), nbytes,
+                               _stream()), "copy_state")
+
+
 def probe_fp64_flops() -> float:
     L = _lib.load()
     v = ctypes.c_double()
