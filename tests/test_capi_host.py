@@ -2,8 +2,8 @@
 for both forms, the batch's per-solve size within the handle's, so that wavemp.batch.Batch.add
 gives wm_batch_set enough), argument validation (every rejected parameter returns 0 bytes and
 WM_ERR_INVALID from wm_create, before any CUDA call), a caller workspace that is too small or
-misaligned (WM_ERR_NOMEM, before the library touches it), and the Python parameter checks. No
-kernel is launched and no device memory is allocated."""
+misaligned (WM_ERR_NOMEM, before the library touches it), wm_copy_state's argument checks, and the
+Python parameter checks. No kernel is launched and no device memory is allocated."""
 import ctypes
 import math
 import os
@@ -150,3 +150,24 @@ def test_static_stage_refuses_the_precision_form_and_large_grids(lib):
     assert lib.wm_rhs_stage_static(ctypes.byref(p), 16, 16, 5, ctypes.byref(empty), None,
                                    1e-6, 0.0, 1.0, None) == WM_ERR_INVALID
     assert b"invalid field pointers" in lib.wm_last_error()
+
+
+def test_copy_state_argument_checks(lib):
+    """wm_copy_state refuses null or unaligned addresses, sizes that are not a multiple of 16 and
+    negative sizes before any CUDA call, and does nothing for 0 bytes; without a device no buffer
+    can be mapped, so even an aligned copy is refused before any launch."""
+    import numpy as np
+    import torch
+
+    buf = np.zeros(128, dtype=np.float64)
+    a = buf.ctypes.data
+    a16 = a + (-a) % 16  # 16-byte aligned, inside buf with 512 bytes after it
+    vp = ctypes.c_void_p
+    assert lib.wm_copy_state(vp(a16), vp(a16 + 256), 24, None) == WM_ERR_INVALID
+    assert lib.wm_copy_state(vp(a16 + 8), vp(a16 + 256), 16, None) == WM_ERR_INVALID
+    assert lib.wm_copy_state(vp(a16), vp(a16 + 264), 16, None) == WM_ERR_INVALID
+    assert lib.wm_copy_state(vp(a16), vp(a16 + 256), -16, None) == WM_ERR_INVALID
+    assert lib.wm_copy_state(None, vp(a16), 16, None) == WM_ERR_INVALID
+    assert lib.wm_copy_state(vp(a16), vp(a16 + 256), 0, None) == 0
+    if not torch.cuda.is_available():
+        assert lib.wm_copy_state(vp(a16), vp(a16 + 256), 64, None) == WM_ERR_INVALID
