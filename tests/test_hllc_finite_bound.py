@@ -149,3 +149,11 @@ def test_specials():
             L[f] = np.full(n, bad)
             ok, _ = check(L, R)
             assert not ok.any(), (f, bad)
+
+
+def test_bit_thresholds_are_the_stated_powers():
+    # mag_at_most_2p60 / mag_at_least_2m60 (csrc/wm_device.cuh) compare the magnitude's bits with
+    # these two patterns and with the exponent field of infinity
+    assert np.float64(2.0 ** 60).view(np.uint64) == 0x43B0000000000000
+    assert np.float64(2.0 ** -60).view(np.uint64) == 0x3C30000000000000
+    assert np.float64(np.inf).view(np.uint64) == 0x7FF0000000000000
