@@ -14,7 +14,7 @@ import pytest
 pytestmark = pytest.mark.skipif(shutil.which("nvcc") is None and not os.path.exists("/usr/local/cuda/bin/nvcc"),
                                 reason="needs nvcc to build the library")
 
-WM_ERR_INVALID, WM_ERR_NOMEM = -1, -3
+WM_ERR_INVALID, WM_ERR_CUDA, WM_ERR_NOMEM = -1, -2, -3
 
 
 @pytest.fixture(scope="module")
@@ -154,8 +154,8 @@ def test_static_stage_refuses_the_precision_form_and_large_grids(lib):
 
 def test_copy_state_argument_checks(lib):
     """wm_copy_state refuses null or unaligned addresses, sizes that are not a multiple of 16 and
-    negative sizes before any CUDA call, and does nothing for 0 bytes; without a device no buffer
-    can be mapped, so even an aligned copy is refused before any launch."""
+    negative sizes before any CUDA call, and does nothing for 0 bytes; without a device even an
+    aligned copy returns an error before any launch."""
     import numpy as np
     import torch
 
@@ -170,4 +170,4 @@ def test_copy_state_argument_checks(lib):
     assert lib.wm_copy_state(None, vp(a16), 16, None) == WM_ERR_INVALID
     assert lib.wm_copy_state(vp(a16), vp(a16 + 256), 0, None) == 0
     if not torch.cuda.is_available():
-        assert lib.wm_copy_state(vp(a16), vp(a16 + 256), 64, None) == WM_ERR_INVALID
+        assert lib.wm_copy_state(vp(a16), vp(a16 + 256), 64, None) == WM_ERR_CUDA

@@ -291,10 +291,10 @@ __global__ void __launch_bounds__(256) state_copy_kernel(uint4 *__restrict__ dst
     for (; k < n; k += stride) dst[k] = src[k];
 }
 
-// The address a kernel uses for p: p itself for device or managed memory, the mapped address of
-// page-locked host memory; nullptr for memory the device cannot address that way. `kind` receives
-// the memory type.
-const char *device_view(const void *p, int &kind)
+// The address a kernel on device `dev` uses for p: p itself for managed memory and for device memory
+// of `dev`, the mapped address of page-locked host memory; nullptr for memory that device cannot
+// address that way (another device's memory included). `kind` receives the memory type.
+const char *device_view(const void *p, int dev, int &kind)
 {
     cudaPointerAttributes a;
     kind = -1;
@@ -303,7 +303,8 @@ const char *device_view(const void *p, int &kind)
         return nullptr;
     }
     kind = (int)a.type;
-    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return static_cast<const char *>(p);
+    if (a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeDevice && a.device == dev))
+        return static_cast<const char *>(p);
     if (a.type == cudaMemoryTypeHost) {
         void *d = nullptr;
         if (cudaHostGetDevicePointer(&d, const_cast<void *>(p), 0) != cudaSuccess) {
@@ -317,11 +318,11 @@ const char *device_view(const void *p, int &kind)
 
 // Device view of the range [p, p + bytes): both ends in memory of the same kind that maps to one
 // contiguous device range, else nullptr.
-const char *range_view(const void *p, long long bytes)
+const char *range_view(const void *p, long long bytes, int dev)
 {
     int k0, k1;
-    const char *d0 = device_view(p, k0);
-    const char *d1 = device_view(static_cast<const char *>(p) + (bytes - 1), k1);
+    const char *d0 = device_view(p, dev, k0);
+    const char *d1 = device_view(static_cast<const char *>(p) + (bytes - 1), dev, k1);
     if (!d0 || !d1 || k0 != k1 || d1 - d0 != bytes - 1) return nullptr;
     return d0;
 }
@@ -336,18 +337,18 @@ extern "C" int wm_copy_state(void *dst, const void *src, long long bytes, void *
         return WM_ERR_INVALID;
     }
     if (bytes == 0) return WM_OK;
-    const char *d = range_view(dst, bytes), *s = range_view(src, bytes);
-    if (!d || !s) {
-        wm::set_error_text("wm_copy_state: a buffer is neither device memory nor page-locked host memory "
-                           "mapped for the device over its whole range");
-        return WM_ERR_INVALID;
-    }
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
         cudaGetLastError();
         wm::set_error_text("wm_copy_state: no CUDA device");
         return WM_ERR_CUDA;
+    }
+    const char *d = range_view(dst, bytes, dev), *s = range_view(src, bytes, dev);
+    if (!d || !s) {
+        wm::set_error_text("wm_copy_state: a buffer is neither memory of the current device nor page-locked "
+                           "host memory mapped for it over its whole range");
+        return WM_ERR_INVALID;
     }
     const long long n = bytes / 16;
     // 4 resident blocks of 256 a SM (64 registers): one wave, four 16-byte loads in flight a thread
