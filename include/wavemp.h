@@ -306,9 +306,10 @@ int wm_schlieren(const wm_fields *q, int nx, int ny, int g, const double *xh, co
  * state transfers, which the reference makes with wp.copy of wp.array(host) (SC:1877-1886) and
  * .numpy() (SC:2004-2007). Each side is memory of the current device, managed memory, or
  * page-locked host memory (cudaHostAlloc / cudaHostRegister; torch's pin_memory), read or written
- * in place through its mapped address. Both addresses 16-byte aligned and bytes a multiple of 16; a buffer the device
- * cannot address that way over its whole range is refused (WM_ERR_INVALID) before any launch;
- * WM_ERR_CUDA without a usable device.
+ * in place through its mapped address. Both addresses 16-byte aligned and bytes a multiple of 16.
+ * Refused before any launch (WM_ERR_INVALID): a first or last byte of a range that is not in such
+ * memory, or not in memory of one kind; a range that runs past its allocation into an adjacent one
+ * is the caller's error, as for cudaMemcpyAsync. WM_ERR_CUDA without a usable device.
  * Asynchronous on `stream`. No counterpart in the reference's kernels. */
 int wm_copy_state(void *dst, const void *src, long long bytes, void *stream);
 

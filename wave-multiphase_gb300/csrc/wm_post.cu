@@ -317,7 +317,8 @@ const char *device_view(const void *p, int dev, int &kind)
 }
 
 // Device view of the range [p, p + bytes): both ends in memory of the same kind that maps to one
-// contiguous device range, else nullptr.
+// contiguous device range, else nullptr. The ends only: a range that runs past its allocation into
+// an adjacent one of the same kind is not detected.
 const char *range_view(const void *p, long long bytes, int dev)
 {
     int k0, k1;
